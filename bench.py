@@ -1,0 +1,269 @@
+#!/usr/bin/env python3
+"""Benchmark of the GeothermalWells.jl time-step hot path on GB300.
+
+Workload: the large single coaxial well, 205 x 205 x 2002 = 8.41e7 cells,
+dt = 300 s (ROCK2 z-diffusion + ADI x/y line solves + semi-Lagrangian pipe
+advection per step).  One bench step = one time step of the whole grid.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+                  [--impl ours|reference]
+
+The default arm times the fused device path (gw_step, graph-captured) with
+CUDA events on the library's stream; `e2e` times the same steps through the
+public solve() path with host buffers (field upload, steps, outlet series and
+final field download).  `--impl reference` times the CPU FP64 restatement of
+the reference (the oracle) on the host cores.  With N > 1 GPUs each rank runs
+an independent replica of the well (the single-well step does not shard).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "geothermalwells.jl_gb300"))
+
+METRIC = "Mcell-steps/s"
+WORD = {"fp64": 8, "mixed": 4}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--workload", default="large", choices=["large", "2mm"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample-steps", type=int, default=1)
+    return p.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(name):
+    from geothermalwells_gb300 import workloads as W
+    return W.single_well_large() if name == "large" else W.single_well_2mm()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks_%d.csv" % os.getpid())
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0])); mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, world, local, dist
+    return 0, 1, 0, None
+
+
+def cpu_baseline(w, sample_steps):
+    """The oracle (CPU FP64 restatement of the reference) on all host cores,
+    timed on a bounded sample: sample_steps full time steps of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from geothermalwells_gb300 import rock2
+    cores = O.set_threads(os.cpu_count() or 1)
+    orc = O.Oracle(w["gridx"], w["gridy"], w["gridz"], w["boreholes"], w["materials"],
+                   w["inlet_model"])
+    s, _ = rock2.choose_stages(w["dt"], orc.eigen_estimate())
+    u = w["T0"].copy(order="F")
+    t0 = time.perf_counter()
+    orc.simulate(u, 0.0, w["dt"], sample_steps, s, rock2.coefficients(s))
+    el = time.perf_counter() - t0
+    ncell = u.size
+    return {"value": ncell * sample_steps / el / 1e6, "unit": METRIC, "cores": cores,
+            "kind": "port",
+            "sample": "%d full time step(s) of the %s workload (%d cells), oracle OpenMP"
+                      % (sample_steps, w["name"], ncell),
+            "seconds": el}
+
+
+def run_reference(args):
+    rank, world, local, dist = dist_init(args)
+    if rank != 0:
+        return
+    w = workload(args.workload)
+    steps = max(1, min(args.steps, 2))
+    cb = cpu_baseline(w, steps)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": METRIC,
+            "n_gpus": args.gpus, "steps": steps, "warmup": 0, "ms_per_step": cb["seconds"] * 1e3 / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": w["name"], "cells": int(w["T0"].size),
+                                            "dt_s": w["dt"], "timed_steps_of_requested": [steps, args.steps]},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    rank, world, local, dist = dist_init(args)
+    from geothermalwells_gb300 import _lib, create_cache, GB300
+    L = _lib.load()
+    w = workload(args.workload)
+    cache = create_cache(backend=GB300(device=local, precision=args.precision), gridx=w["gridx"],
+                         gridy=w["gridy"], gridz=w["gridz"], materials=w["materials"],
+                         boreholes=w["boreholes"], inlet_model=w["inlet_model"])
+    ncell = cache.N
+    dt = w["dt"]
+    import ctypes
+    s, cov = ctypes.c_int(), ctypes.c_int()
+    _lib.check(L.gw_rock2_stages(cache.ctx, dt, 100, ctypes.byref(s), ctypes.byref(cov)))
+    cache.set_field(w["T0"])
+    # warm-up (also builds the CUDA graph)
+    _lib.check(L.gw_step(cache.ctx, 0.0, dt, args.warmup, 100))
+    if dist:
+        dist.barrier()
+    clocks = Clocks(local)
+    _lib.check(L.gw_step(cache.ctx, args.warmup * dt, dt, args.steps, 100))
+    ms = ctypes.c_double()
+    _lib.check(L.gw_get_last_step_time(cache.ctx, ctypes.byref(ms)))
+    ck = clocks.stop()
+    t_ms = ms.value
+    if dist:
+        import torch
+        tt = torch.tensor([t_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    value = ncell * args.steps * world / (t_ms / 1e3) / 1e6
+
+    # per-kernel timing for the roofline of the dominant kernel
+    prof = (ctypes.c_double * 5)()
+    _lib.check(L.gw_profile_kernels(cache.ctx, dt, 3, prof))
+    kms = dict(zip(_lib.KERNELS, list(prof)))
+    wb = 8  # the double path moves 8-byte words
+    ncolz = (cache.countxy_inner + cache.countxy_outer) * cache.countz
+    alg = {"zstage": 3 * wb * ncell, "explicit": 2 * wb * ncell, "thomas_x": 2 * wb * ncell,
+           "thomas_y": 2 * wb * ncell, "advection": 2 * wb * ncolz}
+    per_step = {"zstage": s.value, "explicit": 2, "thomas_x": 1, "thomas_y": 1, "advection": 2}
+    share = {k: kms[k] * per_step[k] for k in kms}
+    dom = max(share, key=share.get)
+    peak, peak_kind = peaks()
+    achieved = alg[dom] / (kms[dom] / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_per_cell.json")
+    if os.path.exists(tpath):
+        tr = json.load(open(tpath)).get(args.precision, {}).get(dom)
+        if tr is not None:
+            traffic = tr * (ncolz if dom == "advection" else ncell)
+
+    # end to end through the public path with host buffers (pinned)
+    e2e = None
+    try:
+        import torch
+        pin = torch.empty(ncell, dtype=torch.float64, pin_memory=True).numpy()
+    except Exception:
+        pin = np.empty(ncell)
+    pin[:] = np.asfortranarray(w["T0"]).ravel(order="F")
+    out_pin = np.empty_like(pin)
+    series = np.zeros(args.steps * cache.N_bh)
+    t0 = time.perf_counter()
+    _lib.check(L.gw_set_field(cache.ctx, _lib.dptr(pin)))
+    _lib.check(L.gw_step(cache.ctx, 0.0, dt, args.steps, 100))
+    _lib.check(L.gw_get_outlet_series(cache.ctx, _lib.dptr(series), args.steps))
+    _lib.check(L.gw_get_field(cache.ctx, _lib.dptr(out_pin)))
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        import torch
+        tt = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = {"value": ncell * args.steps * world / e2e_s / 1e6, "unit": METRIC,
+           "h2d_bytes_per_step": 8 * ncell / args.steps,
+           "d2h_bytes_per_step": (8 * ncell + 8 * args.steps * cache.N_bh) / args.steps,
+           "path": "gw_set_field + gw_step(K) + gw_get_outlet_series + gw_get_field, pinned host"}
+    if rank != 0:
+        return
+    cb = None
+    if not args.no_cpu_baseline and world == 1:
+        cb = cpu_baseline(w, args.cpu_sample_steps)
+        cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    launches_per_step = s.value + 2 * 1 + 2 + 2 * 4 + 1
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64acc", "data": "synthetic",
+        "config": {"workload": w["name"], "cells": ncell, "dt_s": dt, "rock2_stages": s.value,
+                   "precision": args.precision, "l2": "inputs larger than L2 (field %.0f MB)"
+                   % (ncell * 8 / 1e6), "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel_ms": kms,
+                     "alg_bytes_per_launch": alg[dom]},
+        "cpu_baseline": cb, "e2e": e2e, "gpu_launches": launches_per_step * args.steps,
+        "clocks": ck,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

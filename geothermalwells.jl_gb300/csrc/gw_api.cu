@@ -1,0 +1,432 @@
+// gw_api.cu -- the extern "C" entry points declared in include/gw_gb300.h.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gw_internal.h"
+
+namespace {
+thread_local std::string g_err;
+
+template <typename T>
+int dalloc(gw_ctx *c, T **p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) return gw_cuda_fail(e, "cudaMalloc");
+    c->allocations.push_back((void *)*p);
+    c->device_bytes += (long long)(n * sizeof(T));
+    return GW_OK;
+}
+
+template <typename T>
+int upload(gw_ctx *c, T **p, const std::vector<T> &v) {
+    int rc = dalloc(c, p, v.size());
+    if (rc) return rc;
+    if (!v.empty()) GW_CUDA(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return GW_OK;
+}
+
+size_t ncell(const gw_ctx *c) { return (size_t)c->nx * c->ny * c->nz; }
+
+int set_device(gw_ctx *c) {
+    GW_CUDA(cudaSetDevice(c->device));
+    return GW_OK;
+}
+
+int sync(gw_ctx *c) {
+    GW_CUDA(cudaStreamSynchronize(c->stream));
+    return GW_OK;
+}
+
+// One ROCK2 step on u (stage count s, step dt) using buffers {u, g1, spare}.
+// Each stage reads its stencil input and, pointwise, the stage before it, so
+// the output may overwrite the older stage; the last stage lands in u.
+int rock2_step(gw_ctx *c, double *u, double *g1, double *spare, double dt, int s) {
+    const double *mu, *nu, *kappa;
+    double sigma, tau;
+    gw_rock2_coefs(s, &mu, &nu, &kappa, &sigma, &tau);
+    double *pool[3] = {u, g1, spare};
+    int cur = 0, prev = -1, rc;
+    auto pick = [&](int a, int b) {
+        for (int q = 0; q < 3; ++q)
+            if (q != a && q != b) return q;
+        return -1;
+    };
+    for (int j = 1; j <= s - 2; ++j) {
+        int out = prev >= 0 ? prev : pick(cur, 0);
+        double kap = j == 1 ? 0.0 : kappa[j - 1];
+        rc = gw_launch_zstage(c, pool[out], pool[cur], prev >= 0 ? pool[prev] : nullptr,
+                              dt * mu[j - 1], kap, 0);
+        if (rc) return rc;
+        prev = cur;
+        cur = out;
+    }
+    // finishing procedure: gq = gp + h sigma A gp, then
+    // y = gq + (h tau / sigma) A gq + (1 - tau / sigma^2) (gq - gp), written into u
+    int gp = cur;
+    int gq = pick(gp, 0);
+    rc = gw_launch_zstage(c, pool[gq], pool[gp], nullptr, dt * sigma, 0.0, 0);
+    if (rc) return rc;
+    return gw_launch_zstage(c, pool[0], pool[gq], pool[gp], dt * tau / sigma,
+                            1.0 - tau / (sigma * sigma), 0);
+}
+
+// ADI_and_ADV_callback! (src/solver.jl:432-464)
+// The Thomas factors for h = dt/2 must be current (gw_ensure_factors).
+int adi_adv(gw_ctx *c, double *u, double *temp, double dt) {
+    int rc;
+    if ((rc = gw_launch_explicit(c, temp, u, dt / 2, GW_DIR_Y))) return rc;
+    if ((rc = gw_launch_advection(c, temp, dt / 2))) return rc;
+    if ((rc = gw_launch_thomas(c, u, temp, GW_DIR_X))) return rc;
+    if ((rc = gw_launch_explicit(c, temp, u, dt / 2, GW_DIR_X))) return rc;
+    if ((rc = gw_launch_advection(c, temp, dt / 2))) return rc;
+    return gw_launch_thomas(c, u, temp, GW_DIR_Y);
+}
+
+int check_field_ptrs(const void *a, const void *b) {
+    if (!a || !b) return gw_fail(GW_ERR_ARG, "field pointer is NULL");
+    return GW_OK;
+}
+}  // namespace
+
+int gw_fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+int gw_cuda_fail(cudaError_t e, const char *what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return GW_ERR_CUDA;
+}
+
+// Recompute the Thomas factors of (I - h A_x) and (I - h A_y) when h changes.
+int gw_ensure_factors(gw_ctx *c, double h) {
+    if (h == c->factors_h) return GW_OK;
+    std::vector<double> cxm, cxp, cym, cyp, czm, czp;
+    gw_build_coefs(c, cxm, cxp, cym, cyp, czm, czp);
+    std::vector<double> a, ib, cu;
+    GW_CUDA(cudaStreamSynchronize(c->stream));
+    gw_build_factors(c, h, GW_DIR_X, cxm, cxp, a, ib, cu);
+    GW_CUDA(cudaMemcpy(c->c64.fx.a, a.data(), a.size() * 8, cudaMemcpyHostToDevice));
+    GW_CUDA(cudaMemcpy(c->c64.fx.ib, ib.data(), ib.size() * 8, cudaMemcpyHostToDevice));
+    GW_CUDA(cudaMemcpy(c->c64.fx.cu, cu.data(), cu.size() * 8, cudaMemcpyHostToDevice));
+    gw_build_factors(c, h, GW_DIR_Y, cym, cyp, a, ib, cu);
+    GW_CUDA(cudaMemcpy(c->c64.fy.a, a.data(), a.size() * 8, cudaMemcpyHostToDevice));
+    GW_CUDA(cudaMemcpy(c->c64.fy.ib, ib.data(), ib.size() * 8, cudaMemcpyHostToDevice));
+    GW_CUDA(cudaMemcpy(c->c64.fy.cu, cu.data(), cu.size() * 8, cudaMemcpyHostToDevice));
+    c->factors_h = h;
+    return GW_OK;
+}
+
+extern "C" {
+
+const char *gw_last_error(void) { return g_err.c_str(); }
+
+const char *gw_version(void) { return "gw_gb300 0.1 (sm_103a)"; }
+
+int gw_create(const gw_desc *desc, gw_ctx **out) {
+    if (!out) return gw_fail(GW_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    gw_ctx *c = new gw_ctx();
+    int rc = gw_setup_host(c, desc);
+    if (rc) { delete c; return rc; }
+    if (c->nbh > 1024) { delete c; return gw_fail(GW_ERR_ARG, "at most 1024 boreholes"); }
+    c->device = desc->device;
+    auto fail = [&](int r) { gw_destroy(c); return r; };
+    if ((rc = set_device(c))) return fail(rc);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(gw_cuda_fail(e, "cudaStreamCreate"));
+    if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess)
+        return fail(gw_cuda_fail(e, "cudaEventCreate"));
+
+    std::vector<double> cxm, cxp, cym, cyp, czm, czp;
+    gw_build_coefs(c, cxm, cxp, cym, cyp, czm, czp);
+    if ((rc = upload(c, &c->c64.cxm, cxm)) || (rc = upload(c, &c->c64.cxp, cxp)) ||
+        (rc = upload(c, &c->c64.cym, cym)) || (rc = upload(c, &c->c64.cyp, cyp)) ||
+        (rc = upload(c, &c->c64.czm, czm)) || (rc = upload(c, &c->c64.czp, czp)))
+        return fail(rc);
+    if ((rc = dalloc(c, &c->c64.fx.a, cxm.size())) || (rc = dalloc(c, &c->c64.fx.ib, cxm.size())) ||
+        (rc = dalloc(c, &c->c64.fx.cu, cxm.size())) || (rc = dalloc(c, &c->c64.fy.a, cym.size())) ||
+        (rc = dalloc(c, &c->c64.fy.ib, cym.size())) || (rc = dalloc(c, &c->c64.fy.cu, cym.size())))
+        return fail(rc);
+    if ((rc = upload(c, &c->d_gz, c->gz)) || (rc = upload(c, &c->d_zclass, c->zclass)) ||
+        (rc = upload(c, &c->d_colprof, c->colprof)) || (rc = upload(c, &c->d_pipe_i, c->pipe_i)) ||
+        (rc = upload(c, &c->d_pipe_j, c->pipe_j)) || (rc = upload(c, &c->d_pipe_b, c->pipe_b)))
+        return fail(rc);
+    std::vector<GwBhDev> bhd(c->nbh);
+    for (int b = 0; b < c->nbh; ++b) {
+        bhd[b].h = c->bh[b].h; bhd[b].v_inner = c->bh[b].v_inner; bhd[b].v_outer = c->bh[b].v_outer;
+        bhd[b].mdot = c->bh[b].mdot;
+        bhd[b].inner_begin = bhd[b].outer_begin = -1;
+        bhd[b].inner_count = bhd[b].outer_count = 0;
+    }
+    for (int q = 0; q < c->n_inner + c->n_outer; ++q) {
+        GwBhDev &B = bhd[c->pipe_b[q]];
+        if (q < c->n_inner) { if (B.inner_begin < 0) B.inner_begin = q; B.inner_count++; }
+        else { if (B.outer_begin < 0) B.outer_begin = q; B.outer_count++; }
+    }
+    for (auto &B : bhd) { if (B.inner_begin < 0) B.inner_begin = 0; if (B.outer_begin < 0) B.outer_begin = 0; }
+    if ((rc = upload(c, &c->d_bh, bhd))) return fail(rc);
+    const size_t N = ncell(c);
+    const int ncol = c->n_inner + c->n_outer;
+    if ((rc = dalloc(c, &c->d_u, N)) || (rc = dalloc(c, &c->d_temp, N)) || (rc = dalloc(c, &c->d_g1, N)) ||
+        (rc = dalloc(c, &c->d_utmp, (size_t)ncol * c->countz)) ||
+        (rc = dalloc(c, &c->d_annmean, (size_t)c->nbh * c->nz)) ||
+        (rc = dalloc(c, &c->d_outlet, c->nbh)) || (rc = dalloc(c, &c->d_energy, c->nbh)) ||
+        (rc = dalloc(c, &c->d_step_counter, 1)) || (rc = dalloc(c, &c->d_flag, 1)))
+        return fail(rc);
+    GW_CUDA(cudaMemset(c->d_u, 0, N * sizeof(double)));
+    GW_CUDA(cudaMemset(c->d_outlet, 0, c->nbh * sizeof(double)));
+    GW_CUDA(cudaMemset(c->d_energy, 0, c->nbh * sizeof(double)));
+    *out = c;
+    return GW_OK;
+}
+
+int gw_destroy(gw_ctx *c) {
+    if (!c) return GW_OK;
+    cudaSetDevice(c->device);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    for (void *p : c->allocations) cudaFree(p);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return GW_OK;
+}
+
+int gw_get_info(gw_ctx *c, gw_info_t *o) {
+    if (!c || !o) return gw_fail(GW_ERR_ARG, "NULL argument");
+    o->nx = c->nx; o->ny = c->ny; o->nz = c->nz; o->n_boreholes = c->nbh;
+    o->countxy_inner = c->n_inner; o->countxy_outer = c->n_outer; o->countz = c->countz;
+    o->n_zclass = c->n_zclass; o->n_profiles = c->n_profiles;
+    o->eigen_estimate = c->eigen_estimate;
+    o->device_bytes = c->device_bytes;
+    return GW_OK;
+}
+
+int gw_set_field(gw_ctx *c, const double *T) {
+    if (!c || !T) return gw_fail(GW_ERR_ARG, "NULL argument");
+    int rc = set_device(c);
+    if (rc) return rc;
+    GW_CUDA(cudaMemcpyAsync(c->d_u, T, ncell(c) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    return sync(c);
+}
+
+int gw_get_field(gw_ctx *c, double *T) {
+    if (!c || !T) return gw_fail(GW_ERR_ARG, "NULL argument");
+    int rc = set_device(c);
+    if (rc) return rc;
+    GW_CUDA(cudaMemcpyAsync(T, c->d_u, ncell(c) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    return sync(c);
+}
+
+int gw_init_thermal_gradient(gw_ctx *c, double T_surface, double gradient) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL argument");
+    std::vector<double> T(ncell(c));
+    for (int i = 0; i < c->nx; ++i)
+        for (int j = 0; j < c->ny; ++j)
+            for (int k = 0; k < c->nz; ++k)
+                T[k + (size_t)c->nz * (j + (size_t)c->ny * i)] = T_surface + gradient * c->gz[k];
+    return gw_set_field(c, T.data());
+}
+
+int gw_rhs_diffusion_z(gw_ctx *c, double *dphi, const double *phi) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
+    int rc = check_field_ptrs(dphi, phi);
+    if (rc || (rc = set_device(c))) return rc;
+    if (dphi == phi) return gw_fail(GW_ERR_ARG, "dphi must not alias phi");
+    if ((rc = gw_launch_zstage(c, dphi, phi, nullptr, 1.0, 0.0, 1))) return rc;
+    return sync(c);
+}
+
+int gw_diffusion_1d(gw_ctx *c, double *dphi, const double *phi, double dt, int dir, int plus_I) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
+    int rc = check_field_ptrs(dphi, phi);
+    if (rc || (rc = set_device(c))) return rc;
+    if (dphi == phi) return gw_fail(GW_ERR_ARG, "dphi must not alias phi");
+    if (dir == GW_DIR_Z) {
+        if (plus_I) rc = gw_launch_zstage(c, dphi, phi, nullptr, dt, 0.0, 0);
+        else rc = gw_launch_zstage(c, dphi, phi, nullptr, 1.0, 0.0, 1);
+    } else if (dir == GW_DIR_X || dir == GW_DIR_Y) {
+        if (plus_I) rc = gw_launch_explicit(c, dphi, phi, dt, dir);
+        else return gw_fail(GW_ERR_UNSUPPORTED, "A_x/A_y without the identity is not on the path");
+    } else {
+        return gw_fail(GW_ERR_ARG, "Invalid direction chosen");
+    }
+    if (rc) return rc;
+    return sync(c);
+}
+
+int gw_thomas(gw_ctx *c, double *U, const double *RHS, double dt, int dir) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
+    int rc = check_field_ptrs(U, RHS);
+    if (rc || (rc = set_device(c))) return rc;
+    if (dir != GW_DIR_X && dir != GW_DIR_Y) return gw_fail(GW_ERR_ARG, "Invalid direction chosen");
+    if ((void *)U == (const void *)RHS) return gw_fail(GW_ERR_ARG, "U must not alias RHS");
+    if ((rc = gw_ensure_factors(c, dt))) return rc;
+    if ((rc = gw_launch_thomas(c, U, RHS, dir))) return rc;
+    return sync(c);
+}
+
+int gw_advection(gw_ctx *c, double *phi, double dt, double t) {
+    (void)t;
+    if (!c || !phi) return gw_fail(GW_ERR_ARG, "NULL argument");
+    int rc = set_device(c);
+    if (rc || (rc = gw_launch_advection(c, phi, dt))) return rc;
+    return sync(c);
+}
+
+int gw_adi_adv(gw_ctx *c, double *u, double *temp, double t, double dt) {
+    (void)t;
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
+    int rc = check_field_ptrs(u, temp);
+    if (rc || (rc = set_device(c))) return rc;
+    if (u == temp) return gw_fail(GW_ERR_ARG, "temp must not alias u");
+    if ((rc = gw_ensure_factors(c, dt / 2))) return rc;
+    if ((rc = adi_adv(c, u, temp, dt))) return rc;
+    return sync(c);
+}
+
+int gw_rock2_stages(gw_ctx *c, double dt, int max_stages, int *stages, int *covered) {
+    if (!c || !stages || !covered) return gw_fail(GW_ERR_ARG, "NULL argument");
+    return gw_rock2_choose(dt, c->eigen_estimate, max_stages, stages, covered);
+}
+
+int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
+    (void)t0;
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
+    if (nsteps < 0) return gw_fail(GW_ERR_ARG, "nsteps must be >= 0");
+    if (!(dt > 0) || !std::isfinite(dt)) return gw_fail(GW_ERR_ARG, "dt must be positive and finite");
+    int rc = set_device(c);
+    if (rc) return rc;
+    int s, covered;
+    if ((rc = gw_rock2_choose(dt, c->eigen_estimate, max_stages, &s, &covered))) return rc;
+    if (nsteps > c->series_cap) {
+        if (c->d_series) {
+            cudaFree(c->d_series);
+            for (auto &p : c->allocations) if (p == c->d_series) p = nullptr;
+            c->d_series = nullptr;
+        }
+        if ((rc = dalloc(c, &c->d_series, (size_t)nsteps * c->nbh))) return rc;
+        c->series_cap = nsteps;
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+    }
+    GW_CUDA(cudaMemsetAsync(c->d_step_counter, 0, sizeof(int), c->stream));
+    c->last_nsteps = nsteps;
+    if (nsteps == 0) return sync(c);
+    if ((rc = gw_ensure_factors(c, dt / 2))) return rc;
+    if (!c->graph || c->graph_dt != dt || c->graph_s != s) {
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+        cudaGraph_t g;
+        GW_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int r1 = rock2_step(c, c->d_u, c->d_g1, c->d_temp, dt, s);
+        int r2 = r1 ? r1 : adi_adv(c, c->d_u, c->d_temp, dt);
+        int r3 = r2 ? r2 : gw_launch_record(c, dt);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (r3) { if (e == cudaSuccess) cudaGraphDestroy(g); return r3; }
+        if (e != cudaSuccess) return gw_cuda_fail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&c->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return gw_cuda_fail(e, "cudaGraphInstantiate");
+        c->graph_dt = dt;
+        c->graph_s = s;
+    }
+    GW_CUDA(cudaEventRecord(c->ev0, c->stream));
+    for (int n = 0; n < nsteps; ++n) GW_CUDA(cudaGraphLaunch(c->graph, c->stream));
+    GW_CUDA(cudaEventRecord(c->ev1, c->stream));
+    if ((rc = sync(c))) return rc;
+    float ms = 0.f;
+    GW_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    c->last_step_ms = ms;
+    return GW_OK;
+}
+
+int gw_get_last_step_time(gw_ctx *c, double *ms) {
+    if (!c || !ms) return gw_fail(GW_ERR_ARG, "NULL argument");
+    *ms = c->last_step_ms;
+    return GW_OK;
+}
+
+int gw_profile_kernels(gw_ctx *c, double dt, int reps, double *ms_out) {
+    if (!c || !ms_out) return gw_fail(GW_ERR_ARG, "NULL argument");
+    if (reps < 1 || !(dt > 0)) return gw_fail(GW_ERR_ARG, "reps >= 1 and dt > 0 required");
+    int rc = set_device(c);
+    if (rc || (rc = gw_ensure_factors(c, dt / 2))) return rc;
+    const size_t N = ncell(c);
+    // keep the state: u -> g1 copy, restored at the end
+    GW_CUDA(cudaMemcpyAsync(c->d_g1, c->d_u, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    double *u = c->d_u, *t = c->d_temp, *g = c->d_g1;
+    for (int kcls = 0; kcls < GW_KERNEL_COUNT; ++kcls) {
+        float total = 0.f;
+        for (int r = 0; r < reps; ++r) {
+            GW_CUDA(cudaEventRecord(c->ev0, c->stream));
+            switch (kcls) {
+                case GW_KERNEL_ZSTAGE: rc = gw_launch_zstage(c, t, g, u, dt * 0.1, 0.5, 0); break;
+                case GW_KERNEL_EXPLICIT: rc = gw_launch_explicit(c, t, g, dt / 2, r % 2 ? GW_DIR_X : GW_DIR_Y); break;
+                case GW_KERNEL_THOMAS_X: rc = gw_launch_thomas(c, t, g, GW_DIR_X); break;
+                case GW_KERNEL_THOMAS_Y: rc = gw_launch_thomas(c, t, g, GW_DIR_Y); break;
+                default: rc = gw_launch_advection(c, t, dt / 2); break;
+            }
+            if (rc) return rc;
+            GW_CUDA(cudaEventRecord(c->ev1, c->stream));
+            if ((rc = sync(c))) return rc;
+            float ms = 0.f;
+            GW_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+            total += ms;
+        }
+        ms_out[kcls] = total / reps;
+    }
+    GW_CUDA(cudaMemcpyAsync(c->d_u, c->d_g1, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    return sync(c);
+}
+
+int gw_get_outlet(gw_ctx *c, double *T) {
+    if (!c || !T) return gw_fail(GW_ERR_ARG, "NULL argument");
+    int rc = set_device(c);
+    if (rc) return rc;
+    GW_CUDA(cudaMemcpyAsync(T, c->d_outlet, c->nbh * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    return sync(c);
+}
+
+int gw_get_outlet_series(gw_ctx *c, double *T, int nsteps) {
+    if (!c || !T) return gw_fail(GW_ERR_ARG, "NULL argument");
+    if (nsteps < 0 || nsteps > c->last_nsteps) return gw_fail(GW_ERR_ARG, "nsteps exceeds the last gw_step call");
+    if (nsteps == 0) return GW_OK;
+    int rc = set_device(c);
+    if (rc) return rc;
+    GW_CUDA(cudaMemcpyAsync(T, c->d_series, (size_t)nsteps * c->nbh * sizeof(double),
+                            cudaMemcpyDeviceToHost, c->stream));
+    return sync(c);
+}
+
+int gw_get_energy(gw_ctx *c, double *E) {
+    if (!c || !E) return gw_fail(GW_ERR_ARG, "NULL argument");
+    int rc = set_device(c);
+    if (rc) return rc;
+    GW_CUDA(cudaMemcpyAsync(E, c->d_energy, c->nbh * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    return sync(c);
+}
+
+int gw_reset_energy(gw_ctx *c) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL argument");
+    int rc = set_device(c);
+    if (rc) return rc;
+    GW_CUDA(cudaMemsetAsync(c->d_energy, 0, c->nbh * sizeof(double), c->stream));
+    return sync(c);
+}
+
+int gw_check_finite(gw_ctx *c) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL argument");
+    int rc = set_device(c);
+    if (rc || (rc = gw_launch_check_finite(c, c->d_u, ncell(c)))) return rc;
+    int flag = 0;
+    GW_CUDA(cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    if ((rc = sync(c))) return rc;
+    return flag ? gw_fail(GW_ERR_NONFINITE, "state holds NaN or Inf") : GW_OK;
+}
+
+}  // extern "C"

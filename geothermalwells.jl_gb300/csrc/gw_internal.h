@@ -1,0 +1,125 @@
+// gw_internal.h -- device context and kernel launch interface shared by the
+// translation units of libgw_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/gw_gb300.h"
+
+// Borehole record with the derived values of src/physics.jl:48-59.
+struct GwBorehole {
+    double xc, yc, h, r_inner, t_inner, r_and_t_inner_sq, r_outer, r_outer_sq;
+    double t_outer, r_and_t_outer_sq, r_backfill, r_backfill_sq, mdot;
+    double v_inner, v_outer, insulation_depth;
+};
+
+// Per-borehole data the advection kernels read (one small device array).
+struct GwBhDev {
+    double h, v_inner, v_outer, mdot;
+    int inner_begin, inner_count;   // range in the pipe-column list
+    int outer_begin, outer_count;
+};
+
+// Thomas factorisation of one direction's (I - h A) lines, per (zclass, line, row):
+//   forward  y_l = (b_l - a_l * y_{l-1}) * ib_l
+//   backward x_l = y_l - cu_l * x_{l+1}
+template <typename T>
+struct GwFactors {
+    T *a = nullptr, *ib = nullptr, *cu = nullptr;
+};
+
+template <typename T>
+struct GwCoefTables {
+    // x: [zc][j][i], y: [zc][i][j] (row index fastest); z: [profile][k]
+    T *cxm = nullptr, *cxp = nullptr, *cym = nullptr, *cyp = nullptr;
+    T *czm = nullptr, *czp = nullptr;
+    GwFactors<T> fx, fy;   // for h = dt/2 of the current step size
+};
+
+struct gw_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int nx = 0, ny = 0, nz = 0, nbh = 0, precision = GW_PREC_FP64;
+    std::vector<double> gx, gy, gz;
+    std::vector<GwBorehole> bh;
+    // materials (one-layer stratified == homogeneous)
+    std::vector<double> k_layers, rhoc_layers, depths;
+    double k_water, rho_c_water, k_steel, rho_c_steel, k_insulating, rho_c_insulating;
+    double k_backfill, rho_c_backfill;
+    int inlet_kind = 0;
+    double inlet_param = 0.0;
+    double eigen_estimate = 0.0;
+
+    // host-side material model
+    int n_zclass = 0, n_profiles = 0;
+    std::vector<int> zclass;          // [nz]
+    std::vector<int> colprof;         // [nx*ny] (i*ny + j)
+    int n_inner = 0, n_outer = 0, countz = 0;
+    std::vector<int> pipe_i, pipe_j, pipe_b;   // inner list then outer list
+
+    // device: grids, tables, lists
+    double *d_gz = nullptr;
+    int *d_zclass = nullptr, *d_colprof = nullptr;
+    int *d_pipe_i = nullptr, *d_pipe_j = nullptr, *d_pipe_b = nullptr;
+    GwBhDev *d_bh = nullptr;
+    GwCoefTables<double> c64;
+    GwCoefTables<float> c32;
+    double factors_h = -1.0;          // h for which c64.fx/fy (and c32) are valid
+
+    // device state and scratch (double path)
+    double *d_u = nullptr, *d_temp = nullptr, *d_g1 = nullptr, *d_g2 = nullptr;
+    double *d_utmp = nullptr;         // [ncol][countz] (k fastest)
+    double *d_annmean = nullptr;      // [nbh][nz]
+    double *d_outlet = nullptr;       // [nbh]
+    double *d_energy = nullptr;       // [nbh]
+    double *d_series = nullptr;       // [series_cap][nbh]
+    int *d_step_counter = nullptr;
+    int *d_flag = nullptr;
+    int series_cap = 0;
+    int last_nsteps = 0;
+    // mixed path state (allocated for GW_PREC_MIXED)
+    float *f_u = nullptr, *f_temp = nullptr, *f_g1 = nullptr, *f_g2 = nullptr, *f_utmp = nullptr;
+
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_step_ms = 0.0;
+    // graph cache for gw_step
+    cudaGraphExec_t graph = nullptr;
+    double graph_dt = -1.0;
+    int graph_s = -1;
+
+    long long device_bytes = 0;
+    std::vector<void *> allocations;
+};
+
+// error reporting
+int gw_fail(int code, const std::string &msg);
+int gw_cuda_fail(cudaError_t e, const char *what);
+#define GW_CUDA(call)                                                    \
+    do {                                                                 \
+        cudaError_t _e = (call);                                         \
+        if (_e != cudaSuccess) return gw_cuda_fail(_e, #call);           \
+    } while (0)
+
+// setup (gw_setup.cpp)
+int gw_setup_host(gw_ctx *c, const gw_desc *d);
+void gw_build_coefs(const gw_ctx *c, std::vector<double> &cxm, std::vector<double> &cxp,
+                    std::vector<double> &cym, std::vector<double> &cyp,
+                    std::vector<double> &czm, std::vector<double> &czp);
+void gw_build_factors(const gw_ctx *c, double h, int dir, const std::vector<double> &cm,
+                      const std::vector<double> &cp, std::vector<double> &a,
+                      std::vector<double> &ib, std::vector<double> &cu);
+int gw_rock2_choose(double dt, double eigen_est, int max_stages, int *s, int *covered);
+void gw_rock2_coefs(int s, const double **mu, const double **nu, const double **kappa,
+                    double *sigma, double *tau);
+
+// launches (gw_kernels.cu); all enqueue on c->stream
+int gw_launch_zstage(gw_ctx *c, double *out, const double *x, const double *y, double hmu,
+                     double kap, int rhs_only);
+int gw_launch_explicit(gw_ctx *c, double *dst, const double *src, double h, int dir);
+int gw_launch_thomas(gw_ctx *c, double *U, const double *RHS, int dir);
+int gw_launch_advection(gw_ctx *c, double *phi, double dt);
+int gw_launch_record(gw_ctx *c, double dt);
+int gw_launch_check_finite(gw_ctx *c, const double *u, size_t n);
+int gw_ensure_factors(gw_ctx *c, double h);

@@ -1,0 +1,160 @@
+/*
+ * gw_gb300.h -- C ABI of the GB300 (sm_103a) backend for the time-step hot
+ * path of GeothermalWells.jl.
+ *
+ * The reference's plugin point is the KernelAbstractions `backend` value
+ * passed to `create_cache` (src/cache.jl:55); every device-side call then
+ * dispatches on `cache.backend` (src/solver.jl:24,28,256-261,444-461).  This
+ * library is what a GB300 backend value dispatches to: plain C, plain
+ * pointers and sizes, int status codes.
+ *
+ * Conventions
+ *  - Fields are Nz x Ny x Nx arrays of double in the reference's layout
+ *    (Julia column-major, z fastest): element (k, j, i) sits at
+ *    k + Nz * (j + Ny * i), all indices 0-based here.
+ *  - Functions taking `double *` field arguments whose names end in `_dev`
+ *    take device pointers; all others take host pointers.
+ *  - Every call is synchronous with respect to the host unless stated.
+ *  - A context owns one CUDA stream and its device buffers; calls on one
+ *    context must not overlap (the reference's cache is not re-entrant
+ *    either: T_outlet and u_tmp are shared, src/cache.jl:41,62).
+ *  - Return value 0 (GW_OK) on success; otherwise an error code, with a
+ *    message available from gw_last_error() on the calling thread.
+ */
+#ifndef GW_GB300_H
+#define GW_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GW_OK 0
+#define GW_ERR_ARG 1          /* invalid argument or size */
+#define GW_ERR_CUDA 2         /* a CUDA call failed */
+#define GW_ERR_NONFINITE 3    /* NaN/Inf found in the state by gw_check_finite */
+#define GW_ERR_TIMEOUT 4      /* a bounded device wait expired */
+#define GW_ERR_UNSUPPORTED 5  /* a feature the device path does not offer */
+
+#define GW_PREC_FP64 0        /* all storage and arithmetic in double */
+#define GW_PREC_MIXED 1       /* float storage/Thomas, double ROCK2 accumulation + energy balance */
+
+#define GW_INLET_CONSTANT 0        /* ConstantInlet, src/physics.jl:290-293 */
+#define GW_INLET_HEAT_EXCHANGER 1  /* HeatExchangerInlet, src/physics.jl:303-306 */
+
+#define GW_DIR_X 0
+#define GW_DIR_Y 1
+#define GW_DIR_Z 2
+
+/* Borehole constructor arguments, src/physics.jl:30-61 (the derived squared
+ * radii and plug-flow velocities are computed inside, as physics.jl:48-59). */
+typedef struct gw_borehole_desc {
+    double xc, yc, h, r_inner, t_inner, r_outer, t_outer, r_backfill, mdot, insulation_depth;
+} gw_borehole_desc;
+
+/* StratifiedMaterialProperties, src/physics.jl:81-94.  A
+ * HomogenousMaterialProperties (physics.jl:159-170) is n_layers = 1. */
+typedef struct gw_material_desc {
+    int n_layers;
+    const double *k_rock_layers;
+    const double *rho_c_rock_layers;
+    const double *layer_depths;
+    double k_water, rho_c_water, k_steel, rho_c_steel;
+    double k_insulating, rho_c_insulating, k_backfill, rho_c_backfill;
+} gw_material_desc;
+
+/* Everything create_cache(; backend, gridx, gridy, gridz, materials,
+ * boreholes, inlet_model) receives (src/cache.jl:55). */
+typedef struct gw_desc {
+    int nx, ny, nz;
+    const double *gridx, *gridy, *gridz;   /* strictly increasing, host */
+    int n_boreholes;
+    const gw_borehole_desc *boreholes;
+    gw_material_desc materials;
+    int inlet_kind;        /* GW_INLET_*; CustomInlet closures cannot cross the ABI */
+    double inlet_param;    /* T_const or DeltaT */
+    int precision;         /* GW_PREC_* (the fused gw_step path) */
+    int device;            /* CUDA device ordinal */
+} gw_desc;
+
+/* Sizes the reference keeps in its cache (src/cache.jl:28-39,57-58,65). */
+typedef struct gw_info_t {
+    int nx, ny, nz, n_boreholes;
+    int countxy_inner, countxy_outer, countz;
+    int n_zclass, n_profiles;
+    double eigen_estimate;           /* src/solver.jl:474-488 */
+    long long device_bytes;          /* device memory held by the context */
+} gw_info_t;
+
+typedef struct gw_ctx gw_ctx;
+
+const char *gw_last_error(void);
+const char *gw_version(void);
+
+/* create_cache (src/cache.jl:55-116): builds the material model, the advection
+ * index lists (src/cache.jl:9-44) and all buffers on the device. */
+int gw_create(const gw_desc *desc, gw_ctx **out);
+int gw_destroy(gw_ctx *ctx);
+int gw_get_info(gw_ctx *ctx, gw_info_t *out);
+
+/* The solution state u owned by the context (the integrator's u). */
+int gw_set_field(gw_ctx *ctx, const double *T);
+int gw_get_field(gw_ctx *ctx, double *T);
+/* initial_condition_thermal_gradient (src/physics.jl:333-348) into u. */
+int gw_init_thermal_gradient(gw_ctx *ctx, double T_surface, double gradient);
+
+/* ---- fine-grained entry points on caller-owned device fields (double) ---- */
+/* rhs_diffusion_z!(dphi, phi, cache, t), src/solver.jl:23-31 */
+int gw_rhs_diffusion_z(gw_ctx *ctx, double *dphi_dev, const double *phi_dev);
+/* diffusion_1D!(dphi, phi, ..., dt, Val(dir), Val(plus_I)), src/solver.jl:34-58 */
+int gw_diffusion_1d(gw_ctx *ctx, double *dphi_dev, const double *phi_dev, double dt, int dir,
+                    int plus_I);
+/* thomas_I_minus_A!(U, RHS, ..., dt, ..., Val(dir)), src/solver.jl:111-232; dir X or Y */
+int gw_thomas(gw_ctx *ctx, double *U_dev, const double *RHS_dev, double dt, int dir);
+/* advection!(phi, dt, t, cache, boreholes), src/solver.jl:250-264 */
+int gw_advection(gw_ctx *ctx, double *phi_dev, double dt, double t);
+/* ADI_and_ADV_callback!(integrator), src/solver.jl:432-464: u = integrator.u,
+ * temp = integrator.uprev (clobbered), t = integrator.t, dt = t - tprev. */
+int gw_adi_adv(gw_ctx *ctx, double *u_dev, double *temp_dev, double t, double dt);
+
+/* ---- fused step on the context's own state ---- */
+/* Advance u by nsteps fixed steps of size dt from time t0: per step one
+ * ROCK2 step of rhs_diffusion_z! (stage count from the eigenvalue estimate,
+ * src/solver.jl:495, capped at max_stages) then ADI_and_ADV_callback!.  The
+ * step is captured once in a CUDA graph and replayed.  Records the outlet
+ * temperature and extracted heat after every step. */
+int gw_step(gw_ctx *ctx, double t0, double dt, int nsteps, int max_stages);
+/* Stage count gw_step uses for dt (and whether its interval covers dt*lambda). */
+int gw_rock2_stages(gw_ctx *ctx, double dt, int max_stages, int *stages, int *covered);
+
+/* cache.T_outlet after the last advection (src/solver.jl:253-257). */
+int gw_get_outlet(gw_ctx *ctx, double *T_outlet);
+/* Outlet temperature after each of the last gw_step call's steps, nsteps x nbh. */
+int gw_get_outlet_series(gw_ctx *ctx, double *T_series, int nsteps);
+/* Extracted heat per borehole integrated over all gw_step steps so far [J]:
+ * sum over steps of mdot * c_w * (T_outlet - T_inlet) * dt, c_w = rho_c_water / 998.2. */
+int gw_get_energy(gw_ctx *ctx, double *E);
+int gw_reset_energy(gw_ctx *ctx);
+/* GW_ERR_NONFINITE if the context's u holds a NaN or Inf. */
+int gw_check_finite(gw_ctx *ctx);
+
+/* Device time of the last gw_step call's replay loop [ms], from CUDA events
+ * recorded on the context's stream around the graph launches. */
+int gw_get_last_step_time(gw_ctx *ctx, double *ms);
+
+/* Kernel timing for the roofline: runs each kernel class of one step of size
+ * dt `reps` times on the context's buffers (the state u is restored
+ * afterwards) and writes the mean device time per launch [ms] into
+ * ms_out[GW_KERNEL_COUNT], indexed by GW_KERNEL_*.  Each launch is bracketed
+ * by CUDA events on the context's stream. */
+#define GW_KERNEL_ZSTAGE 0     /* one ROCK2 stage of the z-stencil */
+#define GW_KERNEL_EXPLICIT 1   /* (I + dt/2 A_x) or (I + dt/2 A_y) sweep */
+#define GW_KERNEL_THOMAS_X 2   /* x-line solves */
+#define GW_KERNEL_THOMAS_Y 3   /* y-line solves */
+#define GW_KERNEL_ADVECTION 4  /* outlet mean + annulus mean + advect + scatter */
+#define GW_KERNEL_COUNT 5
+int gw_profile_kernels(gw_ctx *ctx, double dt, int reps, double *ms_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GW_GB300_H */
