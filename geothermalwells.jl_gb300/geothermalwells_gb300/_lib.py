@@ -76,6 +76,7 @@ SIGNATURES = {
     "gw_check_finite": (_i, [_vp]),
     "gw_get_last_step_time": (_i, [_vp, _dp]),
     "gw_profile_kernels": (_i, [_vp, _d, _i, _dp]),
+    "gw_advection_noalloc": (_i, [_vp, _vp, _d, _d, _vp]),
 }
 KERNELS = ("zstage", "explicit", "thomas_x", "thomas_y", "advection")
 

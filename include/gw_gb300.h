@@ -154,6 +154,31 @@ int gw_get_last_step_time(gw_ctx *ctx, double *ms);
 #define GW_KERNEL_COUNT 5
 int gw_profile_kernels(gw_ctx *ctx, double dt, int reps, double *ms_out);
 
+/* advection! (same result as gw_advection) for callers that must not make
+ * the library allocate device memory.  No counterpart in the reference.
+ *
+ * Who needs it: a host integrator that owns every device buffer itself --
+ * e.g. a Julia caller whose arrays come from its own pool allocator and must
+ * keep the device footprint fixed after set-up, or a caller recording the
+ * step into its own CUDA graph, where cudaMalloc is not allowed.  This entry
+ * point calls no cudaMalloc, cudaFree or allocating library routine.
+ *
+ * Its scratch (outlet means and per-level annulus means) lives in one
+ * file-scope device array of 65536 doubles (512 KiB) that every GPU which
+ * loads the library holds until the process exits; each pipe column is
+ * advected inside one thread block's shared memory, so no column buffer is
+ * needed.  Limits: n_boreholes * (nz + 1) <= 65536 and at most 12288 levels
+ * at or above the deepest borehole bottom; larger problems get GW_ERR_ARG.
+ * T_outlet_dev (device, n_boreholes doubles) receives cache.T_outlet.
+ *
+ * The first call on a device looks up the array's device address and sets
+ * the kernel's shared-memory limit for that device; make that first call
+ * before any stream capture.  All calls share the one array (every value a
+ * call reads is first written by the same call, so nothing needs clearing
+ * between calls); calls that overlap on the GPU -- from two contexts or two
+ * threads at once -- race on it and must be serialised by the caller. */
+int gw_advection_noalloc(gw_ctx *ctx, double *phi_dev, double dt, double t, double *T_outlet_dev);
+
 #ifdef __cplusplus
 }
 #endif
