@@ -186,14 +186,17 @@ def run_ours(args):
     value = ncell * args.steps * world / (t_ms / 1e3) / 1e6
 
     # per-kernel timing for the roofline of the dominant kernel
-    prof = (ctypes.c_double * 5)()
+    prof = (ctypes.c_double * len(_lib.KERNELS))()
     _lib.check(L.gw_profile_kernels(cache.ctx, dt, 3, prof))
     kms = dict(zip(_lib.KERNELS, list(prof)))
-    wb = 8  # the double path moves 8-byte words
-    ncolz = (cache.countxy_inner + cache.countxy_outer) * cache.countz
-    alg = {"zstage": 3 * wb * ncell, "explicit": 2 * wb * ncell, "thomas_x": 2 * wb * ncell,
-           "thomas_y": 2 * wb * ncell, "advection": 2 * wb * ncolz}
-    per_step = {"zstage": s.value, "explicit": 2, "thomas_x": 1, "thomas_y": 1, "advection": 2}
+    wb = WORD[args.precision]
+    ncol = cache.countxy_inner + cache.countxy_outer
+    # compulsory bytes per launch: each fused field kernel reads and writes the
+    # field once; the pipe pass reads and writes the pipe columns
+    alg = {"rock2_columns": 2 * wb * ncell, "half_step_x": 2 * wb * ncell,
+           "half_step_y": 2 * wb * ncell,
+           "pipe": 2 * wb * ncol * cache.Nz + 2 * wb * ncol * cache.countz}
+    per_step = {"rock2_columns": 1, "half_step_x": 1, "half_step_y": 1, "pipe": 2}
     share = {k: kms[k] * per_step[k] for k in kms}
     dom = max(share, key=share.get)
     peak, peak_kind = peaks()
@@ -203,7 +206,7 @@ def run_ours(args):
     if os.path.exists(tpath):
         tr = json.load(open(tpath)).get(args.precision, {}).get(dom)
         if tr is not None:
-            traffic = tr * (ncolz if dom == "advection" else ncell)
+            traffic = tr * (ncol * cache.Nz if dom == "pipe" else ncell)
 
     # end to end through the public path with host buffers (pinned)
     e2e = None
@@ -236,7 +239,7 @@ def run_ours(args):
     if not args.no_cpu_baseline and world == 1:
         cb = cpu_baseline(w, args.cpu_sample_steps)
         cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
-    launches_per_step = s.value + 2 * 1 + 2 + 2 * 4 + 1
+    launches_per_step = 1 + 2 + 2 * 5 + 1   # rock2 columns, 2 half steps, 2 x 5 pipe kernels, record
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
@@ -248,7 +251,8 @@ def run_ours(args):
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel_ms": kms,
-                     "alg_bytes_per_launch": alg[dom]},
+                     "alg_bytes_per_launch": alg[dom],
+                     "step_share": {k: share[k] / sum(share.values()) for k in share}},
         "cpu_baseline": cb, "e2e": e2e, "gpu_launches": launches_per_step * args.steps,
         "clocks": ck,
     }

@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "gw_fused.h"
 #include "gw_internal.h"
 
 namespace {
@@ -30,6 +31,18 @@ int upload(gw_ctx *c, T **p, const std::vector<T> &v) {
     return GW_OK;
 }
 
+template <typename T>
+int copy_to(T *dst, const std::vector<T> &v) {
+    if (!v.empty()) GW_CUDA(cudaMemcpy(dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return GW_OK;
+}
+
+std::vector<float> to_float(const std::vector<double> &v) {
+    std::vector<float> f(v.size());
+    for (size_t i = 0; i < v.size(); ++i) f[i] = (float)v[i];
+    return f;
+}
+
 size_t ncell(const gw_ctx *c) { return (size_t)c->nx * c->ny * c->nz; }
 
 int set_device(gw_ctx *c) {
@@ -42,7 +55,9 @@ int sync(gw_ctx *c) {
     return GW_OK;
 }
 
-// One ROCK2 step on u (stage count s, step dt) using buffers {u, g1, spare}.
+bool mixed(const gw_ctx *c) { return c->precision == GW_PREC_MIXED; }
+
+// One ROCK2 step on u with the modular kernels (buffers {u, g1, spare}).
 // Each stage reads its stencil input and, pointwise, the stage before it, so
 // the output may overwrite the older stage; the last stage lands in u.
 int rock2_step(gw_ctx *c, double *u, double *g1, double *spare, double dt, int s) {
@@ -65,8 +80,6 @@ int rock2_step(gw_ctx *c, double *u, double *g1, double *spare, double dt, int s
         prev = cur;
         cur = out;
     }
-    // finishing procedure: gq = gp + h sigma A gp, then
-    // y = gq + (h tau / sigma) A gq + (1 - tau / sigma^2) (gq - gp), written into u
     int gp = cur;
     int gq = pick(gp, 0);
     rc = gw_launch_zstage(c, pool[gq], pool[gp], nullptr, dt * sigma, 0.0, 0);
@@ -75,7 +88,7 @@ int rock2_step(gw_ctx *c, double *u, double *g1, double *spare, double dt, int s
                             1.0 - tau / (sigma * sigma), 0);
 }
 
-// ADI_and_ADV_callback! (src/solver.jl:432-464)
+// ADI_and_ADV_callback! (src/solver.jl:432-464) with the modular kernels.
 // The Thomas factors for h = dt/2 must be current (gw_ensure_factors).
 int adi_adv(gw_ctx *c, double *u, double *temp, double dt) {
     int rc;
@@ -91,6 +104,43 @@ int check_field_ptrs(const void *a, const void *b) {
     if (!a || !b) return gw_fail(GW_ERR_ARG, "field pointer is NULL");
     return GW_OK;
 }
+
+// ROCK2 stage table for the fused column kernel (layout in gw_fused.cu)
+int upload_stages(gw_ctx *c, double dt, int s) {
+    const double *mu, *nu, *kappa;
+    double sigma, tau;
+    gw_rock2_coefs(s, &mu, &nu, &kappa, &sigma, &tau);
+    std::vector<double> sc;
+    for (int j = 0; j < s - 2; ++j) {
+        sc.push_back(dt * mu[j]);
+        sc.push_back(j == 0 ? 0.0 : kappa[j]);
+    }
+    sc.push_back(dt * sigma);
+    sc.push_back(dt * tau / sigma);
+    sc.push_back(1.0 - tau / (sigma * sigma));
+    if ((int)sc.size() > GW_STAGE_TABLE) return gw_fail(GW_ERR_ARG, "stage table too long");
+    GW_CUDA(cudaMemcpy(c->d_stage, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice));
+    return GW_OK;
+}
+
+// Mixed path: T_ref = the field's first column (i = j = 0), and the source
+// A_z T_ref per column profile.
+int set_reference_profile(gw_ctx *c, const double *T) {
+    const int nz = c->nz;
+    c->Tref.assign(T, T + nz);
+    std::vector<double> f((size_t)c->n_profiles * nz);
+    for (int p = 0; p < c->n_profiles; ++p)
+        for (int k = 0; k < nz; ++k) {
+            double tc = c->Tref[k];
+            double tp = k < nz - 1 ? c->Tref[k + 1] : tc;
+            double tm = k > 0 ? c->Tref[k - 1] : tc;
+            size_t q = (size_t)p * nz + k;
+            f[q] = c->h_czp[q] * (tp - tc) - c->h_czm[q] * (tc - tm);
+        }
+    int rc;
+    if ((rc = copy_to(c->d_Tref, c->Tref))) return rc;
+    return copy_to(c->f_fref, to_float(f));
+}
 }  // namespace
 
 int gw_fail(int code, const std::string &msg) {
@@ -103,21 +153,26 @@ int gw_cuda_fail(cudaError_t e, const char *what) {
     return GW_ERR_CUDA;
 }
 
-// Recompute the Thomas factors of (I - h A_x) and (I - h A_y) when h changes.
+// Recompute the Thomas factors of (I - h A_x) and (I - h A_y) when h changes
+// (in double; the mixed path gets them rounded to float).
 int gw_ensure_factors(gw_ctx *c, double h) {
     if (h == c->factors_h) return GW_OK;
     std::vector<double> cxm, cxp, cym, cyp, czm, czp;
     gw_build_coefs(c, cxm, cxp, cym, cyp, czm, czp);
     std::vector<double> a, ib, cu;
     GW_CUDA(cudaStreamSynchronize(c->stream));
-    gw_build_factors(c, h, GW_DIR_X, cxm, cxp, a, ib, cu);
-    GW_CUDA(cudaMemcpy(c->c64.fx.a, a.data(), a.size() * 8, cudaMemcpyHostToDevice));
-    GW_CUDA(cudaMemcpy(c->c64.fx.ib, ib.data(), ib.size() * 8, cudaMemcpyHostToDevice));
-    GW_CUDA(cudaMemcpy(c->c64.fx.cu, cu.data(), cu.size() * 8, cudaMemcpyHostToDevice));
-    gw_build_factors(c, h, GW_DIR_Y, cym, cyp, a, ib, cu);
-    GW_CUDA(cudaMemcpy(c->c64.fy.a, a.data(), a.size() * 8, cudaMemcpyHostToDevice));
-    GW_CUDA(cudaMemcpy(c->c64.fy.ib, ib.data(), ib.size() * 8, cudaMemcpyHostToDevice));
-    GW_CUDA(cudaMemcpy(c->c64.fy.cu, cu.data(), cu.size() * 8, cudaMemcpyHostToDevice));
+    int rc;
+    for (int dir = GW_DIR_X; dir <= GW_DIR_Y; ++dir) {
+        gw_build_factors(c, h, dir, dir == GW_DIR_X ? cxm : cym, dir == GW_DIR_X ? cxp : cyp, a, ib, cu);
+        GwFactors<double> &f = dir == GW_DIR_X ? c->c64.fx : c->c64.fy;
+        if ((rc = copy_to(f.a, a)) || (rc = copy_to(f.ib, ib)) || (rc = copy_to(f.cu, cu))) return rc;
+        if (mixed(c)) {
+            GwFactors<float> &g = dir == GW_DIR_X ? c->c32.fx : c->c32.fy;
+            if ((rc = copy_to(g.a, to_float(a))) || (rc = copy_to(g.ib, to_float(ib))) ||
+                (rc = copy_to(g.cu, to_float(cu))))
+                return rc;
+        }
+    }
     c->factors_h = h;
     return GW_OK;
 }
@@ -126,7 +181,7 @@ extern "C" {
 
 const char *gw_last_error(void) { return g_err.c_str(); }
 
-const char *gw_version(void) { return "gw_gb300 0.1 (sm_103a)"; }
+const char *gw_version(void) { return "gw_gb300 0.2 (sm_103a)"; }
 
 int gw_create(const gw_desc *desc, gw_ctx **out) {
     if (!out) return gw_fail(GW_ERR_ARG, "out is NULL");
@@ -143,8 +198,12 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
     if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess)
         return fail(gw_cuda_fail(e, "cudaEventCreate"));
 
+    // material model as coefficient tables (double always: the fine-grained
+    // entry points work on double fields)
     std::vector<double> cxm, cxp, cym, cyp, czm, czp;
     gw_build_coefs(c, cxm, cxp, cym, cyp, czm, czp);
+    c->h_czm = czm;
+    c->h_czp = czp;
     if ((rc = upload(c, &c->c64.cxm, cxm)) || (rc = upload(c, &c->c64.cxp, cxp)) ||
         (rc = upload(c, &c->c64.cym, cym)) || (rc = upload(c, &c->c64.cyp, cyp)) ||
         (rc = upload(c, &c->c64.czm, czm)) || (rc = upload(c, &c->c64.czp, czp)))
@@ -164,24 +223,59 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         bhd[b].inner_begin = bhd[b].outer_begin = -1;
         bhd[b].inner_count = bhd[b].outer_count = 0;
     }
-    for (int q = 0; q < c->n_inner + c->n_outer; ++q) {
+    const int ncol = c->n_inner + c->n_outer;
+    std::vector<int> pipe_of((size_t)c->nx * c->ny, -1);
+    bool unique_cols = true;
+    for (int q = 0; q < ncol; ++q) {
         GwBhDev &B = bhd[c->pipe_b[q]];
         if (q < c->n_inner) { if (B.inner_begin < 0) B.inner_begin = q; B.inner_count++; }
         else { if (B.outer_begin < 0) B.outer_begin = q; B.outer_count++; }
+        int &slot = pipe_of[(size_t)c->pipe_i[q] * c->ny + c->pipe_j[q]];
+        if (slot >= 0) unique_cols = false;   // overlapping boreholes
+        slot = q;
     }
     for (auto &B : bhd) { if (B.inner_begin < 0) B.inner_begin = 0; if (B.outer_begin < 0) B.outer_begin = 0; }
-    if ((rc = upload(c, &c->d_bh, bhd))) return fail(rc);
+    if ((rc = upload(c, &c->d_bh, bhd)) || (rc = upload(c, &c->d_pipe_of, pipe_of))) return fail(rc);
     const size_t N = ncell(c);
-    const int ncol = c->n_inner + c->n_outer;
-    if ((rc = dalloc(c, &c->d_u, N)) || (rc = dalloc(c, &c->d_temp, N)) || (rc = dalloc(c, &c->d_g1, N)) ||
-        (rc = dalloc(c, &c->d_utmp, (size_t)ncol * c->countz)) ||
+    if ((rc = dalloc(c, &c->d_utmp, (size_t)ncol * c->countz)) ||
         (rc = dalloc(c, &c->d_annmean, (size_t)c->nbh * c->nz)) ||
+        (rc = dalloc(c, &c->d_annpart, (size_t)c->nbh * 32 * c->nz)) ||
         (rc = dalloc(c, &c->d_outlet, c->nbh)) || (rc = dalloc(c, &c->d_energy, c->nbh)) ||
+        (rc = dalloc(c, &c->d_stage, GW_STAGE_TABLE)) ||
         (rc = dalloc(c, &c->d_step_counter, 1)) || (rc = dalloc(c, &c->d_flag, 1)))
         return fail(rc);
-    GW_CUDA(cudaMemset(c->d_u, 0, N * sizeof(double)));
+    if (mixed(c)) {
+        if ((rc = dalloc(c, &c->f_u, N)) || (rc = dalloc(c, &c->f_temp, N)) || (rc = dalloc(c, &c->f_g1, N)) ||
+            (rc = dalloc(c, &c->f_tp, (size_t)ncol * c->nz)) ||
+            (rc = dalloc(c, &c->f_pp, (size_t)ncol * c->countz)) ||
+            (rc = dalloc(c, &c->f_fref, (size_t)c->n_profiles * c->nz)) ||
+            (rc = dalloc(c, &c->d_Tref, c->nz)))
+            return fail(rc);
+        if ((rc = upload(c, &c->c32.cxm, to_float(cxm))) || (rc = upload(c, &c->c32.cxp, to_float(cxp))) ||
+            (rc = upload(c, &c->c32.cym, to_float(cym))) || (rc = upload(c, &c->c32.cyp, to_float(cyp))) ||
+            (rc = upload(c, &c->c32.czm, to_float(czm))) || (rc = upload(c, &c->c32.czp, to_float(czp))))
+            return fail(rc);
+        if ((rc = dalloc(c, &c->c32.fx.a, cxm.size())) || (rc = dalloc(c, &c->c32.fx.ib, cxm.size())) ||
+            (rc = dalloc(c, &c->c32.fx.cu, cxm.size())) || (rc = dalloc(c, &c->c32.fy.a, cym.size())) ||
+            (rc = dalloc(c, &c->c32.fy.ib, cym.size())) || (rc = dalloc(c, &c->c32.fy.cu, cym.size())))
+            return fail(rc);
+        GW_CUDA(cudaMemset(c->f_u, 0, N * sizeof(float)));
+        std::vector<double> zero(c->nz, 0.0);
+        if ((rc = set_reference_profile(c, zero.data()))) return fail(rc);
+    } else {
+        if ((rc = dalloc(c, &c->d_u, N)) || (rc = dalloc(c, &c->d_temp, N)) || (rc = dalloc(c, &c->d_g1, N)) ||
+            (rc = dalloc(c, &c->d_tp, (size_t)ncol * c->nz)) ||
+            (rc = dalloc(c, &c->d_pp, (size_t)ncol * c->countz)))
+            return fail(rc);
+        GW_CUDA(cudaMemset(c->d_u, 0, N * sizeof(double)));
+    }
     GW_CUDA(cudaMemset(c->d_outlet, 0, c->nbh * sizeof(double)));
     GW_CUDA(cudaMemset(c->d_energy, 0, c->nbh * sizeof(double)));
+    c->fused = unique_cols && gw_fused_supported(c);
+    if (c->fused && (rc = gw_fused_prepare(c))) return fail(rc);
+    if (mixed(c) && !c->fused)
+        return fail(gw_fail(GW_ERR_UNSUPPORTED, "GW_PREC_MIXED needs the fused step: nz too large or "
+                                                "a pipe column shared by two boreholes"));
     *out = c;
     return GW_OK;
 }
@@ -189,10 +283,11 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
 int gw_destroy(gw_ctx *c) {
     if (!c) return GW_OK;
     cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
-    for (void *p : c->allocations) cudaFree(p);
+    for (void *p : c->allocations) if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return GW_OK;
@@ -212,6 +307,15 @@ int gw_set_field(gw_ctx *c, const double *T) {
     if (!c || !T) return gw_fail(GW_ERR_ARG, "NULL argument");
     int rc = set_device(c);
     if (rc) return rc;
+    if (mixed(c)) {
+        if ((rc = set_reference_profile(c, T))) return rc;
+        const size_t N = ncell(c);
+        std::vector<float> th(N);
+        const int nz = c->nz;
+        for (size_t q = 0; q < N; ++q) th[q] = (float)(T[q] - c->Tref[q % nz]);
+        GW_CUDA(cudaMemcpy(c->f_u, th.data(), N * sizeof(float), cudaMemcpyHostToDevice));
+        return GW_OK;
+    }
     GW_CUDA(cudaMemcpyAsync(c->d_u, T, ncell(c) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     return sync(c);
 }
@@ -220,6 +324,15 @@ int gw_get_field(gw_ctx *c, double *T) {
     if (!c || !T) return gw_fail(GW_ERR_ARG, "NULL argument");
     int rc = set_device(c);
     if (rc) return rc;
+    if (mixed(c)) {
+        const size_t N = ncell(c);
+        std::vector<float> th(N);
+        GW_CUDA(cudaMemcpyAsync(th.data(), c->f_u, N * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        if ((rc = sync(c))) return rc;
+        const int nz = c->nz;
+        for (size_t q = 0; q < N; ++q) T[q] = (double)th[q] + c->Tref[q % nz];
+        return GW_OK;
+    }
     GW_CUDA(cudaMemcpyAsync(T, c->d_u, ncell(c) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     return sync(c);
 }
@@ -307,6 +420,7 @@ int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
     if ((rc = gw_rock2_choose(dt, c->eigen_estimate, max_stages, &s, &covered))) return rc;
     if (nsteps > c->series_cap) {
         if (c->d_series) {
+            GW_CUDA(cudaStreamSynchronize(c->stream));
             cudaFree(c->d_series);
             for (auto &p : c->allocations) if (p == c->d_series) p = nullptr;
             c->d_series = nullptr;
@@ -321,11 +435,17 @@ int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
     if ((rc = gw_ensure_factors(c, dt / 2))) return rc;
     if (!c->graph || c->graph_dt != dt || c->graph_s != s) {
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+        if (c->fused && (rc = upload_stages(c, dt, s))) return rc;
         cudaGraph_t g;
         GW_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        int r1 = rock2_step(c, c->d_u, c->d_g1, c->d_temp, dt, s);
-        int r2 = r1 ? r1 : adi_adv(c, c->d_u, c->d_temp, dt);
-        int r3 = r2 ? r2 : gw_launch_record(c, dt);
+        int r3;
+        if (c->fused) {
+            r3 = gw_fused_step(c, dt, s);
+        } else {
+            int r1 = rock2_step(c, c->d_u, c->d_g1, c->d_temp, dt, s);
+            int r2 = r1 ? r1 : adi_adv(c, c->d_u, c->d_temp, dt);
+            r3 = r2 ? r2 : gw_launch_record(c, dt);
+        }
         cudaError_t e = cudaStreamEndCapture(c->stream, &g);
         if (r3) { if (e == cudaSuccess) cudaGraphDestroy(g); return r3; }
         if (e != cudaSuccess) return gw_cuda_fail(e, "cudaStreamEndCapture");
@@ -354,33 +474,32 @@ int gw_get_last_step_time(gw_ctx *c, double *ms) {
 int gw_profile_kernels(gw_ctx *c, double dt, int reps, double *ms_out) {
     if (!c || !ms_out) return gw_fail(GW_ERR_ARG, "NULL argument");
     if (reps < 1 || !(dt > 0)) return gw_fail(GW_ERR_ARG, "reps >= 1 and dt > 0 required");
+    if (!c->fused) return gw_fail(GW_ERR_UNSUPPORTED, "this context runs the modular step");
     int rc = set_device(c);
     if (rc || (rc = gw_ensure_factors(c, dt / 2))) return rc;
+    int s, covered;
+    if ((rc = gw_rock2_choose(dt, c->eigen_estimate, 100, &s, &covered))) return rc;
+    if ((rc = upload_stages(c, dt, s))) return rc;
+    c->graph_dt = -1.0;   // the stage table may differ from the captured step's
     const size_t N = ncell(c);
-    // keep the state: u -> g1 copy, restored at the end
-    GW_CUDA(cudaMemcpyAsync(c->d_g1, c->d_u, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-    double *u = c->d_u, *t = c->d_temp, *g = c->d_g1;
-    for (int kcls = 0; kcls < GW_KERNEL_COUNT; ++kcls) {
+    void *u = mixed(c) ? (void *)c->f_u : (void *)c->d_u;
+    void *bak = mixed(c) ? (void *)c->f_g1 : (void *)c->d_g1;
+    const size_t bytes = N * (mixed(c) ? sizeof(float) : sizeof(double));
+    GW_CUDA(cudaMemcpyAsync(bak, u, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    for (int part = 0; part < GW_KERNEL_COUNT; ++part) {
         float total = 0.f;
         for (int r = 0; r < reps; ++r) {
             GW_CUDA(cudaEventRecord(c->ev0, c->stream));
-            switch (kcls) {
-                case GW_KERNEL_ZSTAGE: rc = gw_launch_zstage(c, t, g, u, dt * 0.1, 0.5, 0); break;
-                case GW_KERNEL_EXPLICIT: rc = gw_launch_explicit(c, t, g, dt / 2, r % 2 ? GW_DIR_X : GW_DIR_Y); break;
-                case GW_KERNEL_THOMAS_X: rc = gw_launch_thomas(c, t, g, GW_DIR_X); break;
-                case GW_KERNEL_THOMAS_Y: rc = gw_launch_thomas(c, t, g, GW_DIR_Y); break;
-                default: rc = gw_launch_advection(c, t, dt / 2); break;
-            }
-            if (rc) return rc;
+            if ((rc = gw_fused_time_part(c, dt, s, part))) return rc;
             GW_CUDA(cudaEventRecord(c->ev1, c->stream));
             if ((rc = sync(c))) return rc;
             float ms = 0.f;
             GW_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
             total += ms;
         }
-        ms_out[kcls] = total / reps;
+        ms_out[part] = total / reps;
     }
-    GW_CUDA(cudaMemcpyAsync(c->d_u, c->d_g1, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    GW_CUDA(cudaMemcpyAsync(u, bak, bytes, cudaMemcpyDeviceToDevice, c->stream));
     return sync(c);
 }
 
@@ -422,7 +541,10 @@ int gw_reset_energy(gw_ctx *c) {
 int gw_check_finite(gw_ctx *c) {
     if (!c) return gw_fail(GW_ERR_ARG, "NULL argument");
     int rc = set_device(c);
-    if (rc || (rc = gw_launch_check_finite(c, c->d_u, ncell(c)))) return rc;
+    if (rc) return rc;
+    if (mixed(c)) rc = gw_fused_check_finite(c);
+    else rc = gw_launch_check_finite(c, c->d_u, ncell(c));
+    if (rc) return rc;
     int flag = 0;
     GW_CUDA(cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     if ((rc = sync(c))) return rc;

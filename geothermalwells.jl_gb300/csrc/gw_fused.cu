@@ -1,0 +1,538 @@
+// gw_fused.cu -- the fused time step used by gw_step, for both precisions.
+//
+// Per step the field crosses HBM three times:
+//   1. k_rock2_col: every ROCK2 stage of the z-diffusion for one z-column,
+//      the column held in shared memory (the z-stencil only couples levels
+//      of one column, so all stages run without touching HBM in between);
+//   2. k_half_step (x-lines): explicit y-sweep + advected pipe values +
+//      Thomas x-solve, one thread per line, the explicit sweep evaluated on
+//      the fly while the forward elimination streams the line;
+//   3. k_half_step (y-lines): explicit x-sweep + pipe values + Thomas y-solve.
+// Before each half step the pipe columns (5-9 % of the columns) get the
+// explicit sweep into a compact [column][level] buffer on which the outlet
+// mean, the per-level annulus means and the semi-Lagrangian advection run.
+//
+// Storage type T: double (GW_PREC_FP64) or float (GW_PREC_MIXED).  The mixed
+// path stores theta = T - T_ref(z) (T_ref = the initial field's first
+// column), so far-field cells carry small numbers whose increments are not
+// absorbed by float rounding; A_x and A_y annihilate T_ref, A_z T_ref enters
+// as a per-(column profile, level) source term, and the pipe advection
+// converts to absolute temperature in double.  ROCK2 in the mixed path
+// accumulates its stages as increments over the column's start value, so the
+// stored field is rounded once per step.
+#include <cuda_runtime.h>
+
+#include "gw_internal.h"
+#include "gw_fused.h"
+
+namespace {
+
+inline unsigned grid_for(long long n, int block) { return (unsigned)((n + block - 1) / block); }
+
+// ---------------------------------------------------------------------------
+// 1. ROCK2 on whole columns
+// sc: per recurrence stage j = 1..s-2: (h mu_j, kappa_j); then (h sigma,
+// h tau / sigma, 1 - tau / sigma^2).
+template <typename T, bool INC>
+__global__ void __launch_bounds__(256) k_rock2_col(T *__restrict__ u, const int *__restrict__ colprof,
+                                                   const T *__restrict__ czm,
+                                                   const T *__restrict__ czp,
+                                                   const T *__restrict__ fref,
+                                                   const double *__restrict__ sc, int s, int nz,
+                                                   long long ncols) {
+    // shared memory: base (the column at the step start), b0, and for the
+    // increment form F0 = A base (+ source) and b1.  A stage reads its input
+    // as a stencil and the stage before it only at its own level, so each
+    // stage overwrites the older of the two.
+    extern __shared__ unsigned char smem_raw[];
+    T *base = reinterpret_cast<T *>(smem_raw);
+    T *b0 = base + nz;
+    T *F0 = b0 + nz;
+    T *b1 = F0 + nz;
+    const int nrec = s - 2;
+    for (long long col = blockIdx.x; col < ncols; col += gridDim.x) {
+        const int p = colprof[col];
+        const T *cmc = czm + (size_t)p * nz;
+        const T *cpc = czp + (size_t)p * nz;
+        T *uc = u + col * nz;
+        for (int k = threadIdx.x; k < nz; k += blockDim.x) base[k] = uc[k];
+        __syncthreads();
+        // A_z on a column in shared memory; Neumann ends (src/solver.jl:95-109)
+        auto A = [&](const T *g, int k) {
+            T gc = g[k];
+            T gp = k < nz - 1 ? g[k + 1] : gc;
+            T gm = k > 0 ? g[k - 1] : gc;
+            return __ldg(cpc + k) * (gp - gc) - __ldg(cmc + k) * (gc - gm);
+        };
+        T *prev, *cur;
+        if (INC) {
+            for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+                T f = A(base, k);
+                if (fref) f += __ldg(fref + (size_t)p * nz + k);
+                F0[k] = f;
+                b0[k] = T(0);
+                b1[k] = T(0);
+            }
+            prev = b0;
+            cur = b1;
+            __syncthreads();
+        } else {
+            prev = nullptr;
+            cur = base;
+        }
+        // recurrence g_j = g_{j-1} + h mu_j A g_{j-1} + kappa_j (g_{j-1} - g_{j-2})
+        for (int j = 0; j < nrec; ++j) {
+            const T hmu = (T)sc[2 * j], kap = (T)sc[2 * j + 1];
+            T *out = prev ? prev : b0;
+            for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+                T gc = cur[k];
+                T a = A(cur, k);
+                if (INC) a += F0[k];
+                T gp = prev ? prev[k] : gc;
+                out[k] = gc + hmu * a + kap * (gc - gp);
+            }
+            __syncthreads();
+            prev = cur;
+            cur = out;
+        }
+        // finishing procedure: gq = gp + h sigma A gp;
+        // y = gq + (h tau / sigma) A gq + (1 - tau / sigma^2) (gq - gp)
+        const T hs = (T)sc[2 * nrec], hts = (T)sc[2 * nrec + 1], c3 = (T)sc[2 * nrec + 2];
+        T *q = prev ? prev : b0;
+        for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+            T a = A(cur, k);
+            if (INC) a += F0[k];
+            q[k] = cur[k] + hs * a;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+            T gq = q[k];
+            T a = A(q, k);
+            if (INC) a += F0[k];
+            T y = gq + hts * a + c3 * (gq - cur[k]);
+            uc[k] = INC ? base[k] + y : y;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2. pipe columns: explicit sweep (I + h A_dir) into tp[q][k], all levels
+template <typename T>
+__global__ void __launch_bounds__(256) k_pipe_explicit(T *__restrict__ tp, const T *__restrict__ src,
+                                                       const int *__restrict__ pi,
+                                                       const int *__restrict__ pj,
+                                                       const int *__restrict__ zclass,
+                                                       const T *__restrict__ cmt,
+                                                       const T *__restrict__ cpt, int nx, int ny,
+                                                       int nz, int ncol, double h, int dir) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)ncol * nz) return;
+    const int k = (int)(e % nz);
+    const int q = (int)(e / nz);
+    const int i = pi[q], j = pj[q];
+    const long long c = k + (long long)nz * (j + (long long)ny * i);
+    const int zc = zclass[k];
+    T xc = src[c], xp, xm;
+    size_t t;
+    if (dir == GW_DIR_X) {
+        long long st = (long long)nz * ny;
+        xp = (i < nx - 1) ? src[c + st] : xc;
+        xm = (i > 0) ? src[c - st] : xc;
+        t = ((size_t)zc * ny + j) * nx + i;
+    } else {
+        xp = (j < ny - 1) ? src[c + nz] : xc;
+        xm = (j > 0) ? src[c - nz] : xc;
+        t = ((size_t)zc * nx + i) * ny + j;
+    }
+    T a = __ldg(cpt + t) * (xp - xc) - __ldg(cmt + t) * (xc - xm);
+    tp[e] = fma((T)h, a, xc);
+}
+
+// absolute temperature of a pipe value (theta + T_ref in the mixed path)
+template <typename T>
+__device__ __forceinline__ double absT(T v, const double *Tref, int k) {
+    return Tref ? (double)v + Tref[k] : (double)v;
+}
+
+// kernel_accumulate_outlet! (src/solver.jl:267-282) on the compact pipe buffer
+template <typename T>
+__global__ void __launch_bounds__(256) k_outlet_c(double *__restrict__ outlet,
+                                                  const T *__restrict__ tp,
+                                                  const double *__restrict__ gz,
+                                                  const GwBhDev *__restrict__ bh,
+                                                  const double *__restrict__ Tref, int nz, double dt) {
+    const int b = blockIdx.x;
+    const GwBhDev B = bh[b];
+    const double zmax = B.v_inner * dt;
+    __shared__ int s_nlev;
+    __shared__ double s_red[256];
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = nz;
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (gz[mid] <= zmax) lo = mid + 1; else hi = mid;
+        }
+        s_nlev = lo;
+    }
+    __syncthreads();
+    const int nlev = s_nlev;
+    const long long tot = (long long)B.inner_count * nlev;
+    double acc = 0.0;
+    for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
+        int q = B.inner_begin + (int)(e / nlev);
+        int k = (int)(e % nlev);
+        acc += absT(tp[(size_t)q * nz + k], Tref, k);
+    }
+    s_red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) s_red[threadIdx.x] += s_red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) outlet[b] = s_red[0] / (double)tot;
+}
+
+constexpr int kAnnChunks = 32;
+
+// annulus sums per (borehole, chunk of annulus columns, level)
+template <typename T>
+__global__ void __launch_bounds__(128) k_annulus_part(double *__restrict__ part, const T *__restrict__ tp,
+                                                      const GwBhDev *__restrict__ bh,
+                                                      const double *__restrict__ Tref, int nz) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ch = blockIdx.y, b = blockIdx.z;
+    if (k >= nz) return;
+    const GwBhDev B = bh[b];
+    const int per = (B.outer_count + kAnnChunks - 1) / kAnnChunks;
+    const int q0 = B.outer_begin + ch * per;
+    const int q1 = min(q0 + per, B.outer_begin + B.outer_count);
+    double s = 0.0;
+    for (int q = q0; q < q1; ++q) s += absT(tp[(size_t)q * nz + k], Tref, k);
+    part[((size_t)b * kAnnChunks + ch) * nz + k] = s;
+}
+
+__global__ void __launch_bounds__(128) k_annulus_fin(double *__restrict__ mean,
+                                                     const double *__restrict__ part,
+                                                     const GwBhDev *__restrict__ bh, int nz) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    if (k >= nz) return;
+    double s = 0.0;
+    for (int ch = 0; ch < kAnnChunks; ++ch) s += part[((size_t)b * kAnnChunks + ch) * nz + k];
+    mean[(size_t)b * nz + k] = s / (double)bh[b].outer_count;
+}
+
+__device__ __forceinline__ void interp_c(const double *__restrict__ g, int n, double dep, int &il,
+                                         int &ir, double &alpha) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = lo + ((hi - lo) >> 1);
+        if (g[mid] < dep) lo = mid + 1; else hi = mid;
+    }
+    ir = lo;
+    il = lo - 1;
+    if (il < 0) il = 0;
+    if (ir > n - 1) ir = n - 1;
+    alpha = __ddiv_rn(__dsub_rn(dep, g[il]), __dsub_rn(g[ir], g[il]));
+}
+
+// kernel_advection! (src/solver.jl:285-360) on the compact buffer; the
+// result (minus T_ref in the mixed path) goes to pp[q][k], k < countz.
+template <typename T>
+__global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *__restrict__ tp,
+                                                  const double *__restrict__ gz,
+                                                  const int *__restrict__ pb,
+                                                  const GwBhDev *__restrict__ bh,
+                                                  const double *__restrict__ ann_mean,
+                                                  const double *__restrict__ outlet,
+                                                  const double *__restrict__ Tref, int n_inner,
+                                                  int ncol, int nz, int countz, double dt,
+                                                  int inlet_kind, double inlet_param) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)ncol * countz) return;
+    const int k = (int)(e % countz);
+    const int q = (int)(e / countz);
+    const int b = pb[q];
+    const GwBhDev B = bh[b];
+    const T *col = tp + (size_t)q * nz;
+    const double z = gz[k];
+    double v;
+    if (z > B.h) {
+        v = absT(col[k], Tref, k);
+    } else if (q < n_inner) {
+        double zd = __fma_rn(B.v_inner, dt, z);
+        if (zd > B.h) {
+            double dt1 = __ddiv_rn(__dsub_rn(B.h, z), B.v_inner);
+            double dt2 = __dsub_rn(dt, dt1);
+            double zd2 = __fma_rn(-B.v_outer, dt2, B.h);
+            int il, ir; double a;
+            interp_c(gz, nz, zd2, il, ir, a);
+            const double *m = ann_mean + (size_t)b * nz;
+            v = __fma_rn(a, m[ir], __dmul_rn(__dsub_rn(1.0, a), m[il]));
+        } else {
+            int il, ir; double a;
+            interp_c(gz, nz, zd, il, ir, a);
+            v = __fma_rn(a, absT(col[ir], Tref, ir), __dmul_rn(__dsub_rn(1.0, a), absT(col[il], Tref, il)));
+        }
+    } else {
+        double zd = __fma_rn(-B.v_outer, dt, z);
+        if (zd <= 0.0) {
+            v = inlet_kind == GW_INLET_CONSTANT ? inlet_param : outlet[b] - inlet_param;
+        } else {
+            int il, ir; double a;
+            interp_c(gz, nz, zd, il, ir, a);
+            v = __fma_rn(a, absT(col[ir], Tref, ir), __dmul_rn(__dsub_rn(1.0, a), absT(col[il], Tref, il)));
+        }
+    }
+    pp[e] = (T)(Tref ? v - Tref[k] : v);
+}
+
+// ---------------------------------------------------------------------------
+// 3. half step: explicit sweep in direction edir + pipe values + Thomas
+//    along the other direction.  XL: x-lines (explicit y), else y-lines.
+template <typename T, bool XL>
+__global__ void __launch_bounds__(128) k_half_step(T *__restrict__ dst, const T *__restrict__ src,
+                                                   const T *__restrict__ pp,
+                                                   const int *__restrict__ pipe_of,
+                                                   const int *__restrict__ zclass,
+                                                   const T *__restrict__ ecm,
+                                                   const T *__restrict__ ecp,
+                                                   const T *__restrict__ fa,
+                                                   const T *__restrict__ fib,
+                                                   const T *__restrict__ fcu, int nx, int ny, int nz,
+                                                   int countz, double h) {
+    const int nl = XL ? ny : nx;   // lines per level
+    const int N = XL ? nx : ny;    // line length
+    long long L = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= (long long)nz * nl) return;
+    const int k = (int)(L % nz);
+    const int m = (int)(L / nz);
+    const int zc = zclass[k];
+    const size_t fb = ((size_t)zc * nl + m) * N;
+    const bool in_pipe_levels = k < countz;
+    long long stride, off0, es;   // es: neighbour offset of the explicit direction
+    bool has_m, has_p;
+    if (XL) {    // line (k, j = m); explicit y: neighbours j -+ 1
+        stride = (long long)nz * ny;
+        off0 = k + (long long)nz * m;
+        es = nz;
+        has_m = m > 0;
+        has_p = m < ny - 1;
+    } else {     // line (k, i = m); explicit x: neighbours i -+ 1
+        stride = nz;
+        off0 = k + (long long)nz * ny * m;
+        es = (long long)nz * ny;
+        has_m = m > 0;
+        has_p = m < nx - 1;
+    }
+    const T hh = (T)h;
+    T y = T(0);
+    for (int l = 0; l < N; ++l) {
+        const long long o = off0 + l * stride;
+        // column index i * ny + j of row l
+        const int colidx = XL ? l * ny + m : m * ny + l;
+        const int q = in_pipe_levels ? __ldg(pipe_of + colidx) : -1;
+        T rhs;
+        if (q >= 0) {
+            rhs = pp[(size_t)q * countz + k];
+        } else {
+            const T xc = src[o];
+            const T xp = has_p ? src[o + es] : xc;
+            const T xm = has_m ? src[o - es] : xc;
+            const size_t t = XL ? ((size_t)zc * nx + l) * ny + m : ((size_t)zc * ny + l) * nx + m;
+            const T a = __ldg(ecp + t) * (xp - xc) - __ldg(ecm + t) * (xc - xm);
+            rhs = fma(hh, a, xc);
+        }
+        y = (rhs - __ldg(fa + fb + l) * y) * __ldg(fib + fb + l);
+        dst[o] = y;
+    }
+    T x = y;
+    for (int l = N - 2; l >= 0; --l) {
+        const long long o = off0 + l * stride;
+        x = dst[o] - __ldg(fcu + fb + l) * x;
+        dst[o] = x;
+    }
+}
+
+template <typename T>
+__global__ void k_finite(const T *__restrict__ u, size_t n, int *__restrict__ flag) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t s = (size_t)gridDim.x * blockDim.x;
+    bool bad = false;
+    for (; i < n; i += s) bad |= !isfinite((double)u[i]);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
+}
+
+template <typename T>
+struct Bufs {
+    T *u, *temp, *tp, *pp;
+    const GwCoefTables<T> *ct;
+    const T *fref;
+    const double *Tref;
+};
+
+template <typename T>
+Bufs<T> bufs(gw_ctx *c);
+template <>
+Bufs<double> bufs<double>(gw_ctx *c) {
+    return {c->d_u, c->d_temp, c->d_tp, c->d_pp, &c->c64, nullptr, nullptr};
+}
+template <>
+Bufs<float> bufs<float>(gw_ctx *c) {
+    return {c->f_u, c->f_temp, c->f_tp, c->f_pp, &c->c32, c->f_fref, c->d_Tref};
+}
+
+template <typename T>
+size_t rock2_smem(int nz) {
+    const bool inc = sizeof(T) == 4;   // the float path runs the increment form
+    return (size_t)nz * sizeof(T) * (inc ? 4 : 2);
+}
+
+template <typename T>
+int launch_rock2(gw_ctx *c, int s) {
+    Bufs<T> B = bufs<T>(c);
+    const long long ncols = (long long)c->nx * c->ny;
+    const size_t sm = rock2_smem<T>(c->nz);
+    unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid ? ncols : c->rock2_grid);
+    if (sizeof(T) == 4)
+        k_rock2_col<float, true><<<grid, 256, sm, c->stream>>>(
+            (float *)B.u, c->d_colprof, (const float *)B.ct->czm, (const float *)B.ct->czp,
+            (const float *)B.fref, c->d_stage, s, c->nz, ncols);
+    else
+        k_rock2_col<double, false><<<grid, 256, sm, c->stream>>>(
+            (double *)B.u, c->d_colprof, (const double *)B.ct->czm, (const double *)B.ct->czp,
+            nullptr, c->d_stage, s, c->nz, ncols);
+    GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}
+
+// explicit sweep along edir at the pipe columns, outlet/annulus means, advection
+template <typename T>
+int launch_pipe(gw_ctx *c, const T *src, int edir, double h) {
+    Bufs<T> B = bufs<T>(c);
+    const int ncol = c->n_inner + c->n_outer;
+    if (ncol == 0) {
+        k_outlet_c<T><<<c->nbh, 256, 0, c->stream>>>(c->d_outlet, B.tp, c->d_gz, c->d_bh, B.Tref,
+                                                     c->nz, h);
+        GW_CUDA(cudaGetLastError());
+        return GW_OK;
+    }
+    const T *cm = edir == GW_DIR_X ? B.ct->cxm : B.ct->cym;
+    const T *cp = edir == GW_DIR_X ? B.ct->cxp : B.ct->cyp;
+    long long n = (long long)ncol * c->nz;
+    k_pipe_explicit<T><<<grid_for(n, 256), 256, 0, c->stream>>>(B.tp, src, c->d_pipe_i, c->d_pipe_j,
+                                                                c->d_zclass, cm, cp, c->nx, c->ny,
+                                                                c->nz, ncol, h, edir);
+    GW_CUDA(cudaGetLastError());
+    k_outlet_c<T><<<c->nbh, 256, 0, c->stream>>>(c->d_outlet, B.tp, c->d_gz, c->d_bh, B.Tref, c->nz, h);
+    GW_CUDA(cudaGetLastError());
+    dim3 gp(grid_for(c->nz, 128), kAnnChunks, c->nbh);
+    k_annulus_part<T><<<gp, 128, 0, c->stream>>>(c->d_annpart, B.tp, c->d_bh, B.Tref, c->nz);
+    GW_CUDA(cudaGetLastError());
+    dim3 gf(grid_for(c->nz, 128), c->nbh);
+    k_annulus_fin<<<gf, 128, 0, c->stream>>>(c->d_annmean, c->d_annpart, c->d_bh, c->nz);
+    GW_CUDA(cudaGetLastError());
+    long long na = (long long)ncol * c->countz;
+    if (na > 0) {
+        k_advect_c<T><<<grid_for(na, 256), 256, 0, c->stream>>>(
+            B.pp, B.tp, c->d_gz, c->d_pipe_b, c->d_bh, c->d_annmean, c->d_outlet, B.Tref, c->n_inner,
+            ncol, c->nz, c->countz, h, c->inlet_kind, c->inlet_param);
+        GW_CUDA(cudaGetLastError());
+    }
+    return GW_OK;
+}
+
+template <typename T>
+int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h) {
+    Bufs<T> B = bufs<T>(c);
+    const GwFactors<T> &f = xlines ? B.ct->fx : B.ct->fy;
+    const T *ecm = xlines ? B.ct->cym : B.ct->cxm;
+    const T *ecp = xlines ? B.ct->cyp : B.ct->cxp;
+    long long lines = (long long)c->nz * (xlines ? c->ny : c->nx);
+    if (xlines)
+        k_half_step<T, true><<<grid_for(lines, 128), 128, 0, c->stream>>>(
+            dst, src, B.pp, c->d_pipe_of, c->d_zclass, ecm, ecp, f.a, f.ib, f.cu, c->nx, c->ny,
+            c->nz, c->countz, h);
+    else
+        k_half_step<T, false><<<grid_for(lines, 128), 128, 0, c->stream>>>(
+            dst, src, B.pp, c->d_pipe_of, c->d_zclass, ecm, ecp, f.a, f.ib, f.cu, c->nx, c->ny,
+            c->nz, c->countz, h);
+    GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}
+
+template <typename T>
+int fused_step(gw_ctx *c, double dt, int s) {
+    Bufs<T> B = bufs<T>(c);
+    int rc;
+    if ((rc = launch_rock2<T>(c, s))) return rc;
+    if ((rc = launch_pipe<T>(c, B.u, GW_DIR_Y, dt / 2))) return rc;
+    if ((rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2))) return rc;
+    if ((rc = launch_pipe<T>(c, B.temp, GW_DIR_X, dt / 2))) return rc;
+    if ((rc = launch_half<T>(c, B.u, B.temp, 0, dt / 2))) return rc;
+    return gw_launch_record(c, dt);
+}
+
+template <typename T>
+int time_part(gw_ctx *c, double dt, int s, int part) {
+    Bufs<T> B = bufs<T>(c);
+    switch (part) {
+        case GW_KERNEL_ROCK2: return launch_rock2<T>(c, s);
+        case GW_KERNEL_HALF_X: return launch_half<T>(c, B.temp, B.u, 1, dt / 2);
+        case GW_KERNEL_HALF_Y: return launch_half<T>(c, B.temp, B.u, 0, dt / 2);
+        default: return launch_pipe<T>(c, B.u, GW_DIR_Y, dt / 2);
+    }
+}
+
+}  // namespace
+
+int gw_fused_supported(const gw_ctx *c) {
+    const size_t need = c->precision == GW_PREC_MIXED ? rock2_smem<float>(c->nz) : rock2_smem<double>(c->nz);
+    return need <= 200 * 1024;
+}
+
+int gw_fused_prepare(gw_ctx *c) {
+    // shared-memory opt-in for the column kernel (once per context is enough)
+    cudaError_t e;
+    if (c->precision == GW_PREC_MIXED)
+        e = cudaFuncSetAttribute(k_rock2_col<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)rock2_smem<float>(c->nz));
+    else
+        e = cudaFuncSetAttribute(k_rock2_col<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)rock2_smem<double>(c->nz));
+    if (e != cudaSuccess) return gw_cuda_fail(e, "cudaFuncSetAttribute(k_rock2_col)");
+    int per_sm = 0;
+    if (c->precision == GW_PREC_MIXED)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rock2_col<float, true>, 256,
+                                                          rock2_smem<float>(c->nz));
+    else
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rock2_col<double, false>, 256,
+                                                          rock2_smem<double>(c->nz));
+    if (e != cudaSuccess) return gw_cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (e != cudaSuccess) return gw_cuda_fail(e, "cudaDeviceGetAttribute");
+    c->rock2_grid = (per_sm > 0 ? per_sm : 1) * sms * 8;
+    return GW_OK;
+}
+
+int gw_fused_step(gw_ctx *c, double dt, int s) {
+    return c->precision == GW_PREC_MIXED ? fused_step<float>(c, dt, s) : fused_step<double>(c, dt, s);
+}
+
+int gw_fused_time_part(gw_ctx *c, double dt, int s, int part) {
+    return c->precision == GW_PREC_MIXED ? time_part<float>(c, dt, s, part)
+                                         : time_part<double>(c, dt, s, part);
+}
+
+int gw_fused_check_finite(gw_ctx *c) {
+    size_t n = (size_t)c->nx * c->ny * c->nz;
+    GW_CUDA(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
+    if (c->precision == GW_PREC_MIXED)
+        k_finite<float><<<1216, 256, 0, c->stream>>>(c->f_u, n, c->d_flag);
+    else
+        k_finite<double><<<1216, 256, 0, c->stream>>>(c->d_u, n, c->d_flag);
+    GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}

@@ -1,0 +1,15 @@
+// gw_fused.h -- the fused step (gw_fused.cu) as seen by gw_api.cu.
+#pragma once
+#include "gw_internal.h"
+
+// 1 if the column kernel's shared memory fits this context's nz.
+int gw_fused_supported(const gw_ctx *c);
+// Per-context kernel attributes and the column kernel's grid size.
+int gw_fused_prepare(gw_ctx *c);
+// Enqueue one full step (ROCK2 columns, two half steps, record) on c->stream.
+// Requires the Thomas factors for dt/2 and the stage table c->d_stage for s.
+int gw_fused_step(gw_ctx *c, double dt, int s);
+// Enqueue one kernel class of the step (GW_KERNEL_*), for timing.
+int gw_fused_time_part(gw_ctx *c, double dt, int s, int part);
+// Set c->d_flag if the state holds a NaN or Inf.
+int gw_fused_check_finite(gw_ctx *c);

@@ -79,8 +79,20 @@ struct gw_ctx {
     int *d_flag = nullptr;
     int series_cap = 0;
     int last_nsteps = 0;
-    // mixed path state (allocated for GW_PREC_MIXED)
-    float *f_u = nullptr, *f_temp = nullptr, *f_g1 = nullptr, *f_g2 = nullptr, *f_utmp = nullptr;
+    // fused step (both precisions)
+    int *d_pipe_of = nullptr;         // [nx*ny] pipe-column index or -1
+    double *d_annpart = nullptr;      // [nbh][32][nz] partial annulus sums
+    double *d_stage = nullptr;        // ROCK2 stage coefficients of the captured step
+    double *d_tp = nullptr;           // double path: [ncol][nz] swept pipe columns
+    double *d_pp = nullptr;           // double path: [ncol][countz] advected pipe values
+    int rock2_grid = 0;
+    bool fused = false;
+    // mixed path state (GW_PREC_MIXED): theta = T - T_ref(z) in float
+    float *f_u = nullptr, *f_temp = nullptr, *f_g1 = nullptr, *f_tp = nullptr, *f_pp = nullptr;
+    float *f_fref = nullptr;          // [profile][nz] A_z T_ref
+    double *d_Tref = nullptr;         // [nz]
+    std::vector<double> Tref;         // host copy
+    std::vector<double> h_czm, h_czp; // host copies of the z coefficients
 
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_step_ms = 0.0;
@@ -123,3 +135,5 @@ int gw_launch_advection(gw_ctx *c, double *phi, double dt);
 int gw_launch_record(gw_ctx *c, double dt);
 int gw_launch_check_finite(gw_ctx *c, const double *u, size_t n);
 int gw_ensure_factors(gw_ctx *c, double h);
+
+#define GW_STAGE_TABLE 208   // doubles: 2 per recurrence stage (<= 98) + 3

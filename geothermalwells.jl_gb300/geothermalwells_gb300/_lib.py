@@ -78,7 +78,7 @@ SIGNATURES = {
     "gw_profile_kernels": (_i, [_vp, _d, _i, _dp]),
     "gw_advection_noalloc": (_i, [_vp, _vp, _d, _d, _vp]),
 }
-KERNELS = ("zstage", "explicit", "thomas_x", "thomas_y", "advection")
+KERNELS = ("rock2_columns", "half_step_x", "half_step_y", "pipe")
 
 _lib = None
 

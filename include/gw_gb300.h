@@ -141,17 +141,16 @@ int gw_check_finite(gw_ctx *ctx);
  * recorded on the context's stream around the graph launches. */
 int gw_get_last_step_time(gw_ctx *ctx, double *ms);
 
-/* Kernel timing for the roofline: runs each kernel class of one step of size
- * dt `reps` times on the context's buffers (the state u is restored
- * afterwards) and writes the mean device time per launch [ms] into
- * ms_out[GW_KERNEL_COUNT], indexed by GW_KERNEL_*.  Each launch is bracketed
- * by CUDA events on the context's stream. */
-#define GW_KERNEL_ZSTAGE 0     /* one ROCK2 stage of the z-stencil */
-#define GW_KERNEL_EXPLICIT 1   /* (I + dt/2 A_x) or (I + dt/2 A_y) sweep */
-#define GW_KERNEL_THOMAS_X 2   /* x-line solves */
-#define GW_KERNEL_THOMAS_Y 3   /* y-line solves */
-#define GW_KERNEL_ADVECTION 4  /* outlet mean + annulus mean + advect + scatter */
-#define GW_KERNEL_COUNT 5
+/* Kernel timing for the roofline: runs each kernel class of the fused step
+ * of size dt (in the context's precision) `reps` times on the context's
+ * buffers (the state u is restored afterwards) and writes the mean device
+ * time per launch [ms] into ms_out[GW_KERNEL_COUNT], indexed by GW_KERNEL_*.
+ * Each launch is bracketed by CUDA events on the context's stream. */
+#define GW_KERNEL_ROCK2 0      /* all ROCK2 stages of the z-diffusion, whole columns */
+#define GW_KERNEL_HALF_X 1     /* explicit y-sweep + pipe values + x-line Thomas */
+#define GW_KERNEL_HALF_Y 2     /* explicit x-sweep + pipe values + y-line Thomas */
+#define GW_KERNEL_PIPE 3       /* pipe columns: sweep, outlet/annulus means, advection */
+#define GW_KERNEL_COUNT 4
 int gw_profile_kernels(gw_ctx *ctx, double dt, int reps, double *ms_out);
 
 /* advection! (same result as gw_advection) for callers that must not make
