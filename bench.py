@@ -41,6 +41,8 @@ def parse():
     p.add_argument("--workload", default="large", choices=["large", "2mm"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-steps", type=int, default=1)
+    p.add_argument("--accuracy", type=int, default=0, metavar="NSTEPS",
+                   help="run FP64 and mixed for NSTEPS steps and report their differences")
     return p.parse_args()
 
 
@@ -261,8 +263,42 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_accuracy(args):
+    """Mixed vs FP64 on the same workload over NSTEPS steps: max |dT| of the
+    final field, the largest outlet-temperature difference over all steps and
+    the relative difference of the extracted heat."""
+    from geothermalwells_gb300 import (GB300, ODEProblem, ROCK2, create_cache, eigen_estimator,
+                                       rhs_diffusion_z, solve)
+    w = workload(args.workload)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        cache = create_cache(backend=GB300(precision=prec), gridx=w["gridx"], gridy=w["gridy"],
+                             gridz=w["gridz"], materials=w["materials"],
+                             boreholes=w["boreholes"], inlet_model=w["inlet_model"])
+        prob = ODEProblem(rhs_diffusion_z, w["T0"], (0.0, args.accuracy * w["dt"]), cache)
+        t0 = time.perf_counter()
+        sol = solve(prob, ROCK2(max_stages=100, eigen_est=eigen_estimator), dt=w["dt"])
+        res[prec] = (sol, time.perf_counter() - t0)
+        cache.close()
+    a, b = res["fp64"][0], res["mixed"][0]
+    line = {"accuracy": {"workload": w["name"], "steps": args.accuracy, "dt_s": w["dt"],
+                         "simulated_days": args.accuracy * w["dt"] / 86400.0,
+                         "field_max_abs_dT_K": float(np.max(np.abs(b.u[-1] - a.u[-1]))),
+                         "outlet_max_abs_err_K": float(np.max(np.abs(b.T_outlet - a.T_outlet))),
+                         "outlet_final_fp64_C": float(a.T_outlet[-1, 0]),
+                         "outlet_final_mixed_C": float(b.T_outlet[-1, 0]),
+                         "energy_fp64_J": float(a.energy[0]), "energy_mixed_J": float(b.energy[0]),
+                         "energy_rel_err": float(abs(b.energy[0] - a.energy[0]) / abs(a.energy[0])),
+                         "wall_s": {"fp64": res["fp64"][1], "mixed": res["mixed"][1]},
+                         "reference": "the FP64 GPU path (pinned to the FP64 oracle at 1e-10 in the parity tests)"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.accuracy:
+        run_accuracy(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -155,31 +155,36 @@ __device__ __forceinline__ double absT(T v, const double *Tref, int k) {
     return Tref ? (double)v + Tref[k] : (double)v;
 }
 
-// kernel_accumulate_outlet! (src/solver.jl:267-282) on the compact pipe buffer
-template <typename T>
-__global__ void __launch_bounds__(256) k_outlet_c(double *__restrict__ outlet,
-                                                  const T *__restrict__ tp,
-                                                  const double *__restrict__ gz,
-                                                  const GwBhDev *__restrict__ bh,
-                                                  const double *__restrict__ Tref, int nz, double dt) {
-    const int b = blockIdx.x;
-    const GwBhDev B = bh[b];
-    const double zmax = B.v_inner * dt;
-    __shared__ int s_nlev;
-    __shared__ double s_red[256];
-    if (threadIdx.x == 0) {
-        int lo = 0, hi = nz;
-        while (lo < hi) {
-            int mid = (lo + hi) >> 1;
-            if (gz[mid] <= zmax) lo = mid + 1; else hi = mid;
-        }
-        s_nlev = lo;
+// kernel_accumulate_outlet! (src/solver.jl:267-282) on the compact pipe
+// buffer: block (chunk, b) sums its share of the borehole's inner-pipe cells
+// with z <= v_inner * dt; k_outlet_fin adds the chunks in a fixed order.
+constexpr int kOutChunks = 64;
+
+__device__ __forceinline__ int outlet_levels(const double *__restrict__ gz, int nz, double zmax) {
+    int lo = 0, hi = nz;   // gz is sorted: the levels with gz <= zmax are a prefix
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (gz[mid] <= zmax) lo = mid + 1; else hi = mid;
     }
-    __syncthreads();
-    const int nlev = s_nlev;
+    return lo;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_outlet_part(double *__restrict__ part,
+                                                     const T *__restrict__ tp,
+                                                     const double *__restrict__ gz,
+                                                     const GwBhDev *__restrict__ bh,
+                                                     const double *__restrict__ Tref, int nz,
+                                                     double dt) {
+    const int ch = blockIdx.x, b = blockIdx.y;
+    const GwBhDev B = bh[b];
+    const int nlev = outlet_levels(gz, nz, B.v_inner * dt);
     const long long tot = (long long)B.inner_count * nlev;
+    const long long per = (tot + kOutChunks - 1) / kOutChunks;
+    const long long e0 = ch * per, e1 = min(e0 + per, tot);
+    __shared__ double s_red[256];
     double acc = 0.0;
-    for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
+    for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         int q = B.inner_begin + (int)(e / nlev);
         int k = (int)(e % nlev);
         acc += absT(tp[(size_t)q * nz + k], Tref, k);
@@ -190,7 +195,20 @@ __global__ void __launch_bounds__(256) k_outlet_c(double *__restrict__ outlet,
         if (threadIdx.x < w) s_red[threadIdx.x] += s_red[threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) outlet[b] = s_red[0] / (double)tot;
+    if (threadIdx.x == 0) part[(size_t)b * kOutChunks + ch] = s_red[0];
+}
+
+// outlet[b] = sum / count (0/0 = NaN when the window is empty, as in the reference)
+__global__ void k_outlet_fin(double *__restrict__ outlet, const double *__restrict__ part,
+                             const double *__restrict__ gz, const GwBhDev *__restrict__ bh, int nbh,
+                             int nz, double dt) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbh) return;
+    const GwBhDev B = bh[b];
+    const int nlev = outlet_levels(gz, nz, B.v_inner * dt);
+    double s = 0.0;
+    for (int ch = 0; ch < kOutChunks; ++ch) s += part[(size_t)b * kOutChunks + ch];
+    outlet[b] = s / (double)((long long)B.inner_count * nlev);
 }
 
 constexpr int kAnnChunks = 32;
@@ -328,26 +346,25 @@ __global__ void __launch_bounds__(128) k_half_step(T *__restrict__ dst, const T 
     }
     const T hh = (T)h;
     T y = T(0);
+    // every load of a row is independent of the elimination chain, so the
+    // unrolled loop can issue several rows' loads ahead of the dependent FMAs
+#pragma unroll 4
     for (int l = 0; l < N; ++l) {
         const long long o = off0 + l * stride;
-        // column index i * ny + j of row l
         const int colidx = XL ? l * ny + m : m * ny + l;
         const int q = in_pipe_levels ? __ldg(pipe_of + colidx) : -1;
-        T rhs;
-        if (q >= 0) {
-            rhs = pp[(size_t)q * countz + k];
-        } else {
-            const T xc = src[o];
-            const T xp = has_p ? src[o + es] : xc;
-            const T xm = has_m ? src[o - es] : xc;
-            const size_t t = XL ? ((size_t)zc * nx + l) * ny + m : ((size_t)zc * ny + l) * nx + m;
-            const T a = __ldg(ecp + t) * (xp - xc) - __ldg(ecm + t) * (xc - xm);
-            rhs = fma(hh, a, xc);
-        }
+        const T xc = src[o];
+        const T xp = has_p ? src[o + es] : xc;
+        const T xm = has_m ? src[o - es] : xc;
+        const size_t t = XL ? ((size_t)zc * nx + l) * ny + m : ((size_t)zc * ny + l) * nx + m;
+        const T a = __ldg(ecp + t) * (xp - xc) - __ldg(ecm + t) * (xc - xm);
+        T rhs = fma(hh, a, xc);
+        if (q >= 0) rhs = pp[(size_t)q * countz + k];
         y = (rhs - __ldg(fa + fb + l) * y) * __ldg(fib + fb + l);
         dst[o] = y;
     }
     T x = y;
+#pragma unroll 4
     for (int l = N - 2; l >= 0; --l) {
         const long long o = off0 + l * stride;
         x = dst[o] - __ldg(fcu + fb + l) * x;
@@ -412,12 +429,17 @@ template <typename T>
 int launch_pipe(gw_ctx *c, const T *src, int edir, double h) {
     Bufs<T> B = bufs<T>(c);
     const int ncol = c->n_inner + c->n_outer;
-    if (ncol == 0) {
-        k_outlet_c<T><<<c->nbh, 256, 0, c->stream>>>(c->d_outlet, B.tp, c->d_gz, c->d_bh, B.Tref,
-                                                     c->nz, h);
+    auto outlet = [&]() -> int {
+        k_outlet_part<T><<<dim3(kOutChunks, c->nbh), 256, 0, c->stream>>>(c->d_outpart, B.tp, c->d_gz,
+                                                                          c->d_bh, B.Tref, c->nz, h);
+        GW_CUDA(cudaGetLastError());
+        k_outlet_fin<<<grid_for(c->nbh, 128), 128, 0, c->stream>>>(c->d_outlet, c->d_outpart, c->d_gz,
+                                                                   c->d_bh, c->nbh, c->nz, h);
         GW_CUDA(cudaGetLastError());
         return GW_OK;
-    }
+    };
+    int rc;
+    if (ncol == 0) return outlet();
     const T *cm = edir == GW_DIR_X ? B.ct->cxm : B.ct->cym;
     const T *cp = edir == GW_DIR_X ? B.ct->cxp : B.ct->cyp;
     long long n = (long long)ncol * c->nz;
@@ -425,8 +447,7 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h) {
                                                                 c->d_zclass, cm, cp, c->nx, c->ny,
                                                                 c->nz, ncol, h, edir);
     GW_CUDA(cudaGetLastError());
-    k_outlet_c<T><<<c->nbh, 256, 0, c->stream>>>(c->d_outlet, B.tp, c->d_gz, c->d_bh, B.Tref, c->nz, h);
-    GW_CUDA(cudaGetLastError());
+    if ((rc = outlet())) return rc;
     dim3 gp(grid_for(c->nz, 128), kAnnChunks, c->nbh);
     k_annulus_part<T><<<gp, 128, 0, c->stream>>>(c->d_annpart, B.tp, c->d_bh, B.Tref, c->nz);
     GW_CUDA(cudaGetLastError());

@@ -82,6 +82,7 @@ struct gw_ctx {
     // fused step (both precisions)
     int *d_pipe_of = nullptr;         // [nx*ny] pipe-column index or -1
     double *d_annpart = nullptr;      // [nbh][32][nz] partial annulus sums
+    double *d_outpart = nullptr;      // [nbh][64] partial outlet sums
     double *d_stage = nullptr;        // ROCK2 stage coefficients of the captured step
     double *d_tp = nullptr;           // double path: [ncol][nz] swept pipe columns
     double *d_pp = nullptr;           // double path: [ncol][countz] advected pipe values
