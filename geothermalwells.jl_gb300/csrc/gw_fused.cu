@@ -4,10 +4,10 @@
 //   1. k_rock2_col: every ROCK2 stage of the z-diffusion for one z-column,
 //      the column held in shared memory (the z-stencil only couples levels
 //      of one column, so all stages run without touching HBM in between);
-//   2. k_half_step (x-lines): explicit y-sweep + advected pipe values +
+//   2. k_half_tile (x-lines): explicit y-sweep + advected pipe values +
 //      Thomas x-solve, one thread per line, the explicit sweep evaluated on
 //      the fly while the forward elimination streams the line;
-//   3. k_half_step (y-lines): explicit x-sweep + pipe values + Thomas y-solve.
+//   3. k_half_tile (y-lines): explicit x-sweep + pipe values + Thomas y-solve.
 // Before each half step the pipe columns (5-9 % of the columns) get the
 // explicit sweep into a compact [column][level] buffer on which the outlet
 // mean, the per-level annulus means and the semi-Lagrangian advection run.
@@ -307,68 +307,131 @@ __global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *_
 }
 
 // ---------------------------------------------------------------------------
-// 3. half step: explicit sweep in direction edir + pipe values + Thomas
-//    along the other direction.  XL: x-lines (explicit y), else y-lines.
+// 3. half step: explicit sweep in the other direction + advected pipe values
+//    + Thomas along the line direction.  XL: x-lines (explicit y), else
+//    y-lines (explicit x).
+//
+// A block owns 32 consecutive levels (one per lane) of kHW neighbouring lines
+// (one warp each).  Rows are streamed in chunks of kHR: the block copies the
+// chunk's rows of its kHW lines plus the two neighbouring lines (which the
+// explicit sweep needs) into shared memory with cp.async, double-buffered so
+// the next chunk is in flight while the current one is eliminated.  The
+// forward sweep stores y_l in dst; the backward sweep reads it back in
+// batches loaded ahead of their use and overwrites it with x_l.
+constexpr int kHW = 4;    // lines (warps) per block
+constexpr int kHR = 32;   // rows per chunk
+constexpr int kHB = 8;    // rows per backward batch
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem, bool pred) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    const int n = pred ? BYTES : 0;   // 0: zero-fill, nothing is read
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(s), "l"(gmem), "n"(BYTES),
+                 "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
 template <typename T, bool XL>
-__global__ void __launch_bounds__(128) k_half_step(T *__restrict__ dst, const T *__restrict__ src,
-                                                   const T *__restrict__ pp,
-                                                   const int *__restrict__ pipe_of,
-                                                   const int *__restrict__ zclass,
-                                                   const T *__restrict__ ecm,
-                                                   const T *__restrict__ ecp,
-                                                   const T *__restrict__ fa,
-                                                   const T *__restrict__ fib,
-                                                   const T *__restrict__ fcu, int nx, int ny, int nz,
-                                                   int countz, double h) {
+__global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, const T *__restrict__ src,
+                                                        const T *__restrict__ pp,
+                                                        const int *__restrict__ pipe_of,
+                                                        const int *__restrict__ zclass,
+                                                        const T *__restrict__ ecm,
+                                                        const T *__restrict__ ecp,
+                                                        const T *__restrict__ fa,
+                                                        const T *__restrict__ fib,
+                                                        const T *__restrict__ fcu, int nx, int ny,
+                                                        int nz, int countz, double h) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *tile = reinterpret_cast<T *>(smem_raw);   // [2][kHR][kHW + 2][32]
+    constexpr int kTile = kHR * (kHW + 2) * 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nl = XL ? ny : nx;   // lines per level
     const int N = XL ? nx : ny;    // line length
-    long long L = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (L >= (long long)nz * nl) return;
-    const int k = (int)(L % nz);
-    const int m = (int)(L / nz);
-    const int zc = zclass[k];
-    const size_t fb = ((size_t)zc * nl + m) * N;
-    const bool in_pipe_levels = k < countz;
-    long long stride, off0, es;   // es: neighbour offset of the explicit direction
-    bool has_m, has_p;
-    if (XL) {    // line (k, j = m); explicit y: neighbours j -+ 1
-        stride = (long long)nz * ny;
-        off0 = k + (long long)nz * m;
-        es = nz;
-        has_m = m > 0;
-        has_p = m < ny - 1;
-    } else {     // line (k, i = m); explicit x: neighbours i -+ 1
-        stride = nz;
-        off0 = k + (long long)nz * ny * m;
-        es = (long long)nz * ny;
-        has_m = m > 0;
-        has_p = m < nx - 1;
-    }
+    const int k0 = blockIdx.x * 32, m0 = blockIdx.y * kHW;
+    const int k = k0 + lane, m = m0 + warp;
+    const bool active = k < nz && m < nl;
+    const int kc = k < nz ? k : nz - 1, mc = m < nl ? m : nl - 1;   // clamped for table reads
+    // element (k, line m, row l): x-lines (k, j=m, i=l), y-lines (k, i=m, j=l)
+    const long long mst = XL ? (long long)nz : (long long)nz * ny;
+    const long long rst = XL ? (long long)nz * ny : (long long)nz;
+    const int zc = zclass[kc];
+    const size_t fb = ((size_t)zc * nl + mc) * N;
+    const bool has_m = m > 0, has_p = m < nl - 1;
+    const bool pipe_levels = k < countz;
     const T hh = (T)h;
+    const int nchunk = (N + kHR - 1) / kHR;
+
+    auto load_chunk = [&](int ch, int buf) {
+        T *t = tile + buf * kTile;
+        for (int e = threadIdx.x; e < kTile; e += blockDim.x) {
+            const int kk = e & 31;
+            const int mm = (e >> 5) % (kHW + 2);
+            const int r = (e >> 5) / (kHW + 2);
+            const int gk = k0 + kk, gm = m0 - 1 + mm, l = ch * kHR + r;
+            const bool ok = gk < nz && gm >= 0 && gm < nl && l < N;
+            const T *g = ok ? src + gk + gm * mst + (long long)l * rst : src;
+            cp_async<sizeof(T)>(t + e, g, ok);
+        }
+        cp_async_commit();
+    };
+
     T y = T(0);
-    // every load of a row is independent of the elimination chain, so the
-    // unrolled loop can issue several rows' loads ahead of the dependent FMAs
-#pragma unroll 4
-    for (int l = 0; l < N; ++l) {
-        const long long o = off0 + l * stride;
-        const int colidx = XL ? l * ny + m : m * ny + l;
-        const int q = in_pipe_levels ? __ldg(pipe_of + colidx) : -1;
-        const T xc = src[o];
-        const T xp = has_p ? src[o + es] : xc;
-        const T xm = has_m ? src[o - es] : xc;
-        const size_t t = XL ? ((size_t)zc * nx + l) * ny + m : ((size_t)zc * ny + l) * nx + m;
-        const T a = __ldg(ecp + t) * (xp - xc) - __ldg(ecm + t) * (xc - xm);
-        T rhs = fma(hh, a, xc);
-        if (q >= 0) rhs = pp[(size_t)q * countz + k];
-        y = (rhs - __ldg(fa + fb + l) * y) * __ldg(fib + fb + l);
-        dst[o] = y;
+    load_chunk(0, 0);
+    for (int ch = 0; ch < nchunk; ++ch) {
+        if (ch + 1 < nchunk) {
+            load_chunk(ch + 1, (ch + 1) & 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const T *t = tile + (ch & 1) * kTile;
+        const int rmax = min(kHR, N - ch * kHR);
+        for (int r = 0; r < rmax; ++r) {
+            const int l = ch * kHR + r;
+            const T *row = t + r * (kHW + 2) * 32;
+            const T xc = row[(warp + 1) * 32 + lane];
+            const T xp = has_p ? row[(warp + 2) * 32 + lane] : xc;
+            const T xm = has_m ? row[warp * 32 + lane] : xc;
+            const size_t ti = XL ? ((size_t)zc * nx + l) * ny + mc : ((size_t)zc * ny + l) * nx + mc;
+            const T a = __ldg(ecp + ti) * (xp - xc) - __ldg(ecm + ti) * (xc - xm);
+            T rhs = fma(hh, a, xc);
+            if (pipe_levels) {
+                const int colidx = XL ? l * ny + mc : mc * ny + l;
+                const int q = __ldg(pipe_of + colidx);
+                if (q >= 0) rhs = pp[(size_t)q * countz + k];
+            }
+            y = (rhs - __ldg(fa + fb + l) * y) * __ldg(fib + fb + l);
+            if (active) dst[k + m * mst + (long long)l * rst] = y;
+        }
+        __syncthreads();   // the buffer is refilled two chunks later
     }
+    if (!active) return;
+    // backward sweep: batches of kHB rows are loaded before the previous
+    // batch is processed, so the loads overlap the dependent chain
     T x = y;
-#pragma unroll 4
-    for (int l = N - 2; l >= 0; --l) {
-        const long long o = off0 + l * stride;
-        x = dst[o] - __ldg(fcu + fb + l) * x;
-        dst[o] = x;
+    T *col = dst + k + m * mst;
+    T cur[kHB], nxt[kHB];
+    int l = N - 2;
+    auto load_batch = [&](T *v, int top) {
+#pragma unroll
+        for (int b = 0; b < kHB; ++b) v[b] = (top - b >= 0) ? col[(long long)(top - b) * rst] : T(0);
+    };
+    load_batch(cur, l);
+    while (l >= 0) {
+        load_batch(nxt, l - kHB);
+#pragma unroll
+        for (int b = 0; b < kHB; ++b) {
+            if (l - b < 0) break;
+            x = cur[b] - __ldg(fcu + fb + (l - b)) * x;
+            col[(long long)(l - b) * rst] = x;
+        }
+#pragma unroll
+        for (int b = 0; b < kHB; ++b) cur[b] = nxt[b];
+        l -= kHB;
     }
 }
 
@@ -465,18 +528,22 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h) {
 }
 
 template <typename T>
+size_t half_smem() { return 2 * (size_t)kHR * (kHW + 2) * 32 * sizeof(T); }
+
+template <typename T>
 int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h) {
     Bufs<T> B = bufs<T>(c);
     const GwFactors<T> &f = xlines ? B.ct->fx : B.ct->fy;
     const T *ecm = xlines ? B.ct->cym : B.ct->cxm;
     const T *ecp = xlines ? B.ct->cyp : B.ct->cxp;
-    long long lines = (long long)c->nz * (xlines ? c->ny : c->nx);
+    const int nl = xlines ? c->ny : c->nx;
+    dim3 grid((c->nz + 31) / 32, (nl + kHW - 1) / kHW);
     if (xlines)
-        k_half_step<T, true><<<grid_for(lines, 128), 128, 0, c->stream>>>(
+        k_half_tile<T, true><<<grid, 32 * kHW, half_smem<T>(), c->stream>>>(
             dst, src, B.pp, c->d_pipe_of, c->d_zclass, ecm, ecp, f.a, f.ib, f.cu, c->nx, c->ny,
             c->nz, c->countz, h);
     else
-        k_half_step<T, false><<<grid_for(lines, 128), 128, 0, c->stream>>>(
+        k_half_tile<T, false><<<grid, 32 * kHW, half_smem<T>(), c->stream>>>(
             dst, src, B.pp, c->d_pipe_of, c->d_zclass, ecm, ecp, f.a, f.ib, f.cu, c->nx, c->ny,
             c->nz, c->countz, h);
     GW_CUDA(cudaGetLastError());
@@ -523,6 +590,19 @@ int gw_fused_prepare(gw_ctx *c) {
         e = cudaFuncSetAttribute(k_rock2_col<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)rock2_smem<double>(c->nz));
     if (e != cudaSuccess) return gw_cuda_fail(e, "cudaFuncSetAttribute(k_rock2_col)");
+    if (c->precision == GW_PREC_MIXED) {
+        if ((e = cudaFuncSetAttribute(k_half_tile<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)half_smem<float>())) != cudaSuccess ||
+            (e = cudaFuncSetAttribute(k_half_tile<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)half_smem<float>())) != cudaSuccess)
+            return gw_cuda_fail(e, "cudaFuncSetAttribute(k_half_tile)");
+    } else {
+        if ((e = cudaFuncSetAttribute(k_half_tile<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)half_smem<double>())) != cudaSuccess ||
+            (e = cudaFuncSetAttribute(k_half_tile<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)half_smem<double>())) != cudaSuccess)
+            return gw_cuda_fail(e, "cudaFuncSetAttribute(k_half_tile)");
+    }
     int per_sm = 0;
     if (c->precision == GW_PREC_MIXED)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rock2_col<float, true>, 256,
