@@ -241,6 +241,7 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         (rc = dalloc(c, &c->d_annmean, (size_t)c->nbh * c->nz)) ||
         (rc = dalloc(c, &c->d_annpart, (size_t)c->nbh * 32 * c->nz)) ||
         (rc = dalloc(c, &c->d_outpart, (size_t)c->nbh * 64)) ||
+        (rc = dalloc(c, &c->d_advtab, (size_t)c->nbh * c->countz * 2)) ||
         (rc = dalloc(c, &c->d_outlet, c->nbh)) || (rc = dalloc(c, &c->d_energy, c->nbh)) ||
         (rc = dalloc(c, &c->d_stage, GW_STAGE_TABLE)) ||
         (rc = dalloc(c, &c->d_step_counter, 1)) || (rc = dalloc(c, &c->d_flag, 1)))
@@ -436,7 +437,7 @@ int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
     if ((rc = gw_ensure_factors(c, dt / 2))) return rc;
     if (!c->graph || c->graph_dt != dt || c->graph_s != s) {
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
-        if (c->fused && (rc = upload_stages(c, dt, s))) return rc;
+        if (c->fused && ((rc = upload_stages(c, dt, s)) || (rc = gw_fused_set_dt(c, dt)))) return rc;
         cudaGraph_t g;
         GW_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         int r3;
@@ -480,8 +481,8 @@ int gw_profile_kernels(gw_ctx *c, double dt, int reps, double *ms_out) {
     if (rc || (rc = gw_ensure_factors(c, dt / 2))) return rc;
     int s, covered;
     if ((rc = gw_rock2_choose(dt, c->eigen_estimate, 100, &s, &covered))) return rc;
-    if ((rc = upload_stages(c, dt, s))) return rc;
-    c->graph_dt = -1.0;   // the stage table may differ from the captured step's
+    if ((rc = upload_stages(c, dt, s)) || (rc = gw_fused_set_dt(c, dt))) return rc;
+    c->graph_dt = -1.0;   // the tables may differ from the captured step's
     const size_t N = ncell(c);
     void *u = mixed(c) ? (void *)c->f_u : (void *)c->d_u;
     void *bak = mixed(c) ? (void *)c->f_g1 : (void *)c->d_g1;

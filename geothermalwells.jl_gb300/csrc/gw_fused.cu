@@ -241,67 +241,85 @@ __global__ void __launch_bounds__(128) k_annulus_fin(double *__restrict__ mean,
     mean[(size_t)b * nz + k] = s / (double)bh[b].outer_count;
 }
 
-__device__ __forceinline__ void interp_c(const double *__restrict__ g, int n, double dep, int &il,
-                                         int &ir, double &alpha) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        int mid = lo + ((hi - lo) >> 1);
-        if (g[mid] < dep) lo = mid + 1; else hi = mid;
+// Departure table of kernel_advection! (src/solver.jl:285-360): for every
+// borehole b, level k < countz and pipe (0 inner, 1 annulus) the branch
+// taken, the two interpolation levels and the weight.  It depends only on
+// the grid, the velocities and dt, so it is built once per step size with the
+// same floating-point operations (fused multiply-adds as the reference's
+// @muladd) the per-cell evaluation would use.
+enum : int { kAdvKeep = 0, kAdvInterp = 1, kAdvTurn = 2, kAdvInlet = 3 };
+
+__global__ void k_adv_table(GwAdvRec *__restrict__ tab, const double *__restrict__ gz,
+                            const GwBhDev *__restrict__ bh, int nbh, int nz, int countz, double dt) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nbh * countz * 2) return;
+    const int pipe = e & 1, k = (e >> 1) % countz, b = (e >> 1) / countz;
+    const GwBhDev B = bh[b];
+    const double z = gz[k];
+    GwAdvRec r;
+    r.type = kAdvKeep; r.il = k; r.ir = k; r.alpha = 0.0;
+    if (z <= B.h) {
+        double dep;
+        if (pipe == 0) {
+            double zd = __fma_rn(B.v_inner, dt, z);
+            if (zd > B.h) {
+                double dt1 = __ddiv_rn(__dsub_rn(B.h, z), B.v_inner);
+                double dt2 = __dsub_rn(dt, dt1);
+                dep = __fma_rn(-B.v_outer, dt2, B.h);
+                r.type = kAdvTurn;
+            } else {
+                dep = zd;
+                r.type = kAdvInterp;
+            }
+        } else {
+            dep = __fma_rn(-B.v_outer, dt, z);
+            r.type = dep <= 0.0 ? kAdvInlet : kAdvInterp;
+        }
+        if (r.type != kAdvInlet) {
+            int lo = 0, hi = nz - 1;   // gpu_searchsortedfirst + interpolation_helper
+            while (lo < hi) {
+                int mid = lo + ((hi - lo) >> 1);
+                if (gz[mid] < dep) lo = mid + 1; else hi = mid;
+            }
+            int ir = lo, il = lo - 1;
+            if (il < 0) il = 0;
+            if (ir > nz - 1) ir = nz - 1;
+            r.il = il; r.ir = ir;
+            r.alpha = __ddiv_rn(__dsub_rn(dep, gz[il]), __dsub_rn(gz[ir], gz[il]));
+        }
     }
-    ir = lo;
-    il = lo - 1;
-    if (il < 0) il = 0;
-    if (ir > n - 1) ir = n - 1;
-    alpha = __ddiv_rn(__dsub_rn(dep, g[il]), __dsub_rn(g[ir], g[il]));
+    tab[e] = r;
 }
 
-// kernel_advection! (src/solver.jl:285-360) on the compact buffer; the
+// kernel_advection! on the compact buffer with the departure table; the
 // result (minus T_ref in the mixed path) goes to pp[q][k], k < countz.
 template <typename T>
 __global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *__restrict__ tp,
-                                                  const double *__restrict__ gz,
+                                                  const GwAdvRec *__restrict__ tab,
                                                   const int *__restrict__ pb,
-                                                  const GwBhDev *__restrict__ bh,
                                                   const double *__restrict__ ann_mean,
                                                   const double *__restrict__ outlet,
                                                   const double *__restrict__ Tref, int n_inner,
-                                                  int ncol, int nz, int countz, double dt,
-                                                  int inlet_kind, double inlet_param) {
+                                                  int ncol, int nz, int countz, int inlet_kind,
+                                                  double inlet_param) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)ncol * countz) return;
     const int k = (int)(e % countz);
     const int q = (int)(e / countz);
     const int b = pb[q];
-    const GwBhDev B = bh[b];
+    const GwAdvRec r = tab[((size_t)b * countz + k) * 2 + (q < n_inner ? 0 : 1)];
     const T *col = tp + (size_t)q * nz;
-    const double z = gz[k];
     double v;
-    if (z > B.h) {
+    if (r.type == kAdvKeep) {
         v = absT(col[k], Tref, k);
-    } else if (q < n_inner) {
-        double zd = __fma_rn(B.v_inner, dt, z);
-        if (zd > B.h) {
-            double dt1 = __ddiv_rn(__dsub_rn(B.h, z), B.v_inner);
-            double dt2 = __dsub_rn(dt, dt1);
-            double zd2 = __fma_rn(-B.v_outer, dt2, B.h);
-            int il, ir; double a;
-            interp_c(gz, nz, zd2, il, ir, a);
-            const double *m = ann_mean + (size_t)b * nz;
-            v = __fma_rn(a, m[ir], __dmul_rn(__dsub_rn(1.0, a), m[il]));
-        } else {
-            int il, ir; double a;
-            interp_c(gz, nz, zd, il, ir, a);
-            v = __fma_rn(a, absT(col[ir], Tref, ir), __dmul_rn(__dsub_rn(1.0, a), absT(col[il], Tref, il)));
-        }
+    } else if (r.type == kAdvInlet) {
+        v = inlet_kind == GW_INLET_CONSTANT ? inlet_param : outlet[b] - inlet_param;
+    } else if (r.type == kAdvTurn) {
+        const double *m = ann_mean + (size_t)b * nz;
+        v = __fma_rn(r.alpha, m[r.ir], __dmul_rn(__dsub_rn(1.0, r.alpha), m[r.il]));
     } else {
-        double zd = __fma_rn(-B.v_outer, dt, z);
-        if (zd <= 0.0) {
-            v = inlet_kind == GW_INLET_CONSTANT ? inlet_param : outlet[b] - inlet_param;
-        } else {
-            int il, ir; double a;
-            interp_c(gz, nz, zd, il, ir, a);
-            v = __fma_rn(a, absT(col[ir], Tref, ir), __dmul_rn(__dsub_rn(1.0, a), absT(col[il], Tref, il)));
-        }
+        v = __fma_rn(r.alpha, absT(col[r.ir], Tref, r.ir),
+                     __dmul_rn(__dsub_rn(1.0, r.alpha), absT(col[r.il], Tref, r.il)));
     }
     pp[e] = (T)(Tref ? v - Tref[k] : v);
 }
@@ -520,8 +538,8 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h) {
     long long na = (long long)ncol * c->countz;
     if (na > 0) {
         k_advect_c<T><<<grid_for(na, 256), 256, 0, c->stream>>>(
-            B.pp, B.tp, c->d_gz, c->d_pipe_b, c->d_bh, c->d_annmean, c->d_outlet, B.Tref, c->n_inner,
-            ncol, c->nz, c->countz, h, c->inlet_kind, c->inlet_param);
+            B.pp, B.tp, c->d_advtab, c->d_pipe_b, c->d_annmean, c->d_outlet, B.Tref, c->n_inner,
+            ncol, c->nz, c->countz, c->inlet_kind, c->inlet_param);
         GW_CUDA(cudaGetLastError());
     }
     return GW_OK;
@@ -615,6 +633,17 @@ int gw_fused_prepare(gw_ctx *c) {
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     if (e != cudaSuccess) return gw_cuda_fail(e, "cudaDeviceGetAttribute");
     c->rock2_grid = (per_sm > 0 ? per_sm : 1) * sms * 8;
+    return GW_OK;
+}
+
+int gw_fused_set_dt(gw_ctx *c, double dt) {
+    const int n = c->nbh * c->countz * 2;
+    if (n > 0) {
+        k_adv_table<<<grid_for(n, 128), 128, 0, c->stream>>>(c->d_advtab, c->d_gz, c->d_bh, c->nbh,
+                                                             c->nz, c->countz, dt / 2);
+        GW_CUDA(cudaGetLastError());
+    }
+    GW_CUDA(cudaStreamSynchronize(c->stream));
     return GW_OK;
 }
 

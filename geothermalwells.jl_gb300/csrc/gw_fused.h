@@ -6,6 +6,8 @@
 int gw_fused_supported(const gw_ctx *c);
 // Per-context kernel attributes and the column kernel's grid size.
 int gw_fused_prepare(gw_ctx *c);
+// Build the step-size dependent tables (advection departures) for dt.
+int gw_fused_set_dt(gw_ctx *c, double dt);
 // Enqueue one full step (ROCK2 columns, two half steps, record) on c->stream.
 // Requires the Thomas factors for dt/2 and the stage table c->d_stage for s.
 int gw_fused_step(gw_ctx *c, double dt, int s);

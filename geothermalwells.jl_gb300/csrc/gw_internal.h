@@ -15,6 +15,12 @@ struct GwBorehole {
     double v_inner, v_outer, insulation_depth;
 };
 
+// One departure record of the semi-Lagrangian advection (see k_adv_table).
+struct GwAdvRec {
+    double alpha;
+    int il, ir, type, pad;
+};
+
 // Per-borehole data the advection kernels read (one small device array).
 struct GwBhDev {
     double h, v_inner, v_outer, mdot;
@@ -83,6 +89,7 @@ struct gw_ctx {
     int *d_pipe_of = nullptr;         // [nx*ny] pipe-column index or -1
     double *d_annpart = nullptr;      // [nbh][32][nz] partial annulus sums
     double *d_outpart = nullptr;      // [nbh][64] partial outlet sums
+    GwAdvRec *d_advtab = nullptr;     // [nbh][countz][2] departure table for dt/2
     double *d_stage = nullptr;        // ROCK2 stage coefficients of the captured step
     double *d_tp = nullptr;           // double path: [ncol][nz] swept pipe columns
     double *d_pp = nullptr;           // double path: [ncol][countz] advected pipe values
