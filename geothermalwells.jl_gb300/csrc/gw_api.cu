@@ -162,15 +162,21 @@ int gw_ensure_factors(gw_ctx *c, double h) {
     std::vector<double> a, ib, cu;
     GW_CUDA(cudaStreamSynchronize(c->stream));
     int rc;
+    std::vector<double> h4;
     for (int dir = GW_DIR_X; dir <= GW_DIR_Y; ++dir) {
         gw_build_factors(c, h, dir, dir == GW_DIR_X ? cxm : cym, dir == GW_DIR_X ? cxp : cyp, a, ib, cu);
+        // x-lines fold the explicit y sweep, y-lines the explicit x sweep
+        gw_build_half_table(c, h, dir, dir == GW_DIR_X ? cym : cxm, dir == GW_DIR_X ? cyp : cxp, a, ib, h4);
         GwFactors<double> &f = dir == GW_DIR_X ? c->c64.fx : c->c64.fy;
         if ((rc = copy_to(f.a, a)) || (rc = copy_to(f.ib, ib)) || (rc = copy_to(f.cu, cu))) return rc;
         if (mixed(c)) {
             GwFactors<float> &g = dir == GW_DIR_X ? c->c32.fx : c->c32.fy;
             if ((rc = copy_to(g.a, to_float(a))) || (rc = copy_to(g.ib, to_float(ib))) ||
-                (rc = copy_to(g.cu, to_float(cu))))
+                (rc = copy_to(g.cu, to_float(cu))) ||
+                (rc = copy_to(dir == GW_DIR_X ? c->c32.hx : c->c32.hy, to_float(h4))))
                 return rc;
+        } else if ((rc = copy_to(dir == GW_DIR_X ? c->c64.hx : c->c64.hy, h4))) {
+            return rc;
         }
     }
     c->factors_h = h;
@@ -235,7 +241,12 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         slot = q;
     }
     for (auto &B : bhd) { if (B.inner_begin < 0) B.inner_begin = 0; if (B.outer_begin < 0) B.outer_begin = 0; }
-    if ((rc = upload(c, &c->d_bh, bhd)) || (rc = upload(c, &c->d_pipe_of, pipe_of))) return fail(rc);
+    std::vector<int> plx((size_t)c->ny * c->nx);
+    for (int i = 0; i < c->nx; ++i)
+        for (int j = 0; j < c->ny; ++j) plx[(size_t)j * c->nx + i] = pipe_of[(size_t)i * c->ny + j];
+    if ((rc = upload(c, &c->d_bh, bhd)) || (rc = upload(c, &c->d_pipe_of, pipe_of)) ||
+        (rc = upload(c, &c->d_pipe_lx, plx)) || (rc = upload(c, &c->d_pipe_ly, pipe_of)))
+        return fail(rc);
     const size_t N = ncell(c);
     if ((rc = dalloc(c, &c->d_utmp, (size_t)ncol * c->countz)) ||
         (rc = dalloc(c, &c->d_annmean, (size_t)c->nbh * c->nz)) ||
@@ -259,12 +270,15 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
             return fail(rc);
         if ((rc = dalloc(c, &c->c32.fx.a, cxm.size())) || (rc = dalloc(c, &c->c32.fx.ib, cxm.size())) ||
             (rc = dalloc(c, &c->c32.fx.cu, cxm.size())) || (rc = dalloc(c, &c->c32.fy.a, cym.size())) ||
-            (rc = dalloc(c, &c->c32.fy.ib, cym.size())) || (rc = dalloc(c, &c->c32.fy.cu, cym.size())))
+            (rc = dalloc(c, &c->c32.fy.ib, cym.size())) || (rc = dalloc(c, &c->c32.fy.cu, cym.size())) ||
+            (rc = dalloc(c, &c->c32.hx, 4 * cxm.size())) || (rc = dalloc(c, &c->c32.hy, 4 * cym.size())))
             return fail(rc);
         GW_CUDA(cudaMemset(c->f_u, 0, N * sizeof(float)));
         std::vector<double> zero(c->nz, 0.0);
         if ((rc = set_reference_profile(c, zero.data()))) return fail(rc);
     } else {
+        if ((rc = dalloc(c, &c->c64.hx, 4 * cxm.size())) || (rc = dalloc(c, &c->c64.hy, 4 * cym.size())))
+            return fail(rc);
         if ((rc = dalloc(c, &c->d_u, N)) || (rc = dalloc(c, &c->d_temp, N)) || (rc = dalloc(c, &c->d_g1, N)) ||
             (rc = dalloc(c, &c->d_tp, (size_t)ncol * c->nz)) ||
             (rc = dalloc(c, &c->d_pp, (size_t)ncol * c->countz)))
@@ -311,6 +325,7 @@ int gw_set_field(gw_ctx *c, const double *T) {
     if (rc) return rc;
     if (mixed(c)) {
         if ((rc = set_reference_profile(c, T))) return rc;
+        c->graph_dt = -1.0;   // the advection table depends on T_ref
         const size_t N = ncell(c);
         std::vector<float> th(N);
         const int nz = c->nz;

@@ -116,6 +116,128 @@ __global__ void __launch_bounds__(256) k_rock2_col(T *__restrict__ u, const int 
     }
 }
 
+// Register-resident variant for nz <= 256 * LPT: thread t owns the LPT
+// consecutive levels [t LPT, t LPT + LPT) in registers, its coefficients
+// too; a stage only exchanges the two end values of each thread's run through
+// shared memory (double-buffered, one barrier per stage).  The next column is
+// loaded into registers while the current one runs its stages.
+template <typename T, bool INC, int LPT>
+__global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int *__restrict__ colprof,
+                                                   const T *__restrict__ czm,
+                                                   const T *__restrict__ czp,
+                                                   const T *__restrict__ fref,
+                                                   const double *__restrict__ sc, int s, int nz,
+                                                   long long ncols) {
+    __shared__ T s_lo[2][256], s_hi[2][256];
+    const int t = threadIdx.x;
+    const int kb = t * LPT;
+    const int nv = max(0, min(LPT, nz - kb));   // levels this thread owns
+    const bool tail = kb + nv >= nz;            // owns the bottom level of the column
+    const int nrec = s - 2;
+    int xb = 0;
+    // neighbours of this thread's run: level kb - 1 and level kb + nv
+    auto exchange = [&](const T (&v)[LPT], T &left, T &right) {
+        T last = v[0];
+#pragma unroll
+        for (int i = 1; i < LPT; ++i)
+            if (i < nv) last = v[i];
+        s_lo[xb][t] = v[0];
+        s_hi[xb][t] = last;
+        __syncthreads();
+        left = t > 0 ? s_hi[xb][t - 1] : v[0];
+        right = (!tail && t + 1 < 256) ? s_lo[xb][t + 1] : last;
+        xb ^= 1;
+    };
+    auto apply = [&](const T (&v)[LPT], const T (&cm)[LPT], const T (&cp)[LPT], int i, T left,
+                     T right) {
+        const T gc = v[i];
+        const T gm = i == 0 ? left : v[i > 0 ? i - 1 : 0];
+        const T gp = (i + 1 < nv) ? v[i + 1 < LPT ? i + 1 : i] : right;
+        return cp[i] * (gp - gc) - cm[i] * (gc - gm);
+    };
+    T nxt[LPT];
+    long long col = blockIdx.x;
+    if (col < ncols) {
+#pragma unroll
+        for (int i = 0; i < LPT; ++i) nxt[i] = i < nv ? u[col * nz + kb + i] : T(0);
+    }
+    for (; col < ncols; col += gridDim.x) {
+        T base[LPT], cm[LPT], cp[LPT], F0[LPT], prev[LPT], cur[LPT];
+        const int p = colprof[col];
+#pragma unroll
+        for (int i = 0; i < LPT; ++i) {
+            base[i] = nxt[i];
+            const bool ok = i < nv;
+            cm[i] = ok ? __ldg(czm + (size_t)p * nz + kb + i) : T(0);
+            cp[i] = ok ? __ldg(czp + (size_t)p * nz + kb + i) : T(0);
+        }
+        const long long ncol_next = col + gridDim.x;
+        if (ncol_next < ncols) {
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) nxt[i] = i < nv ? u[ncol_next * nz + kb + i] : T(0);
+        }
+        T left, right;
+        exchange(base, left, right);
+        if (INC) {
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) {
+                T f = apply(base, cm, cp, i, left, right);
+                if (fref && i < nv) f += __ldg(fref + (size_t)p * nz + kb + i);
+                F0[i] = f;
+                prev[i] = T(0);
+                cur[i] = T(0);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) { prev[i] = base[i]; cur[i] = base[i]; }
+        }
+        // recurrence g_j = g_{j-1} + h mu_j A g_{j-1} + kappa_j (g_{j-1} - g_{j-2});
+        // in the increment form g = base + delta and A g = F0 + A delta
+        for (int j = 0; j < nrec; ++j) {
+            const T hmu = (T)sc[2 * j], kap = (T)sc[2 * j + 1];
+            if (INC && j == 0) {
+#pragma unroll
+                for (int i = 0; i < LPT; ++i) { prev[i] = cur[i]; cur[i] = hmu * F0[i]; }
+                continue;
+            }
+            exchange(cur, left, right);
+            T out[LPT];
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) {
+                T a = apply(cur, cm, cp, i, left, right);
+                if (INC) a += F0[i];
+                out[i] = cur[i] + hmu * a + kap * (cur[i] - prev[i]);
+            }
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) { prev[i] = cur[i]; cur[i] = out[i]; }
+        }
+        // finishing procedure: gq = gp + h sigma A gp;
+        // y = gq + (h tau / sigma) A gq + (1 - tau / sigma^2) (gq - gp)
+        const T hs = (T)sc[2 * nrec], hts = (T)sc[2 * nrec + 1], c3 = (T)sc[2 * nrec + 2];
+        T q[LPT];
+        if (INC && nrec == 0) {
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) q[i] = hs * F0[i];
+        } else {
+            exchange(cur, left, right);
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) {
+                T a = apply(cur, cm, cp, i, left, right);
+                if (INC) a += F0[i];
+                q[i] = cur[i] + hs * a;
+            }
+        }
+        exchange(q, left, right);
+#pragma unroll
+        for (int i = 0; i < LPT; ++i) {
+            T a = apply(q, cm, cp, i, left, right);
+            if (INC) a += F0[i];
+            const T y = q[i] + hts * a + c3 * (q[i] - cur[i]);
+            if (i < nv) u[col * nz + kb + i] = INC ? base[i] + y : y;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // 2. pipe columns: explicit sweep (I + h A_dir) into tp[q][k], all levels
 template <typename T>
@@ -250,14 +372,15 @@ __global__ void __launch_bounds__(128) k_annulus_fin(double *__restrict__ mean,
 enum : int { kAdvKeep = 0, kAdvInterp = 1, kAdvTurn = 2, kAdvInlet = 3 };
 
 __global__ void k_adv_table(GwAdvRec *__restrict__ tab, const double *__restrict__ gz,
-                            const GwBhDev *__restrict__ bh, int nbh, int nz, int countz, double dt) {
+                            const GwBhDev *__restrict__ bh, const double *__restrict__ Tref, int nbh,
+                            int nz, int countz, double dt) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nbh * countz * 2) return;
     const int pipe = e & 1, k = (e >> 1) % countz, b = (e >> 1) / countz;
     const GwBhDev B = bh[b];
     const double z = gz[k];
     GwAdvRec r;
-    r.type = kAdvKeep; r.il = k; r.ir = k; r.alpha = 0.0;
+    r.type = kAdvKeep; r.il = k; r.ir = k; r.alpha = 0.0; r.dref = 0.0; r.pad = 0;
     if (z <= B.h) {
         double dep;
         if (pipe == 0) {
@@ -286,6 +409,8 @@ __global__ void k_adv_table(GwAdvRec *__restrict__ tab, const double *__restrict
             if (ir > nz - 1) ir = nz - 1;
             r.il = il; r.ir = ir;
             r.alpha = __ddiv_rn(__dsub_rn(dep, gz[il]), __dsub_rn(gz[ir], gz[il]));
+            if (Tref)
+                r.dref = r.alpha * Tref[ir] + (1.0 - r.alpha) * Tref[il] - Tref[k];
         }
     }
     tab[e] = r;
@@ -317,6 +442,12 @@ __global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *_
     } else if (r.type == kAdvTurn) {
         const double *m = ann_mean + (size_t)b * nz;
         v = __fma_rn(r.alpha, m[r.ir], __dmul_rn(__dsub_rn(1.0, r.alpha), m[r.il]));
+    } else if (sizeof(T) == 4) {
+        // mixed path: interpolate theta in float, the T_ref part is the
+        // tabulated double offset
+        const float a = (float)r.alpha;
+        pp[e] = (T)(fmaf(a, (float)col[r.ir], (1.0f - a) * (float)col[r.il]) + (float)r.dref);
+        return;
     } else {
         v = __fma_rn(r.alpha, absT(col[r.ir], Tref, r.ir),
                      __dmul_rn(__dsub_rn(1.0, r.alpha), absT(col[r.il], Tref, r.il)));
@@ -351,47 +482,56 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
+template <typename T>
+struct alignas(4 * sizeof(T)) Quad {
+    T x, y, z, w;
+};
+
 template <typename T, bool XL>
 __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, const T *__restrict__ src,
                                                         const T *__restrict__ pp,
-                                                        const int *__restrict__ pipe_of,
+                                                        const int *__restrict__ pipe_line,
                                                         const int *__restrict__ zclass,
-                                                        const T *__restrict__ ecm,
-                                                        const T *__restrict__ ecp,
-                                                        const T *__restrict__ fa,
+                                                        const Quad<T> *__restrict__ hq,
                                                         const T *__restrict__ fib,
                                                         const T *__restrict__ fcu, int nx, int ny,
-                                                        int nz, int countz, double h) {
+                                                        int nz, int countz) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *tile = reinterpret_cast<T *>(smem_raw);   // [2][kHR][kHW + 2][32]
-    constexpr int kTile = kHR * (kHW + 2) * 32;
+    constexpr int kRow = (kHW + 2) * 32;
+    constexpr int kTile = kHR * kRow;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nl = XL ? ny : nx;   // lines per level
     const int N = XL ? nx : ny;    // line length
     const int k0 = blockIdx.x * 32, m0 = blockIdx.y * kHW;
     const int k = k0 + lane, m = m0 + warp;
-    const bool active = k < nz && m < nl;
-    const int kc = k < nz ? k : nz - 1, mc = m < nl ? m : nl - 1;   // clamped for table reads
+    const bool kok = k < nz;
+    const bool active = kok && m < nl;
+    const int kc = kok ? k : nz - 1, mc = m < nl ? m : nl - 1;   // clamped for table reads
     // element (k, line m, row l): x-lines (k, j=m, i=l), y-lines (k, i=m, j=l)
     const long long mst = XL ? (long long)nz : (long long)nz * ny;
     const long long rst = XL ? (long long)nz * ny : (long long)nz;
-    const int zc = zclass[kc];
-    const size_t fb = ((size_t)zc * nl + mc) * N;
-    const bool has_m = m > 0, has_p = m < nl - 1;
+    const size_t fb = ((size_t)zclass[kc] * nl + mc) * N;
+    const int *pline = pipe_line + (size_t)mc * N;
     const bool pipe_levels = k < countz;
-    const T hh = (T)h;
     const int nchunk = (N + kHR - 1) / kHR;
 
+    // this warp copies neighbour-line slots mm = warp and warp + kHW of each row
     auto load_chunk = [&](int ch, int buf) {
         T *t = tile + buf * kTile;
-        for (int e = threadIdx.x; e < kTile; e += blockDim.x) {
-            const int kk = e & 31;
-            const int mm = (e >> 5) % (kHW + 2);
-            const int r = (e >> 5) / (kHW + 2);
-            const int gk = k0 + kk, gm = m0 - 1 + mm, l = ch * kHR + r;
-            const bool ok = gk < nz && gm >= 0 && gm < nl && l < N;
-            const T *g = ok ? src + gk + gm * mst + (long long)l * rst : src;
-            cp_async<sizeof(T)>(t + e, g, ok);
+        const int l0 = ch * kHR;
+#pragma unroll
+        for (int rep = 0; rep < 2; ++rep) {
+            const int mm = warp + rep * kHW;
+            if (mm >= kHW + 2) break;
+            const int gm = m0 - 1 + mm;
+            const bool lok = kok && gm >= 0 && gm < nl;
+            const T *g = src + k + (long long)gm * mst + (long long)l0 * rst;
+            T *d = t + mm * 32 + lane;
+            for (int r = 0; r < kHR; ++r) {
+                const bool ok = lok && l0 + r < N;
+                cp_async<sizeof(T)>(d + r * kRow, ok ? (const void *)(g + (long long)r * rst) : (const void *)src, ok);
+            }
         }
         cp_async_commit();
     };
@@ -406,23 +546,19 @@ __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, con
             cp_async_wait<0>();
         }
         __syncthreads();
-        const T *t = tile + (ch & 1) * kTile;
+        const T *row = tile + (ch & 1) * kTile + warp * 32 + lane;
         const int rmax = min(kHR, N - ch * kHR);
-        for (int r = 0; r < rmax; ++r) {
+        for (int r = 0; r < rmax; ++r, row += kRow) {
             const int l = ch * kHR + r;
-            const T *row = t + r * (kHW + 2) * 32;
-            const T xc = row[(warp + 1) * 32 + lane];
-            const T xp = has_p ? row[(warp + 2) * 32 + lane] : xc;
-            const T xm = has_m ? row[warp * 32 + lane] : xc;
-            const size_t ti = XL ? ((size_t)zc * nx + l) * ny + mc : ((size_t)zc * ny + l) * nx + mc;
-            const T a = __ldg(ecp + ti) * (xp - xc) - __ldg(ecm + ti) * (xc - xm);
-            T rhs = fma(hh, a, xc);
+            const T xm = row[0], xc = row[32], xp = row[64];
+            const Quad<T> q = hq[fb + l];
+            const T ay = q.w * y;
+            T yn = fma(q.x, xc, fma(q.y, xp, fma(q.z, xm, -ay)));
             if (pipe_levels) {
-                const int colidx = XL ? l * ny + mc : mc * ny + l;
-                const int q = __ldg(pipe_of + colidx);
-                if (q >= 0) rhs = pp[(size_t)q * countz + k];
+                const int pq = __ldg(pline + l);
+                if (pq >= 0) yn = fma(pp[(size_t)pq * countz + k], __ldg(fib + fb + l), -ay);
             }
-            y = (rhs - __ldg(fa + fb + l) * y) * __ldg(fib + fb + l);
+            y = yn;
             if (active) dst[k + m * mst + (long long)l * rst] = y;
         }
         __syncthreads();   // the buffer is refilled two chunks later
@@ -487,22 +623,42 @@ size_t rock2_smem(int nz) {
     return (size_t)nz * sizeof(T) * (inc ? 4 : 2);
 }
 
+// levels per thread of the register-resident ROCK2 kernel (0: use the
+// shared-memory kernel)
+inline int rock2_lpt(int nz) {
+    if (nz <= 512) return 2;
+    if (nz <= 1024) return 4;
+    if (nz <= 2048) return 8;
+    if (nz <= 4096) return 16;
+    return 0;
+}
+
+template <typename T, bool INC>
+int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *fref) {
+    const long long ncols = (long long)c->nx * c->ny;
+    const int lpt = rock2_lpt(c->nz);
+    unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid ? ncols : c->rock2_grid);
+    switch (lpt) {
+        case 2: k_rock2_reg<T, INC, 2><<<grid, 256, 0, c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
+        case 4: k_rock2_reg<T, INC, 4><<<grid, 256, 0, c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
+        case 8: k_rock2_reg<T, INC, 8><<<grid, 256, 0, c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
+        case 16: k_rock2_reg<T, INC, 16><<<grid, 256, 0, c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
+        default:
+            k_rock2_col<T, INC><<<grid, 256, rock2_smem<T>(c->nz), c->stream>>>(u, c->d_colprof, czm, czp, fref,
+                                                                            c->d_stage, s, c->nz, ncols);
+    }
+    GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}
+
 template <typename T>
 int launch_rock2(gw_ctx *c, int s) {
     Bufs<T> B = bufs<T>(c);
-    const long long ncols = (long long)c->nx * c->ny;
-    const size_t sm = rock2_smem<T>(c->nz);
-    unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid ? ncols : c->rock2_grid);
     if (sizeof(T) == 4)
-        k_rock2_col<float, true><<<grid, 256, sm, c->stream>>>(
-            (float *)B.u, c->d_colprof, (const float *)B.ct->czm, (const float *)B.ct->czp,
-            (const float *)B.fref, c->d_stage, s, c->nz, ncols);
-    else
-        k_rock2_col<double, false><<<grid, 256, sm, c->stream>>>(
-            (double *)B.u, c->d_colprof, (const double *)B.ct->czm, (const double *)B.ct->czp,
-            nullptr, c->d_stage, s, c->nz, ncols);
-    GW_CUDA(cudaGetLastError());
-    return GW_OK;
+        return launch_rock2_t<float, true>(c, s, (float *)B.u, (const float *)B.ct->czm,
+                                           (const float *)B.ct->czp, (const float *)B.fref);
+    return launch_rock2_t<double, false>(c, s, (double *)B.u, (const double *)B.ct->czm,
+                                         (const double *)B.ct->czp, nullptr);
 }
 
 // explicit sweep along edir at the pipe columns, outlet/annulus means, advection
@@ -550,20 +706,18 @@ size_t half_smem() { return 2 * (size_t)kHR * (kHW + 2) * 32 * sizeof(T); }
 
 template <typename T>
 int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h) {
+    (void)h;   // folded into the half-step tables
     Bufs<T> B = bufs<T>(c);
     const GwFactors<T> &f = xlines ? B.ct->fx : B.ct->fy;
-    const T *ecm = xlines ? B.ct->cym : B.ct->cxm;
-    const T *ecp = xlines ? B.ct->cyp : B.ct->cxp;
+    const Quad<T> *hq = reinterpret_cast<const Quad<T> *>(xlines ? B.ct->hx : B.ct->hy);
     const int nl = xlines ? c->ny : c->nx;
     dim3 grid((c->nz + 31) / 32, (nl + kHW - 1) / kHW);
     if (xlines)
         k_half_tile<T, true><<<grid, 32 * kHW, half_smem<T>(), c->stream>>>(
-            dst, src, B.pp, c->d_pipe_of, c->d_zclass, ecm, ecp, f.a, f.ib, f.cu, c->nx, c->ny,
-            c->nz, c->countz, h);
+            dst, src, B.pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
     else
         k_half_tile<T, false><<<grid, 32 * kHW, half_smem<T>(), c->stream>>>(
-            dst, src, B.pp, c->d_pipe_of, c->d_zclass, ecm, ecp, f.a, f.ib, f.cu, c->nx, c->ny,
-            c->nz, c->countz, h);
+            dst, src, B.pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }
@@ -598,6 +752,11 @@ int gw_fused_supported(const gw_ctx *c) {
     return need <= 200 * 1024;
 }
 
+template <typename K>
+static cudaError_t occupancy(int *n, K kernel) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, kernel, 256, 0);
+}
+
 int gw_fused_prepare(gw_ctx *c) {
     // shared-memory opt-in for the column kernel (once per context is enough)
     cudaError_t e;
@@ -621,26 +780,34 @@ int gw_fused_prepare(gw_ctx *c) {
                                       (int)half_smem<double>())) != cudaSuccess)
             return gw_cuda_fail(e, "cudaFuncSetAttribute(k_half_tile)");
     }
+    // the column kernels loop over columns: one resident wave of blocks
     int per_sm = 0;
-    if (c->precision == GW_PREC_MIXED)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rock2_col<float, true>, 256,
-                                                          rock2_smem<float>(c->nz));
-    else
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rock2_col<double, false>, 256,
-                                                          rock2_smem<double>(c->nz));
+    const bool mix = c->precision == GW_PREC_MIXED;
+    switch (rock2_lpt(c->nz)) {
+        case 2: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 2>) : occupancy(&per_sm, k_rock2_reg<double, false, 2>); break;
+        case 4: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 4>) : occupancy(&per_sm, k_rock2_reg<double, false, 4>); break;
+        case 8: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 8>) : occupancy(&per_sm, k_rock2_reg<double, false, 8>); break;
+        case 16: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 16>) : occupancy(&per_sm, k_rock2_reg<double, false, 16>); break;
+        default:
+            e = mix ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rock2_col<float, true>, 256,
+                                                                    rock2_smem<float>(c->nz))
+                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rock2_col<double, false>, 256,
+                                                                    rock2_smem<double>(c->nz));
+    }
     if (e != cudaSuccess) return gw_cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     if (e != cudaSuccess) return gw_cuda_fail(e, "cudaDeviceGetAttribute");
-    c->rock2_grid = (per_sm > 0 ? per_sm : 1) * sms * 8;
+    c->rock2_grid = (per_sm > 0 ? per_sm : 1) * sms;
     return GW_OK;
 }
 
 int gw_fused_set_dt(gw_ctx *c, double dt) {
     const int n = c->nbh * c->countz * 2;
     if (n > 0) {
-        k_adv_table<<<grid_for(n, 128), 128, 0, c->stream>>>(c->d_advtab, c->d_gz, c->d_bh, c->nbh,
-                                                             c->nz, c->countz, dt / 2);
+        k_adv_table<<<grid_for(n, 128), 128, 0, c->stream>>>(
+            c->d_advtab, c->d_gz, c->d_bh, c->precision == GW_PREC_MIXED ? c->d_Tref : nullptr, c->nbh,
+            c->nz, c->countz, dt / 2);
         GW_CUDA(cudaGetLastError());
     }
     GW_CUDA(cudaStreamSynchronize(c->stream));

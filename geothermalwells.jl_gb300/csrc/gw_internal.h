@@ -18,6 +18,7 @@ struct GwBorehole {
 // One departure record of the semi-Lagrangian advection (see k_adv_table).
 struct GwAdvRec {
     double alpha;
+    double dref;   // mixed path: alpha T_ref(ir) + (1 - alpha) T_ref(il) - T_ref(k)
     int il, ir, type, pad;
 };
 
@@ -42,6 +43,10 @@ struct GwCoefTables {
     T *cxm = nullptr, *cxp = nullptr, *cym = nullptr, *cyp = nullptr;
     T *czm = nullptr, *czp = nullptr;
     GwFactors<T> fx, fy;   // for h = dt/2 of the current step size
+    // fused half steps, per (zc, line, row) of x-lines (hx) and y-lines (hy):
+    // 4 values {e0, ep, em, a} * ib folding the explicit sweep of the other
+    // direction into the forward elimination (see gw_build_half_tables)
+    T *hx = nullptr, *hy = nullptr;
 };
 
 struct gw_ctx {
@@ -87,6 +92,8 @@ struct gw_ctx {
     int last_nsteps = 0;
     // fused step (both precisions)
     int *d_pipe_of = nullptr;         // [nx*ny] pipe-column index or -1
+    int *d_pipe_lx = nullptr;         // [ny][nx] pipe index along x-lines (j, i)
+    int *d_pipe_ly = nullptr;         // [nx][ny] pipe index along y-lines (i, j)
     double *d_annpart = nullptr;      // [nbh][32][nz] partial annulus sums
     double *d_outpart = nullptr;      // [nbh][64] partial outlet sums
     GwAdvRec *d_advtab = nullptr;     // [nbh][countz][2] departure table for dt/2
@@ -130,6 +137,9 @@ void gw_build_coefs(const gw_ctx *c, std::vector<double> &cxm, std::vector<doubl
 void gw_build_factors(const gw_ctx *c, double h, int dir, const std::vector<double> &cm,
                       const std::vector<double> &cp, std::vector<double> &a,
                       std::vector<double> &ib, std::vector<double> &cu);
+void gw_build_half_table(const gw_ctx *c, double h, int dir, const std::vector<double> &ecm,
+                         const std::vector<double> &ecp, const std::vector<double> &a,
+                         const std::vector<double> &ib, std::vector<double> &out4);
 int gw_rock2_choose(double dt, double eigen_est, int max_stages, int *s, int *covered);
 void gw_rock2_coefs(int s, const double **mu, const double **nu, const double **kappa,
                     double *sigma, double *tau);

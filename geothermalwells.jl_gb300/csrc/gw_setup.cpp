@@ -316,6 +316,32 @@ void gw_build_factors(const gw_ctx *c, double h, int dir, const std::vector<doub
     }
 }
 
+// Per (z-class, line, row) of one line direction: the explicit sweep of the
+// other direction, (I + h A_e), folded with the forward elimination of
+// (I - h A_line):  y_l = e0 x_c + ep x_+ + em x_- - a y_{l-1}  with
+// e0 = (1 - h (cp + cm)) ib, ep = h cp ib, em = h cm ib, a = lower ib.
+// dir X: x-lines (zc, j, i), explicit y coefficients [zc][i][j];
+// dir Y: y-lines (zc, i, j), explicit x coefficients [zc][j][i].
+void gw_build_half_table(const gw_ctx *c, double h, int dir, const std::vector<double> &ecm,
+                         const std::vector<double> &ecp, const std::vector<double> &a,
+                         const std::vector<double> &ib, std::vector<double> &out4) {
+    const int nl = dir == GW_DIR_X ? c->ny : c->nx;
+    const int N = dir == GW_DIR_X ? c->nx : c->ny;
+    out4.assign((size_t)c->n_zclass * nl * N * 4, 0.0);
+    for (int zc = 0; zc < c->n_zclass; ++zc)
+        for (int m = 0; m < nl; ++m)
+            for (int l = 0; l < N; ++l) {
+                const size_t q = ((size_t)zc * nl + m) * N + l;
+                // explicit coefficient table index of the same cell
+                const size_t e = ((size_t)zc * N + l) * nl + m;
+                const double cm = ecm[e], cp = ecp[e], g = ib[q];
+                out4[4 * q + 0] = (1.0 - h * (cp + cm)) * g;
+                out4[4 * q + 1] = h * cp * g;
+                out4[4 * q + 2] = h * cm * g;
+                out4[4 * q + 3] = a[q] * g;
+            }
+}
+
 // Stage count: the smallest s >= 3 (at least one recurrence stage) whose
 // stability interval l_s covers |dt| * eigen_est, capped at max_stages.
 int gw_rock2_choose(double dt, double eigen_est, int max_stages, int *s, int *covered) {
