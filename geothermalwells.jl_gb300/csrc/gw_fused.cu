@@ -29,6 +29,18 @@ namespace {
 
 inline unsigned grid_for(long long n, int block) { return (unsigned)((n + block - 1) / block); }
 
+// cp.async (4/8-byte, zero-fill when pred is false) and its group fences
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem, bool pred) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    const int n = pred ? BYTES : 0;   // 0: zero-fill, nothing is read
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(s), "l"(gmem), "n"(BYTES),
+                 "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
 // ---------------------------------------------------------------------------
 // 1. ROCK2 on whole columns
 // sc: per recurrence stage j = 1..s-2: (h mu_j, kappa_j); then (h sigma,
@@ -117,10 +129,12 @@ __global__ void __launch_bounds__(256) k_rock2_col(T *__restrict__ u, const int 
 }
 
 // Register-resident variant for nz <= 256 * LPT: thread t owns the LPT
-// consecutive levels [t LPT, t LPT + LPT) in registers, its coefficients
+// consecutive levels [t LPT, t LPT + LPT) in registers, their coefficients
 // too; a stage only exchanges the two end values of each thread's run through
-// shared memory (double-buffered, one barrier per stage).  The next column is
-// loaded into registers while the current one runs its stages.
+// shared memory (double-buffered, one barrier per stage).  Columns and their
+// coefficient rows are staged through shared memory: the block copies the
+// next column (coalesced cp.async) while the current one runs its stages,
+// then every thread picks its run out of shared memory.
 template <typename T, bool INC, int LPT>
 __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int *__restrict__ colprof,
                                                    const T *__restrict__ czm,
@@ -128,13 +142,32 @@ __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int 
                                                    const T *__restrict__ fref,
                                                    const double *__restrict__ sc, int s, int nz,
                                                    long long ncols) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    // [2 buffers][4 rows: field, cm, cp, fref][nzs]
+    T *stage = reinterpret_cast<T *>(smem_raw);
+    const int nzs = 256 * LPT;
     __shared__ T s_lo[2][256], s_hi[2][256];
     const int t = threadIdx.x;
     const int kb = t * LPT;
     const int nv = max(0, min(LPT, nz - kb));   // levels this thread owns
     const bool tail = kb + nv >= nz;            // owns the bottom level of the column
     const int nrec = s - 2;
+    const int nrows = INC ? 4 : 3;
     int xb = 0;
+    auto fetch = [&](long long col, int buf) {
+        T *d = stage + (size_t)buf * 4 * nzs;
+        const int p = colprof[col];
+        const T *srcs[4] = {u + col * nz, czm + (size_t)p * nz, czp + (size_t)p * nz,
+                            fref ? fref + (size_t)p * nz : nullptr};
+        for (int rrow = 0; rrow < nrows; ++rrow) {
+            const T *g = srcs[rrow];
+            for (int k = t; k < nz; k += 256) {
+                const bool ok = g != nullptr;
+                cp_async<sizeof(T)>(d + rrow * nzs + k, ok ? (const void *)(g + k) : (const void *)u, ok);
+            }
+        }
+        cp_async_commit();
+    };
     // neighbours of this thread's run: level kb - 1 and level kb + nv
     auto exchange = [&](const T (&v)[LPT], T &left, T &right) {
         T last = v[0];
@@ -155,35 +188,34 @@ __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int 
         const T gp = (i + 1 < nv) ? v[i + 1 < LPT ? i + 1 : i] : right;
         return cp[i] * (gp - gc) - cm[i] * (gc - gm);
     };
-    T nxt[LPT];
     long long col = blockIdx.x;
-    if (col < ncols) {
-#pragma unroll
-        for (int i = 0; i < LPT; ++i) nxt[i] = i < nv ? u[col * nz + kb + i] : T(0);
-    }
-    for (; col < ncols; col += gridDim.x) {
+    int buf = 0;
+    if (col < ncols) fetch(col, 0);
+    for (; col < ncols; col += gridDim.x, buf ^= 1) {
+        const long long nxt = col + gridDim.x;
+        if (nxt < ncols) {
+            fetch(nxt, buf ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const T *st = stage + (size_t)buf * 4 * nzs + kb;
         T base[LPT], cm[LPT], cp[LPT], F0[LPT], prev[LPT], cur[LPT];
-        const int p = colprof[col];
 #pragma unroll
         for (int i = 0; i < LPT; ++i) {
-            base[i] = nxt[i];
             const bool ok = i < nv;
-            cm[i] = ok ? __ldg(czm + (size_t)p * nz + kb + i) : T(0);
-            cp[i] = ok ? __ldg(czp + (size_t)p * nz + kb + i) : T(0);
-        }
-        const long long ncol_next = col + gridDim.x;
-        if (ncol_next < ncols) {
-#pragma unroll
-            for (int i = 0; i < LPT; ++i) nxt[i] = i < nv ? u[ncol_next * nz + kb + i] : T(0);
+            base[i] = ok ? st[i] : T(0);
+            cm[i] = ok ? st[nzs + i] : T(0);
+            cp[i] = ok ? st[2 * nzs + i] : T(0);
+            F0[i] = (INC && fref && ok) ? st[3 * nzs + i] : T(0);
         }
         T left, right;
         exchange(base, left, right);
         if (INC) {
 #pragma unroll
             for (int i = 0; i < LPT; ++i) {
-                T f = apply(base, cm, cp, i, left, right);
-                if (fref && i < nv) f += __ldg(fref + (size_t)p * nz + kb + i);
-                F0[i] = f;
+                F0[i] += apply(base, cm, cp, i, left, right);
                 prev[i] = T(0);
                 cur[i] = T(0);
             }
@@ -228,13 +260,19 @@ __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int 
             }
         }
         exchange(q, left, right);
+        // results go back through the staging buffer for a coalesced store
+        T *so = stage + (size_t)buf * 4 * nzs;
 #pragma unroll
         for (int i = 0; i < LPT; ++i) {
             T a = apply(q, cm, cp, i, left, right);
             if (INC) a += F0[i];
             const T y = q[i] + hts * a + c3 * (q[i] - cur[i]);
-            if (i < nv) u[col * nz + kb + i] = INC ? base[i] + y : y;
+            if (i < nv) so[kb + i] = INC ? base[i] + y : y;
         }
+        __syncthreads();
+        T *uc = u + col * nz;
+        for (int k = t; k < nz; k += 256) uc[k] = so[k];
+        __syncthreads();   // this buffer is refilled by the next iteration's fetch
     }
 }
 
@@ -468,19 +506,10 @@ __global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *_
 // forward sweep stores y_l in dst; the backward sweep reads it back in
 // batches loaded ahead of their use and overwrites it with x_l.
 constexpr int kHW = 4;    // lines (warps) per block
-constexpr int kHR = 32;   // rows per chunk
+constexpr int kHR = 16;   // rows per chunk (a multiple of kHG)
+constexpr int kHG = 4;    // rows whose coefficients are loaded together
 constexpr int kHB = 8;    // rows per backward batch
 
-template <int BYTES>
-__device__ __forceinline__ void cp_async(void *smem, const void *gmem, bool pred) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    const int n = pred ? BYTES : 0;   // 0: zero-fill, nothing is read
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(s), "l"(gmem), "n"(BYTES),
-                 "r"(n));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 template <typename T>
 struct alignas(4 * sizeof(T)) Quad {
@@ -548,18 +577,30 @@ __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, con
         __syncthreads();
         const T *row = tile + (ch & 1) * kTile + warp * 32 + lane;
         const int rmax = min(kHR, N - ch * kHR);
-        for (int r = 0; r < rmax; ++r, row += kRow) {
-            const int l = ch * kHR + r;
-            const T xm = row[0], xc = row[32], xp = row[64];
-            const Quad<T> q = hq[fb + l];
-            const T ay = q.w * y;
-            T yn = fma(q.x, xc, fma(q.y, xp, fma(q.z, xm, -ay)));
-            if (pipe_levels) {
-                const int pq = __ldg(pline + l);
-                if (pq >= 0) yn = fma(pp[(size_t)pq * countz + k], __ldg(fib + fb + l), -ay);
+        for (int r0 = 0; r0 < rmax; r0 += kHG) {
+            // the group's loads are issued before its dependent updates
+            Quad<T> q[kHG];
+            int pq[kHG];
+            T xm[kHG], xc[kHG], xp[kHG];
+#pragma unroll
+            for (int g = 0; g < kHG; ++g) {
+                const int r = min(r0 + g, rmax - 1);
+                const int l = ch * kHR + r;
+                q[g] = hq[fb + l];
+                pq[g] = pipe_levels ? __ldg(pline + l) : -1;
+                const T *rw = row + r * kRow;
+                xm[g] = rw[0]; xc[g] = rw[32]; xp[g] = rw[64];
             }
-            y = yn;
-            if (active) dst[k + m * mst + (long long)l * rst] = y;
+#pragma unroll
+            for (int g = 0; g < kHG; ++g) {
+                if (r0 + g >= rmax) break;
+                const int l = ch * kHR + r0 + g;
+                const T ay = q[g].w * y;
+                T yn = fma(q[g].x, xc[g], fma(q[g].y, xp[g], fma(q[g].z, xm[g], -ay)));
+                if (pq[g] >= 0) yn = fma(pp[(size_t)pq[g] * countz + k], __ldg(fib + fb + l), -ay);
+                y = yn;
+                if (active) dst[k + m * mst + (long long)l * rst] = y;
+            }
         }
         __syncthreads();   // the buffer is refilled two chunks later
     }
@@ -568,23 +609,27 @@ __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, con
     // batch is processed, so the loads overlap the dependent chain
     T x = y;
     T *col = dst + k + m * mst;
-    T cur[kHB], nxt[kHB];
+    T cur[kHB], nxt[kHB], cuc[kHB], cun[kHB];
     int l = N - 2;
-    auto load_batch = [&](T *v, int top) {
+    auto load_batch = [&](T *v, T *cv, int top) {
 #pragma unroll
-        for (int b = 0; b < kHB; ++b) v[b] = (top - b >= 0) ? col[(long long)(top - b) * rst] : T(0);
+        for (int b = 0; b < kHB; ++b) {
+            const bool ok = top - b >= 0;
+            v[b] = ok ? col[(long long)(top - b) * rst] : T(0);
+            cv[b] = ok ? __ldg(fcu + fb + (top - b)) : T(0);
+        }
     };
-    load_batch(cur, l);
+    load_batch(cur, cuc, l);
     while (l >= 0) {
-        load_batch(nxt, l - kHB);
+        load_batch(nxt, cun, l - kHB);
 #pragma unroll
         for (int b = 0; b < kHB; ++b) {
             if (l - b < 0) break;
-            x = cur[b] - __ldg(fcu + fb + (l - b)) * x;
+            x = cur[b] - cuc[b] * x;
             col[(long long)(l - b) * rst] = x;
         }
 #pragma unroll
-        for (int b = 0; b < kHB; ++b) cur[b] = nxt[b];
+        for (int b = 0; b < kHB; ++b) { cur[b] = nxt[b]; cuc[b] = cun[b]; }
         l -= kHB;
     }
 }
@@ -623,6 +668,9 @@ size_t rock2_smem(int nz) {
     return (size_t)nz * sizeof(T) * (inc ? 4 : 2);
 }
 
+template <typename T>
+size_t reg_smem(int lpt) { return 2 * 4 * (size_t)256 * lpt * sizeof(T); }
+
 // levels per thread of the register-resident ROCK2 kernel (0: use the
 // shared-memory kernel)
 inline int rock2_lpt(int nz) {
@@ -639,10 +687,10 @@ int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *
     const int lpt = rock2_lpt(c->nz);
     unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid ? ncols : c->rock2_grid);
     switch (lpt) {
-        case 2: k_rock2_reg<T, INC, 2><<<grid, 256, 0, c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
-        case 4: k_rock2_reg<T, INC, 4><<<grid, 256, 0, c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
-        case 8: k_rock2_reg<T, INC, 8><<<grid, 256, 0, c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
-        case 16: k_rock2_reg<T, INC, 16><<<grid, 256, 0, c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
+        case 2: k_rock2_reg<T, INC, 2><<<grid, 256, reg_smem<T>(2), c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
+        case 4: k_rock2_reg<T, INC, 4><<<grid, 256, reg_smem<T>(4), c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
+        case 8: k_rock2_reg<T, INC, 8><<<grid, 256, reg_smem<T>(8), c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
+        case 16: k_rock2_reg<T, INC, 16><<<grid, 256, reg_smem<T>(16), c->stream>>>(u, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
         default:
             k_rock2_col<T, INC><<<grid, 256, rock2_smem<T>(c->nz), c->stream>>>(u, c->d_colprof, czm, czp, fref,
                                                                             c->d_stage, s, c->nz, ncols);
@@ -753,8 +801,10 @@ int gw_fused_supported(const gw_ctx *c) {
 }
 
 template <typename K>
-static cudaError_t occupancy(int *n, K kernel) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, kernel, 256, 0);
+static cudaError_t occupancy(int *n, K kernel, size_t smem) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, kernel, 256, smem);
 }
 
 int gw_fused_prepare(gw_ctx *c) {
@@ -784,10 +834,10 @@ int gw_fused_prepare(gw_ctx *c) {
     int per_sm = 0;
     const bool mix = c->precision == GW_PREC_MIXED;
     switch (rock2_lpt(c->nz)) {
-        case 2: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 2>) : occupancy(&per_sm, k_rock2_reg<double, false, 2>); break;
-        case 4: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 4>) : occupancy(&per_sm, k_rock2_reg<double, false, 4>); break;
-        case 8: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 8>) : occupancy(&per_sm, k_rock2_reg<double, false, 8>); break;
-        case 16: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 16>) : occupancy(&per_sm, k_rock2_reg<double, false, 16>); break;
+        case 2: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 2>, reg_smem<float>(2)) : occupancy(&per_sm, k_rock2_reg<double, false, 2>, reg_smem<double>(2)); break;
+        case 4: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 4>, reg_smem<float>(4)) : occupancy(&per_sm, k_rock2_reg<double, false, 4>, reg_smem<double>(4)); break;
+        case 8: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 8>, reg_smem<float>(8)) : occupancy(&per_sm, k_rock2_reg<double, false, 8>, reg_smem<double>(8)); break;
+        case 16: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 16>, reg_smem<float>(16)) : occupancy(&per_sm, k_rock2_reg<double, false, 16>, reg_smem<double>(16)); break;
         default:
             e = mix ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rock2_col<float, true>, 256,
                                                                     rock2_smem<float>(c->nz))
