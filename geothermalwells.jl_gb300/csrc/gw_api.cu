@@ -1,6 +1,7 @@
 // gw_api.cu -- the extern "C" entry points declared in include/gw_gb300.h.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -218,6 +219,11 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         (rc = dalloc(c, &c->c64.fx.cu, cxm.size())) || (rc = dalloc(c, &c->c64.fy.a, cym.size())) ||
         (rc = dalloc(c, &c->c64.fy.ib, cym.size())) || (rc = dalloc(c, &c->c64.fy.cu, cym.size())))
         return fail(rc);
+    std::vector<int> order((size_t)c->nx * c->ny);
+    for (size_t q = 0; q < order.size(); ++q) order[q] = (int)q;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return c->colprof[x] < c->colprof[y]; });
+    if ((rc = upload(c, &c->d_colorder, order))) return fail(rc);
     if ((rc = upload(c, &c->d_gz, c->gz)) || (rc = upload(c, &c->d_zclass, c->zclass)) ||
         (rc = upload(c, &c->d_colprof, c->colprof)) || (rc = upload(c, &c->d_pipe_i, c->pipe_i)) ||
         (rc = upload(c, &c->d_pipe_j, c->pipe_j)) || (rc = upload(c, &c->d_pipe_b, c->pipe_b)))

@@ -73,6 +73,7 @@ struct gw_ctx {
     // device: grids, tables, lists
     double *d_gz = nullptr;
     int *d_zclass = nullptr, *d_colprof = nullptr;
+    int *d_colorder = nullptr;        // columns sorted by profile
     int *d_pipe_i = nullptr, *d_pipe_j = nullptr, *d_pipe_b = nullptr;
     GwBhDev *d_bh = nullptr;
     GwCoefTables<double> c64;
