@@ -636,117 +636,6 @@ __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, con
     }
 }
 
-// Mixed-path variant that keeps y in shared memory: a block of M warps
-// (M lines, 32 levels each) holds all N forward-sweep values of its lines,
-// so y never travels to L2 and back; M is the largest count whose y buffer
-// and row tiles fit in shared memory (M >= 2).
-constexpr int kSR = 16;   // rows per chunk
-
-__global__ void __launch_bounds__(256) k_half_smem(float *__restrict__ dst, const float *__restrict__ src,
-                                                   const float *__restrict__ pp,
-                                                   const int *__restrict__ pipe_line,
-                                                   const int *__restrict__ zclass,
-                                                   const Quad<float> *__restrict__ hq,
-                                                   const float *__restrict__ fib,
-                                                   const float *__restrict__ fcu, int nx, int ny,
-                                                   int nz, int countz, int xl) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int M = blockDim.x >> 5;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nl = xl ? ny : nx;
-    const int N = xl ? nx : ny;
-    const int kRow = (M + 2) * 32;
-    const int kTile = kSR * kRow;
-    float *tile = reinterpret_cast<float *>(smem_raw);   // [2][kSR][M + 2][32]
-    float *ybuf = tile + 2 * kTile;                       // [M][N][32]
-    const int k0 = blockIdx.x * 32, m0 = blockIdx.y * M;
-    const int k = k0 + lane, m = m0 + warp;
-    const bool kok = k < nz;
-    const bool active = kok && m < nl;
-    const int kc = kok ? k : nz - 1, mc = m < nl ? m : nl - 1;
-    const long long mst = xl ? (long long)nz : (long long)nz * ny;
-    const long long rst = xl ? (long long)nz * ny : (long long)nz;
-    const size_t fb = ((size_t)zclass[kc] * nl + mc) * N;
-    const int *pline = pipe_line + (size_t)mc * N;
-    const bool pipe_levels = k < countz;
-    const int nchunk = (N + kSR - 1) / kSR;
-    float *yw = ybuf + (size_t)warp * N * 32 + lane;
-
-    auto load_chunk = [&](int ch, int buf) {
-        float *t = tile + buf * kTile;
-        const int l0 = ch * kSR;
-        for (int mm = warp; mm < M + 2; mm += M) {
-            const int gm = m0 - 1 + mm;
-            const bool lok = kok && gm >= 0 && gm < nl;
-            const float *g = src + k + (long long)gm * mst + (long long)l0 * rst;
-            float *d = t + mm * 32 + lane;
-            for (int r = 0; r < kSR; ++r) {
-                const bool ok = lok && l0 + r < N;
-                cp_async<4>(d + r * kRow, ok ? (const void *)(g + (long long)r * rst) : (const void *)src, ok);
-            }
-        }
-        cp_async_commit();
-    };
-
-    float y = 0.f;
-    load_chunk(0, 0);
-    for (int ch = 0; ch < nchunk; ++ch) {
-        if (ch + 1 < nchunk) {
-            load_chunk(ch + 1, (ch + 1) & 1);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
-        __syncthreads();
-        const float *row = tile + (ch & 1) * kTile + warp * 32 + lane;
-        const int rmax = min(kSR, N - ch * kSR);
-        for (int r0 = 0; r0 < rmax; r0 += kHG) {
-            Quad<float> q[kHG];
-            int pq[kHG];
-            float xm[kHG], xc[kHG], xp[kHG];
-#pragma unroll
-            for (int g = 0; g < kHG; ++g) {
-                const int r = min(r0 + g, rmax - 1);
-                const int l = ch * kSR + r;
-                q[g] = hq[fb + l];
-                pq[g] = pipe_levels ? __ldg(pline + l) : -1;
-                const float *rw = row + r * kRow;
-                xm[g] = rw[0]; xc[g] = rw[32]; xp[g] = rw[64];
-            }
-#pragma unroll
-            for (int g = 0; g < kHG; ++g) {
-                if (r0 + g >= rmax) break;
-                const int l = ch * kSR + r0 + g;
-                const float ay = q[g].w * y;
-                float yn = fmaf(q[g].x, xc[g], fmaf(q[g].y, xp[g], fmaf(q[g].z, xm[g], -ay)));
-                if (pq[g] >= 0) yn = fmaf(pp[(size_t)pq[g] * countz + k], __ldg(fib + fb + l), -ay);
-                y = yn;
-                yw[(size_t)l * 32] = y;
-            }
-        }
-        __syncthreads();   // the tile buffer is refilled two chunks later
-    }
-    if (!active) return;
-    float x = y;
-    float *col = dst + k + m * mst;
-    col[(long long)(N - 1) * rst] = x;
-    for (int l0 = N - 2; l0 >= 0; l0 -= kHB) {
-        float cu[kHB], yv[kHB];
-#pragma unroll
-        for (int b = 0; b < kHB; ++b) {
-            const int l = max(l0 - b, 0);
-            cu[b] = __ldg(fcu + fb + l);
-            yv[b] = yw[(size_t)l * 32];
-        }
-#pragma unroll
-        for (int b = 0; b < kHB; ++b) {
-            if (l0 - b < 0) break;
-            x = yv[b] - cu[b] * x;
-            col[(long long)(l0 - b) * rst] = x;
-        }
-    }
-}
-
 template <typename T>
 __global__ void k_finite(const T *__restrict__ u, size_t n, int *__restrict__ flag) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -865,37 +754,10 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h) {
 template <typename T>
 size_t half_smem() { return 2 * (size_t)kHR * (kHW + 2) * 32 * sizeof(T); }
 
-// lines (warps) per block of k_half_smem for line length N, 0 if < 2 fit
-inline int half_smem_lines(int N) {
-    const size_t cap = 227 * 1024;
-    for (int M = 8; M >= 2; --M) {
-        size_t need = (size_t)M * N * 32 * 4 + 2 * (size_t)kSR * (M + 2) * 32 * 4;
-        if (need <= cap) return M;
-    }
-    return 0;
-}
-inline size_t half_smem_bytes(int M, int N) {
-    return (size_t)M * N * 32 * 4 + 2 * (size_t)kSR * (M + 2) * 32 * 4;
-}
-
 template <typename T>
 int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h) {
     (void)h;   // folded into the half-step tables
     Bufs<T> B = bufs<T>(c);
-    if (sizeof(T) == 4) {
-        const int N = xlines ? c->nx : c->ny, nl = xlines ? c->ny : c->nx;
-        const int M = half_smem_lines(N);
-        if (M >= 2) {
-            const GwFactors<float> &f = xlines ? c->c32.fx : c->c32.fy;
-            const Quad<float> *hq = reinterpret_cast<const Quad<float> *>(xlines ? c->c32.hx : c->c32.hy);
-            dim3 grid((c->nz + 31) / 32, (nl + M - 1) / M);
-            k_half_smem<<<grid, 32 * M, half_smem_bytes(M, N), c->stream>>>(
-                (float *)dst, (const float *)src, c->f_pp, xlines ? c->d_pipe_lx : c->d_pipe_ly,
-                c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz, xlines);
-            GW_CUDA(cudaGetLastError());
-            return GW_OK;
-        }
-    }
     const GwFactors<T> &f = xlines ? B.ct->fx : B.ct->fy;
     const Quad<T> *hq = reinterpret_cast<const Quad<T> *>(xlines ? B.ct->hx : B.ct->hy);
     const int nl = xlines ? c->ny : c->nx;
@@ -958,13 +820,6 @@ int gw_fused_prepare(gw_ctx *c) {
                                  (int)rock2_smem<double>(c->nz));
     if (e != cudaSuccess) return gw_cuda_fail(e, "cudaFuncSetAttribute(k_rock2_col)");
     if (c->precision == GW_PREC_MIXED) {
-        const int Mx = half_smem_lines(c->nx), My = half_smem_lines(c->ny);
-        size_t need = 0;
-        if (Mx >= 2) need = std::max(need, half_smem_bytes(Mx, c->nx));
-        if (My >= 2) need = std::max(need, half_smem_bytes(My, c->ny));
-        if (need > 0 &&
-            (e = cudaFuncSetAttribute(k_half_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need)) != cudaSuccess)
-            return gw_cuda_fail(e, "cudaFuncSetAttribute(k_half_smem)");
         if ((e = cudaFuncSetAttribute(k_half_tile<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)half_smem<float>())) != cudaSuccess ||
             (e = cudaFuncSetAttribute(k_half_tile<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
