@@ -121,6 +121,8 @@ int upload_stages(gw_ctx *c, double dt, int s) {
     sc.push_back(1.0 - tau / (sigma * sigma));
     if ((int)sc.size() > GW_STAGE_TABLE) return gw_fail(GW_ERR_ARG, "stage table too long");
     GW_CUDA(cudaMemcpy(c->d_stage, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<float> sf(sc.begin(), sc.end());
+    GW_CUDA(cudaMemcpy(c->f_stage, sf.data(), sf.size() * sizeof(float), cudaMemcpyHostToDevice));
     return GW_OK;
 }
 
@@ -247,11 +249,21 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         slot = q;
     }
     for (auto &B : bhd) { if (B.inner_begin < 0) B.inner_begin = 0; if (B.outer_begin < 0) B.outer_begin = 0; }
-    std::vector<int> plx((size_t)c->ny * c->nx);
+    // per line direction: pipe index along each line, then one flag per line
+    // telling whether the line crosses any pipe column
+    std::vector<int> plx((size_t)c->ny * c->nx + c->ny, 0), ply((size_t)c->nx * c->ny + c->nx, 0);
     for (int i = 0; i < c->nx; ++i)
-        for (int j = 0; j < c->ny; ++j) plx[(size_t)j * c->nx + i] = pipe_of[(size_t)i * c->ny + j];
+        for (int j = 0; j < c->ny; ++j) {
+            const int q = pipe_of[(size_t)i * c->ny + j];
+            plx[(size_t)j * c->nx + i] = q;
+            ply[(size_t)i * c->ny + j] = q;
+            if (q >= 0) {
+                plx[(size_t)c->ny * c->nx + j] = 1;
+                ply[(size_t)c->nx * c->ny + i] = 1;
+            }
+        }
     if ((rc = upload(c, &c->d_bh, bhd)) || (rc = upload(c, &c->d_pipe_of, pipe_of)) ||
-        (rc = upload(c, &c->d_pipe_lx, plx)) || (rc = upload(c, &c->d_pipe_ly, pipe_of)))
+        (rc = upload(c, &c->d_pipe_lx, plx)) || (rc = upload(c, &c->d_pipe_ly, ply)))
         return fail(rc);
     const size_t N = ncell(c);
     if ((rc = dalloc(c, &c->d_utmp, (size_t)ncol * c->countz)) ||
@@ -260,7 +272,7 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         (rc = dalloc(c, &c->d_outpart, (size_t)c->nbh * 64)) ||
         (rc = dalloc(c, &c->d_advtab, (size_t)c->nbh * c->countz * 2)) ||
         (rc = dalloc(c, &c->d_outlet, c->nbh)) || (rc = dalloc(c, &c->d_energy, c->nbh)) ||
-        (rc = dalloc(c, &c->d_stage, GW_STAGE_TABLE)) ||
+        (rc = dalloc(c, &c->d_stage, GW_STAGE_TABLE)) || (rc = dalloc(c, &c->f_stage, GW_STAGE_TABLE)) ||
         (rc = dalloc(c, &c->d_step_counter, 1)) || (rc = dalloc(c, &c->d_flag, 1)))
         return fail(rc);
     if (mixed(c)) {

@@ -138,17 +138,22 @@ __global__ void __launch_bounds__(256) k_rock2_col(T *__restrict__ u, const int 
 // column of a profile) stay in registers and are reloaded only when the
 // profile changes.  The next column is copied into shared memory with
 // coalesced cp.async while the current one runs its stages.
+// Staging index of level k: one pad word per 32, so the coalesced copies
+// (consecutive k per lane) and the per-thread runs (k = LPT t + i) are both
+// free of shared-memory bank conflicts.
+__device__ __forceinline__ int spad(int k) { return k + (k >> 5); }
+
 template <typename T, bool INC, int LPT>
 __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int *__restrict__ order,
                                                    const int *__restrict__ colprof,
                                                    const T *__restrict__ czm,
                                                    const T *__restrict__ czp,
                                                    const T *__restrict__ fref,
-                                                   const double *__restrict__ sc, int s, int nz,
+                                                   const T *__restrict__ sc, int s, int nz,
                                                    long long ncols) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *stage = reinterpret_cast<T *>(smem_raw);   // [2][256 * LPT]
-    const int nzs = 256 * LPT;
+    T *stage = reinterpret_cast<T *>(smem_raw);   // [2][spad(256 * LPT)]
+    const int nzs = spad(256 * LPT);
     __shared__ T s_lo[2][256], s_hi[2][256];
     const int t = threadIdx.x;
     const int kb = t * LPT;
@@ -159,7 +164,7 @@ __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int 
     auto fetch = [&](long long col, int buf) {
         T *d = stage + (size_t)buf * nzs;
         const T *g = u + col * nz;
-        for (int k = t; k < nz; k += 256) cp_async<sizeof(T)>(d + k, g + k, true);
+        for (int k = t; k < nz; k += 256) cp_async<sizeof(T)>(d + spad(k), g + k, true);
         cp_async_commit();
     };
     // neighbours of this thread's run: level kb - 1 and level kb + nv
@@ -212,7 +217,7 @@ __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int 
         T *st = stage + (size_t)buf * nzs;
         T base[LPT], F0[LPT], prev[LPT], cur[LPT];
 #pragma unroll
-        for (int i = 0; i < LPT; ++i) base[i] = i < nv ? st[kb + i] : T(0);
+        for (int i = 0; i < LPT; ++i) base[i] = i < nv ? st[spad(kb + i)] : T(0);
         T left, right;
         exchange(base, left, right);
         if (INC) {
@@ -269,11 +274,11 @@ __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int 
             T a = apply(q, cm, cp, i, left, right);
             if (INC) a += F0[i];
             const T y = q[i] + hts * a + c3 * (q[i] - cur[i]);
-            if (i < nv) st[kb + i] = INC ? base[i] + y : y;
+            if (i < nv) st[spad(kb + i)] = INC ? base[i] + y : y;
         }
         __syncthreads();
         T *uc = u + col * nz;
-        for (int k = t; k < nz; k += 256) uc[k] = st[k];
+        for (int k = t; k < nz; k += 256) uc[k] = st[spad(k)];
         __syncthreads();   // this buffer is refilled by the next iteration's fetch
     }
 }
@@ -507,7 +512,7 @@ __global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *_
 // the next chunk is in flight while the current one is eliminated.  The
 // forward sweep stores y_l in dst; the backward sweep reads it back in
 // batches loaded ahead of their use and overwrites it with x_l.
-constexpr int kHW = 4;    // lines (warps) per block
+constexpr int kHW = 8;    // lines (warps) per block
 constexpr int kHR = 16;   // rows per chunk (a multiple of kHG)
 constexpr int kHG = 4;    // rows whose coefficients are loaded together
 constexpr int kHB = 8;    // rows per backward batch
@@ -544,7 +549,10 @@ __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, con
     const long long rst = XL ? (long long)nz * ny : (long long)nz;
     const size_t fb = ((size_t)zclass[kc] * nl + mc) * N;
     const int *pline = pipe_line + (size_t)mc * N;
-    const bool pipe_levels = k < countz;
+    // lines through no pipe column skip the per-row pipe lookup (most lines)
+    const bool pipe_levels = k < countz && __ldg(pipe_line + (size_t)nl * N + mc) != 0;
+    const Quad<T> *hql = hq + fb;
+    T *dl = dst + k + m * mst;   // row 0 of this thread's line
     const int nchunk = (N + kHR - 1) / kHR;
 
     // this warp copies neighbour-line slots mm = warp and warp + kHW of each row
@@ -588,20 +596,21 @@ __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, con
             for (int g = 0; g < kHG; ++g) {
                 const int r = min(r0 + g, rmax - 1);
                 const int l = ch * kHR + r;
-                q[g] = hq[fb + l];
+                q[g] = hql[l];
                 pq[g] = pipe_levels ? __ldg(pline + l) : -1;
                 const T *rw = row + r * kRow;
                 xm[g] = rw[0]; xc[g] = rw[32]; xp[g] = rw[64];
             }
+            T *dr = dl + (long long)(ch * kHR + r0) * rst;
 #pragma unroll
             for (int g = 0; g < kHG; ++g) {
                 if (r0 + g >= rmax) break;
-                const int l = ch * kHR + r0 + g;
                 const T ay = q[g].w * y;
                 T yn = fma(q[g].x, xc[g], fma(q[g].y, xp[g], fma(q[g].z, xm[g], -ay)));
-                if (pq[g] >= 0) yn = fma(pp[(size_t)pq[g] * countz + k], __ldg(fib + fb + l), -ay);
+                if (pq[g] >= 0) yn = fma(pp[(size_t)pq[g] * countz + k], __ldg(fib + fb + ch * kHR + r0 + g), -ay);
                 y = yn;
-                if (active) dst[k + m * mst + (long long)l * rst] = y;
+                if (active) *dr = y;
+                dr += rst;
             }
         }
         __syncthreads();   // the buffer is refilled two chunks later
@@ -671,7 +680,7 @@ size_t rock2_smem(int nz) {
 }
 
 template <typename T>
-size_t reg_smem(int lpt) { return 2 * (size_t)256 * lpt * sizeof(T); }
+size_t reg_smem(int lpt) { return 2 * (size_t)(256 * lpt + 8 * lpt) * sizeof(T); }
 
 // levels per thread of the register-resident ROCK2 kernel (0: use the
 // shared-memory kernel)
@@ -683,16 +692,23 @@ inline int rock2_lpt(int nz) {
     return 0;
 }
 
+template <typename T>
+const T *stage_table(gw_ctx *c);
+template <>
+const double *stage_table<double>(gw_ctx *c) { return c->d_stage; }
+template <>
+const float *stage_table<float>(gw_ctx *c) { return c->f_stage; }
+
 template <typename T, bool INC>
 int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *fref) {
     const long long ncols = (long long)c->nx * c->ny;
     const int lpt = rock2_lpt(c->nz);
     unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid ? ncols : c->rock2_grid);
     switch (lpt) {
-        case 2: k_rock2_reg<T, INC, 2><<<grid, 256, reg_smem<T>(2), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
-        case 4: k_rock2_reg<T, INC, 4><<<grid, 256, reg_smem<T>(4), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
-        case 8: k_rock2_reg<T, INC, 8><<<grid, 256, reg_smem<T>(8), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
-        case 16: k_rock2_reg<T, INC, 16><<<grid, 256, reg_smem<T>(16), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, c->d_stage, s, c->nz, ncols); break;
+        case 2: k_rock2_reg<T, INC, 2><<<grid, 256, reg_smem<T>(2), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 4: k_rock2_reg<T, INC, 4><<<grid, 256, reg_smem<T>(4), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 8: k_rock2_reg<T, INC, 8><<<grid, 256, reg_smem<T>(8), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 16: k_rock2_reg<T, INC, 16><<<grid, 256, reg_smem<T>(16), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
         default:
             k_rock2_col<T, INC><<<grid, 256, rock2_smem<T>(c->nz), c->stream>>>(u, c->d_colprof, czm, czp, fref,
                                                                             c->d_stage, s, c->nz, ncols);

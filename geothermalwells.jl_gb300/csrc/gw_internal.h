@@ -93,12 +93,13 @@ struct gw_ctx {
     int last_nsteps = 0;
     // fused step (both precisions)
     int *d_pipe_of = nullptr;         // [nx*ny] pipe-column index or -1
-    int *d_pipe_lx = nullptr;         // [ny][nx] pipe index along x-lines (j, i)
-    int *d_pipe_ly = nullptr;         // [nx][ny] pipe index along y-lines (i, j)
+    int *d_pipe_lx = nullptr;         // [ny][nx] pipe index along x-lines (j, i), then [ny] line flags
+    int *d_pipe_ly = nullptr;         // [nx][ny] pipe index along y-lines (i, j), then [nx] line flags
     double *d_annpart = nullptr;      // [nbh][32][nz] partial annulus sums
     double *d_outpart = nullptr;      // [nbh][64] partial outlet sums
     GwAdvRec *d_advtab = nullptr;     // [nbh][countz][2] departure table for dt/2
     double *d_stage = nullptr;        // ROCK2 stage coefficients of the captured step
+    float *f_stage = nullptr;         // the same, rounded to float (mixed path)
     double *d_tp = nullptr;           // double path: [ncol][nz] swept pipe columns
     double *d_pp = nullptr;           // double path: [ncol][countz] advected pipe values
     int rock2_grid = 0;
