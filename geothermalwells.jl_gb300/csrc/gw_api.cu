@@ -249,6 +249,21 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         slot = q;
     }
     for (auto &B : bhd) { if (B.inner_begin < 0) B.inner_begin = 0; if (B.outer_begin < 0) B.outer_begin = 0; }
+    // chunks of at most 32 pipe columns, never spanning two boreholes or pipes
+    std::vector<int4> chunks;
+    std::vector<int> bchunk(4 * (size_t)c->nbh, 0);
+    for (int b = 0; b < c->nbh; ++b)
+        for (int outer = 0; outer < 2; ++outer) {
+            const int q0 = outer ? bhd[b].outer_begin : bhd[b].inner_begin;
+            const int n = outer ? bhd[b].outer_count : bhd[b].inner_count;
+            bchunk[4 * b + 2 * outer] = (int)chunks.size();
+            for (int q = q0; q < q0 + n; q += 32) chunks.push_back(make_int4(b, q, std::min(q + 32, q0 + n), outer));
+            bchunk[4 * b + 2 * outer + 1] = (int)chunks.size();
+        }
+    c->n_pipe_chunks = (int)chunks.size();
+    if ((rc = upload(c, &c->d_pipe_chunks, chunks)) || (rc = upload(c, &c->d_bchunk, bchunk)) ||
+        (rc = dalloc(c, &c->d_pipepart, (size_t)std::max(c->n_pipe_chunks, 1) * c->nz)))
+        return fail(rc);
     // per line direction: pipe index along each line, then one flag per line
     // telling whether the line crosses any pipe column
     std::vector<int> plx((size_t)c->ny * c->nx + c->ny, 0), ply((size_t)c->nx * c->ny + c->nx, 0);
@@ -276,7 +291,8 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         (rc = dalloc(c, &c->d_step_counter, 1)) || (rc = dalloc(c, &c->d_flag, 1)))
         return fail(rc);
     if (mixed(c)) {
-        if ((rc = dalloc(c, &c->f_u, N)) || (rc = dalloc(c, &c->f_temp, N)) || (rc = dalloc(c, &c->f_g1, N)) ||
+        // f_temp and f_g1 are one block, so together they can stage a double field
+        if ((rc = dalloc(c, &c->f_u, N)) || (rc = dalloc(c, &c->f_temp, 2 * N)) ||
             (rc = dalloc(c, &c->f_tp, (size_t)ncol * c->nz)) ||
             (rc = dalloc(c, &c->f_pp, (size_t)ncol * c->countz)) ||
             (rc = dalloc(c, &c->f_fref, (size_t)c->n_profiles * c->nz)) ||
@@ -291,6 +307,7 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
             (rc = dalloc(c, &c->c32.fy.ib, cym.size())) || (rc = dalloc(c, &c->c32.fy.cu, cym.size())) ||
             (rc = dalloc(c, &c->c32.hx, 4 * cxm.size())) || (rc = dalloc(c, &c->c32.hy, 4 * cym.size())))
             return fail(rc);
+        c->f_g1 = c->f_temp + N;
         GW_CUDA(cudaMemset(c->f_u, 0, N * sizeof(float)));
         std::vector<double> zero(c->nz, 0.0);
         if ((rc = set_reference_profile(c, zero.data()))) return fail(rc);
@@ -344,12 +361,7 @@ int gw_set_field(gw_ctx *c, const double *T) {
     if (mixed(c)) {
         if ((rc = set_reference_profile(c, T))) return rc;
         c->graph_dt = -1.0;   // the advection table depends on T_ref
-        const size_t N = ncell(c);
-        std::vector<float> th(N);
-        const int nz = c->nz;
-        for (size_t q = 0; q < N; ++q) th[q] = (float)(T[q] - c->Tref[q % nz]);
-        GW_CUDA(cudaMemcpy(c->f_u, th.data(), N * sizeof(float), cudaMemcpyHostToDevice));
-        return GW_OK;
+        return gw_fused_set_theta(c, T);
     }
     GW_CUDA(cudaMemcpyAsync(c->d_u, T, ncell(c) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     return sync(c);
@@ -359,15 +371,7 @@ int gw_get_field(gw_ctx *c, double *T) {
     if (!c || !T) return gw_fail(GW_ERR_ARG, "NULL argument");
     int rc = set_device(c);
     if (rc) return rc;
-    if (mixed(c)) {
-        const size_t N = ncell(c);
-        std::vector<float> th(N);
-        GW_CUDA(cudaMemcpyAsync(th.data(), c->f_u, N * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-        if ((rc = sync(c))) return rc;
-        const int nz = c->nz;
-        for (size_t q = 0; q < N; ++q) T[q] = (double)th[q] + c->Tref[q % nz];
-        return GW_OK;
-    }
+    if (mixed(c)) return gw_fused_get_theta(c, T);
     GW_CUDA(cudaMemcpyAsync(T, c->d_u, ncell(c) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     return sync(c);
 }

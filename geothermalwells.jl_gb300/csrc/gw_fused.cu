@@ -284,37 +284,7 @@ __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int 
 }
 
 // ---------------------------------------------------------------------------
-// 2. pipe columns: explicit sweep (I + h A_dir) into tp[q][k], all levels
-template <typename T>
-__global__ void __launch_bounds__(256) k_pipe_explicit(T *__restrict__ tp, const T *__restrict__ src,
-                                                       const int *__restrict__ pi,
-                                                       const int *__restrict__ pj,
-                                                       const int *__restrict__ zclass,
-                                                       const T *__restrict__ cmt,
-                                                       const T *__restrict__ cpt, int nx, int ny,
-                                                       int nz, int ncol, double h, int dir) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= (long long)ncol * nz) return;
-    const int k = (int)(e % nz);
-    const int q = (int)(e / nz);
-    const int i = pi[q], j = pj[q];
-    const long long c = k + (long long)nz * (j + (long long)ny * i);
-    const int zc = zclass[k];
-    T xc = src[c], xp, xm;
-    size_t t;
-    if (dir == GW_DIR_X) {
-        long long st = (long long)nz * ny;
-        xp = (i < nx - 1) ? src[c + st] : xc;
-        xm = (i > 0) ? src[c - st] : xc;
-        t = ((size_t)zc * ny + j) * nx + i;
-    } else {
-        xp = (j < ny - 1) ? src[c + nz] : xc;
-        xm = (j > 0) ? src[c - nz] : xc;
-        t = ((size_t)zc * nx + i) * ny + j;
-    }
-    T a = __ldg(cpt + t) * (xp - xc) - __ldg(cmt + t) * (xc - xm);
-    tp[e] = fma((T)h, a, xc);
-}
+// 2. pipe columns
 
 // absolute temperature of a pipe value (theta + T_ref in the mixed path)
 template <typename T>
@@ -322,90 +292,102 @@ __device__ __forceinline__ double absT(T v, const double *Tref, int k) {
     return Tref ? (double)v + Tref[k] : (double)v;
 }
 
-// kernel_accumulate_outlet! (src/solver.jl:267-282) on the compact pipe
-// buffer: block (chunk, b) sums its share of the borehole's inner-pipe cells
-// with z <= v_inner * dt; k_outlet_fin adds the chunks in a fixed order.
-constexpr int kOutChunks = 64;
-
-__device__ __forceinline__ int outlet_levels(const double *__restrict__ gz, int nz, double zmax) {
-    int lo = 0, hi = nz;   // gz is sorted: the levels with gz <= zmax are a prefix
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (gz[mid] <= zmax) lo = mid + 1; else hi = mid;
-    }
-    return lo;
-}
+// Pipe pass in two launches before the advection: k_pipe_sweep applies the
+// explicit sweep to the pipe columns of one chunk (a run of at most kPipeChunk
+// columns of one borehole's inner pipe or annulus) for 128 levels, stores the
+// swept values and the chunk's column sum per level; k_pipe_reduce turns the
+// sums into the outlet mean (src/solver.jl:267-282, 257) and the per-level
+// annulus means (src/solver.jl:322-335).  Fixed summation order: the results
+// do not depend on scheduling.
+constexpr int kPipeChunk = 32;
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_outlet_part(double *__restrict__ part,
-                                                     const T *__restrict__ tp,
-                                                     const double *__restrict__ gz,
-                                                     const GwBhDev *__restrict__ bh,
-                                                     const double *__restrict__ Tref, int nz,
-                                                     double dt) {
-    const int ch = blockIdx.x, b = blockIdx.y;
-    const GwBhDev B = bh[b];
-    const int nlev = outlet_levels(gz, nz, B.v_inner * dt);
-    const long long tot = (long long)B.inner_count * nlev;
-    const long long per = (tot + kOutChunks - 1) / kOutChunks;
-    const long long e0 = ch * per, e1 = min(e0 + per, tot);
-    __shared__ double s_red[256];
+__global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *__restrict__ part,
+                                                    const T *__restrict__ src,
+                                                    const int4 *__restrict__ chunks,
+                                                    const int *__restrict__ pi,
+                                                    const int *__restrict__ pj,
+                                                    const int *__restrict__ zclass,
+                                                    const T *__restrict__ cmt,
+                                                    const T *__restrict__ cpt,
+                                                    const double *__restrict__ Tref, int nx, int ny,
+                                                    int nz, double h, int dir) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ch = blockIdx.y;
+    if (k >= nz) return;
+    const int4 C = chunks[ch];   // (borehole, first column, end column, outer?)
+    const int zc = zclass[k];
+    const T hh = (T)h;
     double acc = 0.0;
-    for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        int q = B.inner_begin + (int)(e / nlev);
-        int k = (int)(e % nlev);
-        acc += absT(tp[(size_t)q * nz + k], Tref, k);
+    for (int q = C.y; q < C.z; ++q) {
+        const int i = pi[q], j = pj[q];
+        const long long c = k + (long long)nz * (j + (long long)ny * i);
+        const T xc = src[c];
+        T xp, xm;
+        size_t t;
+        if (dir == GW_DIR_X) {
+            const long long st = (long long)nz * ny;
+            xp = (i < nx - 1) ? src[c + st] : xc;
+            xm = (i > 0) ? src[c - st] : xc;
+            t = ((size_t)zc * ny + j) * nx + i;
+        } else {
+            xp = (j < ny - 1) ? src[c + nz] : xc;
+            xm = (j > 0) ? src[c - nz] : xc;
+            t = ((size_t)zc * nx + i) * ny + j;
+        }
+        const T a = __ldg(cpt + t) * (xp - xc) - __ldg(cmt + t) * (xc - xm);
+        const T v = fma(hh, a, xc);
+        tp[(size_t)q * nz + k] = v;
+        acc += (double)v;
     }
+    // absolute temperature: add T_ref once per column summed
+    if (Tref) acc += (double)(C.z - C.y) * Tref[k];
+    part[(size_t)ch * nz + k] = acc;
+}
+
+// grid (ceil(nz / 128), nbh): annulus means per level; the first block of a
+// borehole also reduces its inner-pipe chunks over the outlet window.
+__global__ void __launch_bounds__(128) k_pipe_reduce(double *__restrict__ outlet,
+                                                     double *__restrict__ mean,
+                                                     const double *__restrict__ part,
+                                                     const int *__restrict__ bchunk,
+                                                     const double *__restrict__ gz,
+                                                     const GwBhDev *__restrict__ bh, int nz,
+                                                     double dt) {
+    const int b = blockIdx.y;
+    const GwBhDev B = bh[b];
+    // chunks of b: inner [bchunk[4b], bchunk[4b+1]), outer [bchunk[4b+2], bchunk[4b+3])
+    const int i0 = bchunk[4 * b], i1 = bchunk[4 * b + 1], o0 = bchunk[4 * b + 2], o1 = bchunk[4 * b + 3];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nz) {
+        double sacc = 0.0;
+        for (int ch = o0; ch < o1; ++ch) sacc += part[(size_t)ch * nz + k];
+        mean[(size_t)b * nz + k] = sacc / (double)B.outer_count;
+    }
+    if (blockIdx.x != 0) return;
+    __shared__ double s_red[128];
+    __shared__ int s_nlev;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = nz;   // gz sorted: the levels with gz <= v_inner dt are a prefix
+        const double zmax = B.v_inner * dt;
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (gz[mid] <= zmax) lo = mid + 1; else hi = mid;
+        }
+        s_nlev = lo;
+    }
+    __syncthreads();
+    const int nlev = s_nlev;
+    double acc = 0.0;
+    for (int kk = threadIdx.x; kk < nlev; kk += blockDim.x)
+        for (int ch = i0; ch < i1; ++ch) acc += part[(size_t)ch * nz + kk];
     s_red[threadIdx.x] = acc;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w) s_red[threadIdx.x] += s_red[threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) part[(size_t)b * kOutChunks + ch] = s_red[0];
-}
-
-// outlet[b] = sum / count (0/0 = NaN when the window is empty, as in the reference)
-__global__ void k_outlet_fin(double *__restrict__ outlet, const double *__restrict__ part,
-                             const double *__restrict__ gz, const GwBhDev *__restrict__ bh, int nbh,
-                             int nz, double dt) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nbh) return;
-    const GwBhDev B = bh[b];
-    const int nlev = outlet_levels(gz, nz, B.v_inner * dt);
-    double s = 0.0;
-    for (int ch = 0; ch < kOutChunks; ++ch) s += part[(size_t)b * kOutChunks + ch];
-    outlet[b] = s / (double)((long long)B.inner_count * nlev);
-}
-
-constexpr int kAnnChunks = 32;
-
-// annulus sums per (borehole, chunk of annulus columns, level)
-template <typename T>
-__global__ void __launch_bounds__(128) k_annulus_part(double *__restrict__ part, const T *__restrict__ tp,
-                                                      const GwBhDev *__restrict__ bh,
-                                                      const double *__restrict__ Tref, int nz) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int ch = blockIdx.y, b = blockIdx.z;
-    if (k >= nz) return;
-    const GwBhDev B = bh[b];
-    const int per = (B.outer_count + kAnnChunks - 1) / kAnnChunks;
-    const int q0 = B.outer_begin + ch * per;
-    const int q1 = min(q0 + per, B.outer_begin + B.outer_count);
-    double s = 0.0;
-    for (int q = q0; q < q1; ++q) s += absT(tp[(size_t)q * nz + k], Tref, k);
-    part[((size_t)b * kAnnChunks + ch) * nz + k] = s;
-}
-
-__global__ void __launch_bounds__(128) k_annulus_fin(double *__restrict__ mean,
-                                                     const double *__restrict__ part,
-                                                     const GwBhDev *__restrict__ bh, int nz) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int b = blockIdx.y;
-    if (k >= nz) return;
-    double s = 0.0;
-    for (int ch = 0; ch < kAnnChunks; ++ch) s += part[((size_t)b * kAnnChunks + ch) * nz + k];
-    mean[(size_t)b * nz + k] = s / (double)bh[b].outer_count;
+    if (threadIdx.x == 0) outlet[b] = s_red[0] / (double)((long long)B.inner_count * nlev);
 }
 
 // Departure table of kernel_advection! (src/solver.jl:285-360): for every
@@ -645,6 +627,18 @@ __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, con
     }
 }
 
+// mixed path field conversion: theta = T - T_ref(z) and back
+__global__ void k_to_theta(float *__restrict__ th, const double *__restrict__ T,
+                           const double *__restrict__ Tref, size_t n, int nz) {
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        th[q] = (float)(T[q] - Tref[q % nz]);
+}
+__global__ void k_from_theta(double *__restrict__ T, const float *__restrict__ th,
+                             const double *__restrict__ Tref, size_t n, int nz) {
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        T[q] = (double)th[q] + Tref[q % nz];
+}
+
 template <typename T>
 __global__ void k_finite(const T *__restrict__ u, size_t n, int *__restrict__ flag) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -732,30 +726,18 @@ template <typename T>
 int launch_pipe(gw_ctx *c, const T *src, int edir, double h) {
     Bufs<T> B = bufs<T>(c);
     const int ncol = c->n_inner + c->n_outer;
-    auto outlet = [&]() -> int {
-        k_outlet_part<T><<<dim3(kOutChunks, c->nbh), 256, 0, c->stream>>>(c->d_outpart, B.tp, c->d_gz,
-                                                                          c->d_bh, B.Tref, c->nz, h);
-        GW_CUDA(cudaGetLastError());
-        k_outlet_fin<<<grid_for(c->nbh, 128), 128, 0, c->stream>>>(c->d_outlet, c->d_outpart, c->d_gz,
-                                                                   c->d_bh, c->nbh, c->nz, h);
-        GW_CUDA(cudaGetLastError());
-        return GW_OK;
-    };
-    int rc;
-    if (ncol == 0) return outlet();
     const T *cm = edir == GW_DIR_X ? B.ct->cxm : B.ct->cym;
     const T *cp = edir == GW_DIR_X ? B.ct->cxp : B.ct->cyp;
-    long long n = (long long)ncol * c->nz;
-    k_pipe_explicit<T><<<grid_for(n, 256), 256, 0, c->stream>>>(B.tp, src, c->d_pipe_i, c->d_pipe_j,
-                                                                c->d_zclass, cm, cp, c->nx, c->ny,
-                                                                c->nz, ncol, h, edir);
-    GW_CUDA(cudaGetLastError());
-    if ((rc = outlet())) return rc;
-    dim3 gp(grid_for(c->nz, 128), kAnnChunks, c->nbh);
-    k_annulus_part<T><<<gp, 128, 0, c->stream>>>(c->d_annpart, B.tp, c->d_bh, B.Tref, c->nz);
-    GW_CUDA(cudaGetLastError());
-    dim3 gf(grid_for(c->nz, 128), c->nbh);
-    k_annulus_fin<<<gf, 128, 0, c->stream>>>(c->d_annmean, c->d_annpart, c->d_bh, c->nz);
+    if (c->n_pipe_chunks > 0) {
+        dim3 g(grid_for(c->nz, 128), c->n_pipe_chunks);
+        k_pipe_sweep<T><<<g, 128, 0, c->stream>>>(B.tp, c->d_pipepart, src, c->d_pipe_chunks,
+                                                  c->d_pipe_i, c->d_pipe_j, c->d_zclass, cm, cp,
+                                                  B.Tref, c->nx, c->ny, c->nz, h, edir);
+        GW_CUDA(cudaGetLastError());
+    }
+    dim3 gr(grid_for(c->nz, 128), c->nbh);
+    k_pipe_reduce<<<gr, 128, 0, c->stream>>>(c->d_outlet, c->d_annmean, c->d_pipepart, c->d_bchunk,
+                                             c->d_gz, c->d_bh, c->nz, h);
     GW_CUDA(cudaGetLastError());
     long long na = (long long)ncol * c->countz;
     if (na > 0) {
@@ -899,5 +881,25 @@ int gw_fused_check_finite(gw_ctx *c) {
     else
         k_finite<double><<<1216, 256, 0, c->stream>>>(c->d_u, n, c->d_flag);
     GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}
+
+int gw_fused_set_theta(gw_ctx *c, const double *T_host) {
+    const size_t n = (size_t)c->nx * c->ny * c->nz;
+    double *stage = reinterpret_cast<double *>(c->f_temp);   // f_temp and f_g1: 8 n bytes
+    GW_CUDA(cudaMemcpyAsync(stage, T_host, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    k_to_theta<<<1216, 256, 0, c->stream>>>(c->f_u, stage, c->d_Tref, n, c->nz);
+    GW_CUDA(cudaGetLastError());
+    GW_CUDA(cudaStreamSynchronize(c->stream));
+    return GW_OK;
+}
+
+int gw_fused_get_theta(gw_ctx *c, double *T_host) {
+    const size_t n = (size_t)c->nx * c->ny * c->nz;
+    double *stage = reinterpret_cast<double *>(c->f_temp);
+    k_from_theta<<<1216, 256, 0, c->stream>>>(stage, c->f_u, c->d_Tref, n, c->nz);
+    GW_CUDA(cudaGetLastError());
+    GW_CUDA(cudaMemcpyAsync(T_host, stage, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    GW_CUDA(cudaStreamSynchronize(c->stream));
     return GW_OK;
 }

@@ -13,5 +13,9 @@ int gw_fused_set_dt(gw_ctx *c, double dt);
 int gw_fused_step(gw_ctx *c, double dt, int s);
 // Enqueue one kernel class of the step (GW_KERNEL_*), for timing.
 int gw_fused_time_part(gw_ctx *c, double dt, int s, int part);
+// Mixed path: upload a double field as theta / download theta as a double
+// field (through the 8N-byte scratch f_temp..f_g1; T_ref must be current).
+int gw_fused_set_theta(gw_ctx *c, const double *T_host);
+int gw_fused_get_theta(gw_ctx *c, double *T_host);
 // Set c->d_flag if the state holds a NaN or Inf.
 int gw_fused_check_finite(gw_ctx *c);

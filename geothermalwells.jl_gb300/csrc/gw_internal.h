@@ -97,6 +97,10 @@ struct gw_ctx {
     int *d_pipe_ly = nullptr;         // [nx][ny] pipe index along y-lines (i, j), then [nx] line flags
     double *d_annpart = nullptr;      // [nbh][32][nz] partial annulus sums
     double *d_outpart = nullptr;      // [nbh][64] partial outlet sums
+    int4 *d_pipe_chunks = nullptr;    // pipe-column chunks: (borehole, q0, q1, outer)
+    int *d_bchunk = nullptr;          // [nbh][4]: chunk ranges (inner, outer) per borehole
+    double *d_pipepart = nullptr;     // [chunk][nz] column sums of the swept pipe values
+    int n_pipe_chunks = 0;
     GwAdvRec *d_advtab = nullptr;     // [nbh][countz][2] departure table for dt/2
     double *d_stage = nullptr;        // ROCK2 stage coefficients of the captured step
     float *f_stage = nullptr;         // the same, rounded to float (mixed path)
