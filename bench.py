@@ -43,6 +43,7 @@ def parse():
     p.add_argument("--cpu-sample-steps", type=int, default=1)
     p.add_argument("--accuracy", type=int, default=0, metavar="NSTEPS",
                    help="run FP64 and mixed for NSTEPS steps and report their differences")
+    p.add_argument("--dt", type=float, default=0.0, help="override the workload's step size [s]")
     return p.parse_args()
 
 
@@ -55,9 +56,12 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def workload(name):
+def workload(name, dt=0.0):
     from geothermalwells_gb300 import workloads as W
-    return W.single_well_large() if name == "large" else W.single_well_2mm()
+    w = W.single_well_large() if name == "large" else W.single_well_2mm()
+    if dt > 0:
+        w["dt"] = float(dt)
+    return w
 
 
 class Clocks:
@@ -142,7 +146,7 @@ def run_reference(args):
     rank, world, local, dist = dist_init(args)
     if rank != 0:
         return
-    w = workload(args.workload)
+    w = workload(args.workload, args.dt)
     steps = max(1, min(args.steps, 2))
     cb = cpu_baseline(w, steps)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": METRIC,
@@ -160,7 +164,7 @@ def run_ours(args):
     rank, world, local, dist = dist_init(args)
     from geothermalwells_gb300 import _lib, create_cache, GB300
     L = _lib.load()
-    w = workload(args.workload)
+    w = workload(args.workload, args.dt)
     cache = create_cache(backend=GB300(device=local, precision=args.precision), gridx=w["gridx"],
                          gridy=w["gridy"], gridz=w["gridz"], materials=w["materials"],
                          boreholes=w["boreholes"], inlet_model=w["inlet_model"])
@@ -269,7 +273,7 @@ def run_accuracy(args):
     the relative difference of the extracted heat."""
     from geothermalwells_gb300 import (GB300, ODEProblem, ROCK2, create_cache, eigen_estimator,
                                        rhs_diffusion_z, solve)
-    w = workload(args.workload)
+    w = workload(args.workload, args.dt)
     res = {}
     for prec in ("fp64", "mixed"):
         cache = create_cache(backend=GB300(precision=prec), gridx=w["gridx"], gridy=w["gridy"],
