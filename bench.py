@@ -38,7 +38,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    p.add_argument("--workload", default="large", choices=["large", "2mm"])
+    p.add_argument("--workload", default="large", choices=["large", "2mm", "thomas"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-steps", type=int, default=1)
     p.add_argument("--accuracy", type=int, default=0, metavar="NSTEPS",
@@ -298,8 +298,67 @@ def run_accuracy(args):
     print(json.dumps(line), flush=True)
 
 
+def run_thomas(args):
+    """Batched tridiagonal microbenchmark: 262,144 seeded systems, lengths
+    U[32, 1024]; algorithmic traffic 5 words per unknown (a, b, c, d in, x
+    out).  Inputs (5.5 GB) exceed L2."""
+    import torch
+    from geothermalwells_gb300 import _lib
+    from geothermalwells_gb300 import workloads as W
+    L = _lib.load()
+    w = W.tridiagonal_batch()
+    prec = _lib.GW_PREC_MIXED if args.precision == "mixed" else _lib.GW_PREC_FP64
+    dev = {k: torch.from_numpy(np.ascontiguousarray(w[k])).cuda() for k in "abcd"}
+    goff = torch.from_numpy(w["group_off"].astype(np.int64)).cuda()
+    glen = torch.from_numpy(w["group_len"].astype(np.int32)).cuda()
+    x = torch.zeros(w["n"], dtype=torch.float64, device="cuda")
+    scratch = torch.zeros((w["n"] * 12 + 7) // 8, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def solve():
+        _lib.check(L.gw_tridiag_batch(prec, w["ngroups"], goff.data_ptr(), glen.data_ptr(),
+                                      dev["a"].data_ptr(), dev["b"].data_ptr(), dev["c"].data_ptr(),
+                                      dev["d"].data_ptr(), x.data_ptr(), scratch.data_ptr(), w["n"],
+                                      stream.cuda_stream))
+    for _ in range(args.warmup):
+        solve()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        solve()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    # residuals in double on the device: r = d - (a x_{r-1} + b x_r + c x_{r+1})
+    r = dev["d"] - (dev["a"] * torch.roll(x, 32) + dev["b"] * x + dev["c"] * torch.roll(x, -32))
+    res = float(r.abs().max() / dev["d"].abs().max())
+    unknowns = w["unknowns"]
+    alg = 5 * 8 * unknowns
+    peak, peak_kind = peaks()
+    achieved = alg / (ms / 1e3) / 1e9
+    line = {"metric": "Munknowns/s", "value": unknowns / (ms / 1e3) / 1e6, "unit": "Munknowns/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == _lib.GW_PREC_FP64 else "f32+f64refine", "data": "synthetic",
+            "config": {"workload": w["name"], "systems": 262144, "unknowns": unknowns,
+                       "stored_rows_x32": w["n"], "l2": "inputs larger than L2 (5.5 GB)"},
+            "residual_max_rel": res,
+            "roofline": {"kernel": "k_tri_f64" if prec == _lib.GW_PREC_FP64 else "k_tri_mix1+2",
+                         "bound": "hbm", "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "alg_bytes_per_launch": alg},
+            "gpu_launches": args.steps * (1 if prec == _lib.GW_PREC_FP64 else 2), "clocks": ck}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "thomas":
+        run_thomas(args)
+        return
     if args.accuracy:
         run_accuracy(args)
         return

@@ -77,6 +77,7 @@ SIGNATURES = {
     "gw_get_last_step_time": (_i, [_vp, _dp]),
     "gw_profile_kernels": (_i, [_vp, _d, _i, _dp]),
     "gw_advection_noalloc": (_i, [_vp, _vp, _d, _d, _vp]),
+    "gw_tridiag_batch": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_longlong, _vp]),
 }
 KERNELS = ("rock2_columns", "half_step_x", "half_step_y", "pipe")
 

@@ -122,3 +122,41 @@ def small_case(n_layers=1, inlet="constant", nbh=1, nz_cells=12, spacing=0.6, h=
     im = ConstantInlet(10.0) if inlet == "constant" else HeatExchangerInlet(3.0)
     return dict(name="small", gridx=gx, gridy=gy, gridz=gz, boreholes=bhs, materials=mat,
                 inlet_model=im, T0=T0, dt=float(dt), nsteps=6, t0=0.0)
+
+
+def tridiagonal_batch(nsys=262144, lmin=32, lmax=1024, seed=20261203):
+    """Batched Thomas microbenchmark: nsys independent systems with lengths
+    uniform in [lmin, lmax]; a_i, c_i ~ -U(0.1, 1), b_i = 1 + |a_i| + |c_i| +
+    U(0, 2) (strictly diagonally dominant, like the ADI implicit step),
+    d_i ~ U(0, 100); seeded.  Returned in the grouped interleaved layout of
+    gw_tridiag_batch: systems sorted by length (longest first) in groups of
+    32, row r of lane l of group g at group_off[g] + 32 r + l, identity rows
+    as padding, a_0 = c_{len-1} = 0.  Also returns the true lengths per slot
+    and the permutation (slot -> original system index)."""
+    rng = np.random.default_rng(seed)
+    lengths = rng.integers(lmin, lmax + 1, size=nsys)
+    ngroups = (nsys + 31) // 32
+    order = np.argsort(-lengths, kind="stable")
+    slot_len = np.zeros(ngroups * 32, dtype=np.int64)
+    slot_len[:nsys] = lengths[order]
+    glen = slot_len.reshape(ngroups, 32).max(axis=1)
+    goff = np.zeros(ngroups + 1, dtype=np.int64)
+    goff[1:] = np.cumsum(glen * 32)
+    n = int(goff[-1])
+    a = -rng.uniform(0.1, 1.0, n)
+    c = -rng.uniform(0.1, 1.0, n)
+    b = 1.0 + np.abs(a) + np.abs(c) + rng.uniform(0.0, 2.0, n)
+    d = rng.uniform(0.0, 100.0, n)
+    for g in range(ngroups):
+        sl = slice(goff[g], goff[g + 1])
+        lens = slot_len[32 * g:32 * g + 32]
+        rows = np.arange(glen[g])[:, None]
+        pad = rows >= lens[None, :]
+        last = rows == (lens[None, :] - 1)
+        ag, bg, cg, dg = (v[sl].reshape(glen[g], 32) for v in (a, b, c, d))
+        ag[pad] = 0.0; cg[pad] = 0.0; bg[pad] = 1.0; dg[pad] = 0.0
+        ag[0, :] = 0.0
+        cg[last] = 0.0
+    return dict(name="tridiagonal_batch_%d_len%d-%d" % (nsys, lmin, lmax), a=a, b=b, c=c, d=d,
+                group_off=goff[:-1].copy(), group_len=glen.astype(np.int32), n=n,
+                ngroups=ngroups, unknowns=int(lengths.sum()), slot_len=slot_len, order=order)

@@ -153,6 +153,20 @@ int gw_get_last_step_time(gw_ctx *ctx, double *ms);
 #define GW_KERNEL_COUNT 4
 int gw_profile_kernels(gw_ctx *ctx, double dt, int reps, double *ms_out);
 
+/* Batched independent tridiagonal solves A_s x_s = d_s (the elimination of
+ * thomas_I_minus_A!, src/solver.jl:207-218, on arbitrary systems), all
+ * arrays on the device in the grouped interleaved layout: systems sorted by
+ * length in groups of 32; row r of the group's lane l at
+ * group_off[g] + 32 r + l; group_len[g] rows per group (shorter systems
+ * padded with identity rows, a_0 = 0 and c_{len-1} = 0).  n_elements = total
+ * stored rows * 32.  precision GW_PREC_FP64: double elimination, scratch of
+ * 8 * n_elements bytes; GW_PREC_MIXED: float elimination plus one residual
+ * correction (residual in double), scratch of 12 * n_elements bytes.  stream
+ * is a cudaStream_t (NULL: the default stream); returns when done. */
+int gw_tridiag_batch(int precision, int ngroups, const long long *group_off, const int *group_len,
+                     const double *a, const double *b, const double *c, const double *d,
+                     double *x, void *scratch, long long n_elements, void *stream);
+
 /* advection! (same result as gw_advection) for callers that must not make
  * the library allocate device memory.  No counterpart in the reference.
  *

@@ -491,3 +491,38 @@ int ogw_set_threads(int n) {
     return 1;
 #endif
 }
+
+/* Batched independent tridiagonal systems in the grouped interleaved layout
+ * (row r of lane l of group g at goff[g] + 32 r + l; glen[g] rows), solved
+ * one by one with the elimination of thomas_I_minus_A! (solver.jl:207-218):
+ * w = lower/diag; diag -= w upper; rhs -= w rhs_prev; then back substitution
+ * x_l = (rhs_l - upper_l x_{l+1}) / diag_l.  The sub-diagonal entry of row r
+ * is a[r], the super-diagonal c[r]. */
+void ogw_tridiag_batch(int ngroups, const long long *goff, const int *glen, const double *a,
+                       const double *b, const double *c, const double *d, double *x) {
+#pragma omp parallel
+    {
+        int cap = 0;
+        double *dg = NULL, *rh = NULL;
+#pragma omp for schedule(dynamic, 4)
+        for (long long s = 0; s < 32LL * ngroups; ++s) {
+            long long g = s / 32, l = s % 32;
+            int L = glen[g];
+            if (L > cap) { cap = L; dg = (double *)realloc(dg, sizeof(double) * cap); rh = (double *)realloc(rh, sizeof(double) * cap); }
+            long long o = goff[g] + l;
+            for (int r = 0; r < L; ++r) { dg[r] = b[o + 32LL * r]; rh[r] = d[o + 32LL * r]; }
+            for (int r = 1; r < L; ++r) {
+                double w = a[o + 32LL * r] / dg[r - 1];
+                dg[r] = fma(-w, c[o + 32LL * (r - 1)], dg[r]);
+                rh[r] = fma(-w, rh[r - 1], rh[r]);
+            }
+            double xn = rh[L - 1] / dg[L - 1];
+            x[o + 32LL * (L - 1)] = xn;
+            for (int r = L - 2; r >= 0; --r) {
+                xn = fma(-c[o + 32LL * r], xn, rh[r]) / dg[r];
+                x[o + 32LL * r] = xn;
+            }
+        }
+        free(dg); free(rh);
+    }
+}

@@ -51,6 +51,8 @@ def lib():
                                      ctypes.c_double, ctypes.c_double, _dp]
         L.ogw_get_outlet.argtypes = [ctypes.c_void_p, _dp]
         L.ogw_initial_condition.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double]
+        _lp = ctypes.POINTER(ctypes.c_longlong)
+        L.ogw_tridiag_batch.argtypes = [ctypes.c_int, _lp, _ip, _dp, _dp, _dp, _dp, _dp]
         L.ogw_set_threads.restype = ctypes.c_int
         L.ogw_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -179,3 +181,24 @@ class Oracle:
 
 def set_threads(n):
     return lib().ogw_set_threads(int(n))
+
+
+def tridiag_batch(w):
+    """Solve a batch from workloads.tridiagonal_batch on the CPU (FP64)."""
+    L = lib()
+    goff = np.ascontiguousarray(w["group_off"], dtype=np.int64)
+    glen = np.ascontiguousarray(w["group_len"], dtype=np.int32)
+    x = np.zeros(w["n"])
+    arr = [np.ascontiguousarray(w[k], dtype=np.float64) for k in "abcd"]
+    L.ogw_tridiag_batch(w["ngroups"], goff.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                        glen.ctypes.data_as(_ip), *[_p(v) for v in arr], _p(x))
+    return x
+
+
+def tridiag_residual(w, x):
+    """max |d - A x| / max |d| in the grouped interleaved layout."""
+    a, b, c, d = (w[k] for k in "abcd")
+    xm = np.roll(x, 32)
+    xp = np.roll(x, -32)
+    r = d - (a * xm + b * x + c * xp)
+    return float(np.max(np.abs(r)) / np.max(np.abs(d)))
