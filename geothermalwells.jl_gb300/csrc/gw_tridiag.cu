@@ -19,18 +19,6 @@
 
 namespace {
 
-// 1/x in double from a float seed refined by two Newton-Raphson steps
-// (e = 1 - x r, r <- r + r e; each step doubles the correct bits: 24 -> 48
-// -> 96), four double operations instead of a full IEEE division.  Valid
-// for the normal, non-tiny pivots of diagonally dominant systems.
-__device__ __forceinline__ double rcp_nr(double x) {
-    double r = (double)__frcp_rn((float)x);
-    double e = fma(-x, r, 1.0);
-    r = fma(r, e, r);
-    e = fma(-x, r, 1.0);
-    return fma(r, e, r);
-}
-
 __global__ void __launch_bounds__(128) k_tri_f64(const double *__restrict__ a, const double *__restrict__ b,
                                                  const double *__restrict__ c, const double *__restrict__ d,
                                                  double *__restrict__ x, double *__restrict__ cs,
@@ -45,7 +33,7 @@ __global__ void __launch_bounds__(128) k_tri_f64(const double *__restrict__ a, c
     for (int r = 0; r < L; ++r) {
         const long long e = o + 32LL * r;
         const double ar = a[e];
-        const double rden = rcp_nr(fma(-ar, cp, b[e]));
+        const double rden = 1.0 / fma(-ar, cp, b[e]);
         cp = c[e] * rden;
         dp = fma(-ar, dp, d[e]) * rden;
         cs[e] = cp;
