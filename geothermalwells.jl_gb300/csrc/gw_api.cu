@@ -186,6 +186,34 @@ int gw_ensure_factors(gw_ctx *c, double h) {
     return GW_OK;
 }
 
+// Everything a step of size dt with s stages needs before its graph runs:
+// the outlet-series capacity, the step counter, the Thomas factors, and for
+// the fused step the stage and advection tables.
+int gw_prepare_step(gw_ctx *c, double dt, int s, int nsteps) {
+    int rc;
+    if (nsteps > c->series_cap) {
+        GW_CUDA(cudaStreamSynchronize(c->stream));
+        if (c->d_series) {
+            cudaFree(c->d_series);
+            for (auto &p : c->allocations) if (p == c->d_series) p = nullptr;
+            c->d_series = nullptr;
+        }
+        if ((rc = dalloc(c, &c->d_series, (size_t)nsteps * c->nbh))) return rc;
+        c->series_cap = nsteps;
+        ++c->series_gen;
+    }
+    GW_CUDA(cudaMemsetAsync(c->d_step_counter, 0, sizeof(int), c->stream));
+    c->last_nsteps = nsteps;
+    if (nsteps == 0) return GW_OK;
+    if ((rc = gw_ensure_factors(c, dt / 2))) return rc;
+    if (c->fused && (c->tables_dt != dt || c->tables_s != s)) {
+        if ((rc = upload_stages(c, dt, s)) || (rc = gw_fused_set_dt(c, dt))) return rc;
+        c->tables_dt = dt;
+        c->tables_s = s;
+    }
+    return GW_OK;
+}
+
 extern "C" {
 
 const char *gw_last_error(void) { return g_err.c_str(); }
@@ -360,7 +388,7 @@ int gw_set_field(gw_ctx *c, const double *T) {
     if (rc) return rc;
     if (mixed(c)) {
         if ((rc = set_reference_profile(c, T))) return rc;
-        c->graph_dt = -1.0;   // the advection table depends on T_ref
+        c->tables_dt = -1.0;   // the advection table depends on T_ref
         return gw_fused_set_theta(c, T);
     }
     GW_CUDA(cudaMemcpyAsync(c->d_u, T, ncell(c) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -457,24 +485,10 @@ int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
     if (rc) return rc;
     int s, covered;
     if ((rc = gw_rock2_choose(dt, c->eigen_estimate, max_stages, &s, &covered))) return rc;
-    if (nsteps > c->series_cap) {
-        if (c->d_series) {
-            GW_CUDA(cudaStreamSynchronize(c->stream));
-            cudaFree(c->d_series);
-            for (auto &p : c->allocations) if (p == c->d_series) p = nullptr;
-            c->d_series = nullptr;
-        }
-        if ((rc = dalloc(c, &c->d_series, (size_t)nsteps * c->nbh))) return rc;
-        c->series_cap = nsteps;
-        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
-    }
-    GW_CUDA(cudaMemsetAsync(c->d_step_counter, 0, sizeof(int), c->stream));
-    c->last_nsteps = nsteps;
+    if ((rc = gw_prepare_step(c, dt, s, nsteps))) return rc;
     if (nsteps == 0) return sync(c);
-    if ((rc = gw_ensure_factors(c, dt / 2))) return rc;
-    if (!c->graph || c->graph_dt != dt || c->graph_s != s) {
+    if (!c->graph || c->graph_dt != dt || c->graph_s != s || c->graph_gen != c->series_gen) {
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
-        if (c->fused && ((rc = upload_stages(c, dt, s)) || (rc = gw_fused_set_dt(c, dt)))) return rc;
         cudaGraph_t g;
         GW_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         int r3;
@@ -493,6 +507,7 @@ int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
         if (e != cudaSuccess) return gw_cuda_fail(e, "cudaGraphInstantiate");
         c->graph_dt = dt;
         c->graph_s = s;
+        c->graph_gen = c->series_gen;
     }
     GW_CUDA(cudaEventRecord(c->ev0, c->stream));
     for (int n = 0; n < nsteps; ++n) GW_CUDA(cudaGraphLaunch(c->graph, c->stream));
@@ -519,7 +534,8 @@ int gw_profile_kernels(gw_ctx *c, double dt, int reps, double *ms_out) {
     int s, covered;
     if ((rc = gw_rock2_choose(dt, c->eigen_estimate, 100, &s, &covered))) return rc;
     if ((rc = upload_stages(c, dt, s)) || (rc = gw_fused_set_dt(c, dt))) return rc;
-    c->graph_dt = -1.0;   // the tables may differ from the captured step's
+    c->tables_dt = dt;
+    c->tables_s = s;
     const size_t N = ncell(c);
     void *u = mixed(c) ? (void *)c->f_u : (void *)c->d_u;
     void *bak = mixed(c) ? (void *)c->f_g1 : (void *)c->d_g1;

@@ -1,0 +1,186 @@
+// gw_batch.cu -- ensembles of well designs advanced together.
+//
+// A batch holds the contexts of many designs (each built by gw_create with
+// its own grids, materials and boreholes).  One ensemble step is captured as
+// a single CUDA graph: a fork from the batch's stream into every design's
+// stream, that design's fused step (gw_fused.cu), and a join back -- so all
+// designs advance with one graph launch per step and the designs' kernels
+// run concurrently, which fills the GPU even for the small designs.
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "gw_fused.h"
+#include "gw_internal.h"
+
+struct gw_batch {
+    std::vector<gw_ctx *> ctx;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaGraphExec_t graph = nullptr;
+    double graph_dt = -1.0;
+    int graph_steps_cap = -1;
+    std::vector<int> graph_s;
+    std::vector<int> graph_gen;   // each context's series_gen at capture
+    double last_ms = 0.0;
+};
+
+namespace {
+int prepare(gw_ctx *c, double dt, int max_stages, int nsteps, int *s_out) {
+    int s, covered, rc;
+    if ((rc = gw_rock2_choose(dt, c->eigen_estimate, max_stages, &s, &covered))) return rc;
+    if ((rc = gw_prepare_step(c, dt, s, nsteps))) return rc;
+    *s_out = s;
+    return GW_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int gw_batch_create(gw_ctx *const *ctxs, int n, gw_batch **out) {
+    if (!out || !ctxs || n < 1) return gw_fail(GW_ERR_ARG, "need at least one context");
+    *out = nullptr;
+    gw_batch *b = new gw_batch();
+    b->device = ctxs[0]->device;
+    for (int d = 0; d < n; ++d) {
+        gw_ctx *c = ctxs[d];
+        if (!c) { delete b; return gw_fail(GW_ERR_ARG, "NULL context in batch"); }
+        if (c->device != b->device) { delete b; return gw_fail(GW_ERR_ARG, "all contexts must use one device"); }
+        if (!c->fused) { delete b; return gw_fail(GW_ERR_UNSUPPORTED, "a context runs the modular step"); }
+        b->ctx.push_back(c);
+    }
+    cudaError_t e;
+    auto fail = [&](cudaError_t err, const char *what) { gw_batch_destroy(b); return gw_cuda_fail(err, what); };
+    if ((e = cudaSetDevice(b->device)) != cudaSuccess) return fail(e, "cudaSetDevice");
+    if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "cudaStreamCreate");
+    if ((e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreate(&b->ev0)) != cudaSuccess || (e = cudaEventCreate(&b->ev1)) != cudaSuccess)
+        return fail(e, "cudaEventCreate");
+    b->join.assign(n, nullptr);
+    for (int d = 0; d < n; ++d)
+        if ((e = cudaEventCreateWithFlags(&b->join[d], cudaEventDisableTiming)) != cudaSuccess)
+            return fail(e, "cudaEventCreate");
+    *out = b;
+    return GW_OK;
+}
+
+int gw_batch_destroy(gw_batch *b) {
+    if (!b) return GW_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (cudaEvent_t ev : b->join) if (ev) cudaEventDestroy(ev);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return GW_OK;
+}
+
+int gw_batch_set_tiling(gw_batch *b, int tiling) {
+    if (!b) return gw_fail(GW_ERR_ARG, "NULL batch");
+    if (tiling < 0 || tiling >= GW_TILINGS) return gw_fail(GW_ERR_ARG, "tiling out of range");
+    for (gw_ctx *c : b->ctx) { c->half_cfg = tiling; c->graph_dt = -1.0; }
+    b->graph_dt = -1.0;
+    return GW_OK;
+}
+
+// For every design, time each half-step tiling (x- and y-lines, `reps`
+// launches each, CUDA events on the design's stream) and keep the fastest.
+int gw_batch_autotune(gw_batch *b, double dt, int reps, int *tiling_out) {
+    if (!b || !(dt > 0) || reps < 1) return gw_fail(GW_ERR_ARG, "bad arguments");
+    int rc;
+    GW_CUDA(cudaSetDevice(b->device));
+    for (size_t d = 0; d < b->ctx.size(); ++d) {
+        gw_ctx *c = b->ctx[d];
+        int s;
+        if ((rc = prepare(c, dt, 100, 1, &s))) return rc;
+        float best = 1e30f;
+        int arg = 0;
+        for (int t = 0; t < GW_TILINGS; ++t) {
+            c->half_cfg = t;
+            // one untimed launch of each, then `reps` timed
+            if ((rc = gw_fused_time_part(c, dt, s, GW_KERNEL_HALF_X)) ||
+                (rc = gw_fused_time_part(c, dt, s, GW_KERNEL_HALF_Y)))
+                return rc;
+            GW_CUDA(cudaEventRecord(c->ev0, c->stream));
+            for (int r = 0; r < reps; ++r)
+                if ((rc = gw_fused_time_part(c, dt, s, GW_KERNEL_HALF_X)) ||
+                    (rc = gw_fused_time_part(c, dt, s, GW_KERNEL_HALF_Y)))
+                    return rc;
+            GW_CUDA(cudaEventRecord(c->ev1, c->stream));
+            GW_CUDA(cudaEventSynchronize(c->ev1));
+            float ms = 0.f;
+            GW_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+            if (ms < best) { best = ms; arg = t; }
+        }
+        c->half_cfg = arg;
+        c->graph_dt = -1.0;
+        if (tiling_out) tiling_out[d] = arg;
+    }
+    b->graph_dt = -1.0;
+    return GW_OK;
+}
+
+int gw_batch_step(gw_batch *b, double dt, int nsteps, int max_stages) {
+    if (!b) return gw_fail(GW_ERR_ARG, "NULL batch");
+    if (nsteps < 0 || !(dt > 0)) return gw_fail(GW_ERR_ARG, "nsteps >= 0 and dt > 0 required");
+    GW_CUDA(cudaSetDevice(b->device));
+    const int n = (int)b->ctx.size();
+    std::vector<int> s(n);
+    int rc;
+    for (int d = 0; d < n; ++d)
+        if ((rc = prepare(b->ctx[d], dt, max_stages, nsteps, &s[d]))) return rc;
+    if (nsteps == 0) return GW_OK;
+    std::vector<int> gen(n);
+    for (int d = 0; d < n; ++d) gen[d] = b->ctx[d]->series_gen;
+    if (!b->graph || b->graph_dt != dt || b->graph_s != s || b->graph_gen != gen ||
+        b->graph_steps_cap < nsteps) {
+        if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+        cudaGraph_t g;
+        GW_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        int r = GW_OK;
+        cudaError_t e = cudaEventRecord(b->fork, b->stream);
+        for (int d = 0; d < n && e == cudaSuccess && r == GW_OK; ++d) {
+            gw_ctx *c = b->ctx[d];
+            if ((e = cudaStreamWaitEvent(c->stream, b->fork, 0)) != cudaSuccess) break;
+            if ((r = gw_fused_step(c, dt, s[d]))) break;
+            if ((e = cudaEventRecord(b->join[d], c->stream)) != cudaSuccess) break;
+            e = cudaStreamWaitEvent(b->stream, b->join[d], 0);
+        }
+        cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
+        if (r != GW_OK || e != cudaSuccess || ee != cudaSuccess) {
+            if (ee == cudaSuccess) cudaGraphDestroy(g);
+            if (r != GW_OK) return r;
+            return gw_cuda_fail(e != cudaSuccess ? e : ee, "ensemble step capture");
+        }
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return gw_cuda_fail(e, "cudaGraphInstantiate");
+        b->graph_dt = dt;
+        b->graph_s = s;
+        b->graph_gen = gen;
+        b->graph_steps_cap = nsteps;
+    }
+    for (gw_ctx *c : b->ctx) GW_CUDA(cudaStreamSynchronize(c->stream));
+    GW_CUDA(cudaEventRecord(b->ev0, b->stream));
+    for (int k = 0; k < nsteps; ++k) GW_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    GW_CUDA(cudaEventRecord(b->ev1, b->stream));
+    GW_CUDA(cudaStreamSynchronize(b->stream));
+    float ms = 0.f;
+    GW_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    b->last_ms = ms;
+    for (gw_ctx *c : b->ctx) c->last_nsteps = nsteps;
+    return GW_OK;
+}
+
+int gw_batch_get_last_step_time(gw_batch *b, double *ms) {
+    if (!b || !ms) return gw_fail(GW_ERR_ARG, "NULL argument");
+    *ms = b->last_ms;
+    return GW_OK;
+}
+
+}  // extern "C"

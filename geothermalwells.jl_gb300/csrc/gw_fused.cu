@@ -487,15 +487,18 @@ __global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *_
 //    + Thomas along the line direction.  XL: x-lines (explicit y), else
 //    y-lines (explicit x).
 //
-// A block owns 32 consecutive levels (one per lane) of kHW neighbouring lines
-// (one warp each).  Rows are streamed in chunks of kHR: the block copies the
+// A block owns 32 consecutive levels (one per lane) of HW neighbouring lines
+// (one warp each).  Rows are streamed in chunks of HR: the block copies the
 // chunk's rows of its kHW lines plus the two neighbouring lines (which the
 // explicit sweep needs) into shared memory with cp.async, double-buffered so
 // the next chunk is in flight while the current one is eliminated.  The
 // forward sweep stores y_l in dst; the backward sweep reads it back in
 // batches loaded ahead of their use and overwrites it with x_l.
-constexpr int kHW = 8;    // lines (warps) per block
-constexpr int kHR = 16;   // rows per chunk (a multiple of kHG)
+// Tilings (lines per block HW, rows per chunk HR); the autotuner picks one
+// per context, the default is the first.
+constexpr int kTilings = 6;
+constexpr int kTileHW[kTilings] = {8, 4, 8, 4, 2, 8};
+constexpr int kTileHR[kTilings] = {16, 16, 8, 32, 16, 32};
 constexpr int kHG = 4;    // rows whose coefficients are loaded together
 constexpr int kHB = 8;    // rows per backward batch
 
@@ -505,8 +508,8 @@ struct alignas(4 * sizeof(T)) Quad {
     T x, y, z, w;
 };
 
-template <typename T, bool XL>
-__global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, const T *__restrict__ src,
+template <typename T, bool XL, int HW, int HR>
+__global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, const T *__restrict__ src,
                                                         const T *__restrict__ pp,
                                                         const int *__restrict__ pipe_line,
                                                         const int *__restrict__ zclass,
@@ -515,13 +518,13 @@ __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, con
                                                         const T *__restrict__ fcu, int nx, int ny,
                                                         int nz, int countz) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *tile = reinterpret_cast<T *>(smem_raw);   // [2][kHR][kHW + 2][32]
-    constexpr int kRow = (kHW + 2) * 32;
-    constexpr int kTile = kHR * kRow;
+    T *tile = reinterpret_cast<T *>(smem_raw);   // [2][HR][HW + 2][32]
+    constexpr int kRow = (HW + 2) * 32;
+    constexpr int kTile = HR * kRow;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nl = XL ? ny : nx;   // lines per level
     const int N = XL ? nx : ny;    // line length
-    const int k0 = blockIdx.x * 32, m0 = blockIdx.y * kHW;
+    const int k0 = blockIdx.x * 32, m0 = blockIdx.y * HW;
     const int k = k0 + lane, m = m0 + warp;
     const bool kok = k < nz;
     const bool active = kok && m < nl;
@@ -535,21 +538,21 @@ __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, con
     const bool pipe_levels = k < countz && __ldg(pipe_line + (size_t)nl * N + mc) != 0;
     const Quad<T> *hql = hq + fb;
     T *dl = dst + k + m * mst;   // row 0 of this thread's line
-    const int nchunk = (N + kHR - 1) / kHR;
+    const int nchunk = (N + HR - 1) / HR;
 
-    // this warp copies neighbour-line slots mm = warp and warp + kHW of each row
+    // this warp copies neighbour-line slots mm = warp and warp + HW of each row
     auto load_chunk = [&](int ch, int buf) {
         T *t = tile + buf * kTile;
-        const int l0 = ch * kHR;
+        const int l0 = ch * HR;
 #pragma unroll
         for (int rep = 0; rep < 2; ++rep) {
-            const int mm = warp + rep * kHW;
-            if (mm >= kHW + 2) break;
+            const int mm = warp + rep * HW;
+            if (mm >= HW + 2) break;
             const int gm = m0 - 1 + mm;
             const bool lok = kok && gm >= 0 && gm < nl;
             const T *g = src + k + (long long)gm * mst + (long long)l0 * rst;
             T *d = t + mm * 32 + lane;
-            for (int r = 0; r < kHR; ++r) {
+            for (int r = 0; r < HR; ++r) {
                 const bool ok = lok && l0 + r < N;
                 cp_async<sizeof(T)>(d + r * kRow, ok ? (const void *)(g + (long long)r * rst) : (const void *)src, ok);
             }
@@ -568,7 +571,7 @@ __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, con
         }
         __syncthreads();
         const T *row = tile + (ch & 1) * kTile + warp * 32 + lane;
-        const int rmax = min(kHR, N - ch * kHR);
+        const int rmax = min(HR, N - ch * HR);
         for (int r0 = 0; r0 < rmax; r0 += kHG) {
             // the group's loads are issued before its dependent updates
             Quad<T> q[kHG];
@@ -577,19 +580,19 @@ __global__ void __launch_bounds__(32 * kHW) k_half_tile(T *__restrict__ dst, con
 #pragma unroll
             for (int g = 0; g < kHG; ++g) {
                 const int r = min(r0 + g, rmax - 1);
-                const int l = ch * kHR + r;
+                const int l = ch * HR + r;
                 q[g] = hql[l];
                 pq[g] = pipe_levels ? __ldg(pline + l) : -1;
                 const T *rw = row + r * kRow;
                 xm[g] = rw[0]; xc[g] = rw[32]; xp[g] = rw[64];
             }
-            T *dr = dl + (long long)(ch * kHR + r0) * rst;
+            T *dr = dl + (long long)(ch * HR + r0) * rst;
 #pragma unroll
             for (int g = 0; g < kHG; ++g) {
                 if (r0 + g >= rmax) break;
                 const T ay = q[g].w * y;
                 T yn = fma(q[g].x, xc[g], fma(q[g].y, xp[g], fma(q[g].z, xm[g], -ay)));
-                if (pq[g] >= 0) yn = fma(pp[(size_t)pq[g] * countz + k], __ldg(fib + fb + ch * kHR + r0 + g), -ay);
+                if (pq[g] >= 0) yn = fma(pp[(size_t)pq[g] * countz + k], __ldg(fib + fb + ch * HR + r0 + g), -ay);
                 y = yn;
                 if (active) *dr = y;
                 dr += rst;
@@ -750,7 +753,20 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h) {
 }
 
 template <typename T>
-size_t half_smem() { return 2 * (size_t)kHR * (kHW + 2) * 32 * sizeof(T); }
+size_t half_smem(int cfg) { return 2 * (size_t)kTileHR[cfg] * (kTileHW[cfg] + 2) * 32 * sizeof(T); }
+
+template <typename T, int HW, int HR>
+void half_launch(gw_ctx *c, T *dst, const T *src, int xlines, const Quad<T> *hq, const GwFactors<T> &f,
+                 const T *pp, size_t smem) {
+    const int nl = xlines ? c->ny : c->nx;
+    dim3 grid((c->nz + 31) / 32, (nl + HW - 1) / HW);
+    if (xlines)
+        k_half_tile<T, true, HW, HR><<<grid, 32 * HW, smem, c->stream>>>(
+            dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
+    else
+        k_half_tile<T, false, HW, HR><<<grid, 32 * HW, smem, c->stream>>>(
+            dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
+}
 
 template <typename T>
 int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h) {
@@ -758,16 +774,36 @@ int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h) {
     Bufs<T> B = bufs<T>(c);
     const GwFactors<T> &f = xlines ? B.ct->fx : B.ct->fy;
     const Quad<T> *hq = reinterpret_cast<const Quad<T> *>(xlines ? B.ct->hx : B.ct->hy);
-    const int nl = xlines ? c->ny : c->nx;
-    dim3 grid((c->nz + 31) / 32, (nl + kHW - 1) / kHW);
-    if (xlines)
-        k_half_tile<T, true><<<grid, 32 * kHW, half_smem<T>(), c->stream>>>(
-            dst, src, B.pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
-    else
-        k_half_tile<T, false><<<grid, 32 * kHW, half_smem<T>(), c->stream>>>(
-            dst, src, B.pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
+    const int cfg = c->half_cfg;
+    const size_t sm = half_smem<T>(cfg);
+    switch (cfg) {
+        case 1: half_launch<T, 4, 16>(c, dst, src, xlines, hq, f, B.pp, sm); break;
+        case 2: half_launch<T, 8, 8>(c, dst, src, xlines, hq, f, B.pp, sm); break;
+        case 3: half_launch<T, 4, 32>(c, dst, src, xlines, hq, f, B.pp, sm); break;
+        case 4: half_launch<T, 2, 16>(c, dst, src, xlines, hq, f, B.pp, sm); break;
+        case 5: half_launch<T, 8, 32>(c, dst, src, xlines, hq, f, B.pp, sm); break;
+        default: half_launch<T, 8, 16>(c, dst, src, xlines, hq, f, B.pp, sm); break;
+    }
     GW_CUDA(cudaGetLastError());
     return GW_OK;
+}
+
+template <typename T, int HW, int HR>
+cudaError_t half_attr() {
+    const int sm = (int)(2 * (size_t)HR * (HW + 2) * 32 * sizeof(T));
+    cudaError_t e = cudaFuncSetAttribute(k_half_tile<T, true, HW, HR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_half_tile<T, false, HW, HR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+}
+
+template <typename T>
+cudaError_t half_attrs() {
+    cudaError_t e;
+    if ((e = half_attr<T, 8, 16>()) != cudaSuccess || (e = half_attr<T, 4, 16>()) != cudaSuccess ||
+        (e = half_attr<T, 8, 8>()) != cudaSuccess || (e = half_attr<T, 4, 32>()) != cudaSuccess ||
+        (e = half_attr<T, 2, 16>()) != cudaSuccess || (e = half_attr<T, 8, 32>()) != cudaSuccess)
+        return e;
+    return cudaSuccess;
 }
 
 template <typename T>
@@ -817,19 +853,8 @@ int gw_fused_prepare(gw_ctx *c) {
         e = cudaFuncSetAttribute(k_rock2_col<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)rock2_smem<double>(c->nz));
     if (e != cudaSuccess) return gw_cuda_fail(e, "cudaFuncSetAttribute(k_rock2_col)");
-    if (c->precision == GW_PREC_MIXED) {
-        if ((e = cudaFuncSetAttribute(k_half_tile<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)half_smem<float>())) != cudaSuccess ||
-            (e = cudaFuncSetAttribute(k_half_tile<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)half_smem<float>())) != cudaSuccess)
-            return gw_cuda_fail(e, "cudaFuncSetAttribute(k_half_tile)");
-    } else {
-        if ((e = cudaFuncSetAttribute(k_half_tile<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)half_smem<double>())) != cudaSuccess ||
-            (e = cudaFuncSetAttribute(k_half_tile<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)half_smem<double>())) != cudaSuccess)
-            return gw_cuda_fail(e, "cudaFuncSetAttribute(k_half_tile)");
-    }
+    if ((e = (c->precision == GW_PREC_MIXED ? half_attrs<float>() : half_attrs<double>())) != cudaSuccess)
+        return gw_cuda_fail(e, "cudaFuncSetAttribute(k_half_tile)");
     // the column kernels loop over columns: one resident wave of blocks
     int per_sm = 0;
     const bool mix = c->precision == GW_PREC_MIXED;

@@ -107,6 +107,7 @@ struct gw_ctx {
     double *d_tp = nullptr;           // double path: [ncol][nz] swept pipe columns
     double *d_pp = nullptr;           // double path: [ncol][countz] advected pipe values
     int rock2_grid = 0;
+    int half_cfg = 0;                 // half-step tiling (gw_fused.cu kTileHW/kTileHR)
     bool fused = false;
     // mixed path state (GW_PREC_MIXED): theta = T - T_ref(z) in float
     float *f_u = nullptr, *f_temp = nullptr, *f_g1 = nullptr, *f_tp = nullptr, *f_pp = nullptr;
@@ -121,6 +122,10 @@ struct gw_ctx {
     cudaGraphExec_t graph = nullptr;
     double graph_dt = -1.0;
     int graph_s = -1;
+    int graph_gen = -1;               // series_gen the graph was captured with
+    int series_gen = 0;               // bumped when d_series is reallocated
+    double tables_dt = -1.0;          // step size of the loaded stage/advection tables
+    int tables_s = -1;
 
     long long device_bytes = 0;
     std::vector<void *> allocations;
@@ -159,5 +164,6 @@ int gw_launch_advection(gw_ctx *c, double *phi, double dt);
 int gw_launch_record(gw_ctx *c, double dt);
 int gw_launch_check_finite(gw_ctx *c, const double *u, size_t n);
 int gw_ensure_factors(gw_ctx *c, double h);
+int gw_prepare_step(gw_ctx *c, double dt, int s, int nsteps);
 
 #define GW_STAGE_TABLE 208   // doubles: 2 per recurrence stage (<= 98) + 3

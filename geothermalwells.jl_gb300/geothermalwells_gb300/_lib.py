@@ -77,6 +77,12 @@ SIGNATURES = {
     "gw_get_last_step_time": (_i, [_vp, _dp]),
     "gw_profile_kernels": (_i, [_vp, _d, _i, _dp]),
     "gw_advection_noalloc": (_i, [_vp, _vp, _d, _d, _vp]),
+    "gw_batch_create": (_i, [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)]),
+    "gw_batch_destroy": (_i, [_vp]),
+    "gw_batch_set_tiling": (_i, [_vp, _i]),
+    "gw_batch_autotune": (_i, [_vp, _d, _i, _ip]),
+    "gw_batch_step": (_i, [_vp, _d, _i, _i]),
+    "gw_batch_get_last_step_time": (_i, [_vp, _dp]),
     "gw_tridiag_batch": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_longlong, _vp]),
 }
 KERNELS = ("rock2_columns", "half_step_x", "half_step_y", "pipe")

@@ -160,3 +160,62 @@ def tridiagonal_batch(nsys=262144, lmin=32, lmax=1024, seed=20261203):
     return dict(name="tridiagonal_batch_%d_len%d-%d" % (nsys, lmin, lmax), a=a, b=b, c=c, d=d,
                 group_off=goff[:-1].copy(), group_len=glen.astype(np.int32), n=n,
                 ngroups=ngroups, unknowns=int(lengths.sum()), slot_len=slot_len, order=order)
+
+
+def array_design(rng, n_cells, dt=3600.0, years=10.0, spacing=None, h=None, mdot=None):
+    """One 3 x 3 coaxial well array for the ensemble: spacing U(10, 40) m,
+    depth U(1500, 3000) m (snapped to the z grid so no sliver cell appears
+    at h), flow U(2, 8) kg/s, rock k per 100 m layer U(1.8, 3.5) W/m/K.
+    The x/y refinement is chosen so the grid has about n_cells cells with nz
+    between 300 and 1500."""
+    spacing = float(rng.uniform(10.0, 40.0)) if spacing is None else spacing
+    h = float(rng.uniform(1500.0, 3000.0)) if h is None else h
+    mdot = float(rng.uniform(2.0, 8.0)) if mdot is None else mdot
+    zmax = h + 200.0
+    nlay = int(np.ceil(zmax / 100.0))
+    ks = tuple(float(v) for v in rng.uniform(1.8, 3.5, nlay))
+    depths = tuple(100.0 * (q + 1) for q in range(nlay))
+    mat = StratifiedMaterialProperties(ks, (2.2e6,) * nlay, depths, 0.6, 4.18e6, 45.0, 3.73e6,
+                                       0.4, 1.96e6, 1.5, 1.76e6)
+    # nz and nxy: nz in [300, 1500], nxy in [81, 241], nxy^2 nz ~ n_cells
+    nz_target = int(np.clip(rng.uniform(300, 1500), 300, 1500))
+    nxy_target = int(np.clip(np.sqrt(n_cells / nz_target), 81, 241))
+    nz_target = int(np.clip(n_cells / nxy_target ** 2, 300, 1500))
+    dz = zmax / nz_target
+    h = round(h / dz) * dz
+    pos = (-spacing, 0.0, spacing)
+    bhs = tuple(Borehole(x, y, h, 0.0625, 0.01, 0.088, 0.01, 0.108, mdot, 0.0)
+                for y in pos for x in pos)
+    lo, hi = -spacing - 100.0, spacing + 100.0
+    # coarsest refinement whose grid reaches the target point count
+    f_lo, f_hi = 0.002, 0.2
+    for _ in range(30):
+        f = np.sqrt(f_lo * f_hi)
+        n = len(create_adaptive_grid_1d(xmin=lo, xmax=hi, dx_fine=f, growth_factor=1.2,
+                                        dx_max=8.0, boreholes=bhs, direction="x"))
+        if n > nxy_target:
+            f_lo = f
+        else:
+            f_hi = f
+    gx, gy = _xy(lo, hi, f_hi, 1.2, 8.0, bhs)
+    gz = create_uniform_gridz_with_borehole_depths(zmin=0.0, zmax=zmax, dz=dz, boreholes=bhs)
+    return dict(name="array3x3", gridx=gx, gridy=gy, gridz=gz, boreholes=bhs, materials=mat,
+                inlet_model=ConstantInlet(15.0), dt=dt, nsteps=int(round(years * 365 * 86400 / dt)),
+                t0=0.0, T_surface=8.0, gradient=0.03, spacing=spacing, h=h, mdot=mdot)
+
+
+def ensemble(n_designs=64, total_cells=1.5e9, seed=20261204):
+    """The heterogeneous ensemble: n_designs 3 x 3 arrays whose grids (81^2 x
+    300 up to 241^2 x 1500) add up to about total_cells.  Initial fields are
+    built per design on demand (initial_field) to keep host memory small."""
+    rng = np.random.default_rng(seed)
+    w = rng.lognormal(0.0, 0.8, n_designs)
+    w *= total_cells / w.sum()
+    w = np.clip(w, 81 ** 2 * 300, 241 ** 2 * 1500)
+    return [array_design(rng, float(cells)) for cells in w]
+
+
+def initial_field(d):
+    """T0 = T_surface + gradient z for one design (Fortran order, (Nz, Ny, Nx))."""
+    return initial_condition_thermal_gradient(None, np.float64, d["gridx"], d["gridy"], d["gridz"],
+                                              T_surface=d["T_surface"], gradient=d["gradient"])

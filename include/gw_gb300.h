@@ -153,6 +153,27 @@ int gw_get_last_step_time(gw_ctx *ctx, double *ms);
 #define GW_KERNEL_COUNT 4
 int gw_profile_kernels(gw_ctx *ctx, double dt, int reps, double *ms_out);
 
+/* ---- ensembles: many well designs advanced together ---- */
+/* Configuration 4 of the benchmark set (no single counterpart in the
+ * reference, which runs one cache per solve): a batch advances the contexts
+ * of many designs -- each created by gw_create with GW_PREC_MIXED or
+ * GW_PREC_FP64 on one device -- with one CUDA-graph launch per step in
+ * which the designs' fused steps run concurrently.  The contexts stay owned
+ * by the caller and must outlive the batch; per-design state, outlet series
+ * and energies are read with the single-context getters. */
+typedef struct gw_batch gw_batch;
+#define GW_TILINGS 6   /* half-step tilings (lines per block, rows per chunk) */
+int gw_batch_create(gw_ctx *const *ctxs, int n, gw_batch **out);
+int gw_batch_destroy(gw_batch *batch);
+/* Use one tiling (0 .. GW_TILINGS-1) for every design (0 is the default). */
+int gw_batch_set_tiling(gw_batch *batch, int tiling);
+/* Per design, time every tiling of the half-step kernels (`reps` launches,
+ * CUDA events) and keep the fastest; tiling_out[n] receives the choices. */
+int gw_batch_autotune(gw_batch *batch, double dt, int reps, int *tiling_out);
+/* nsteps fixed steps of size dt for every design (as gw_step per context). */
+int gw_batch_step(gw_batch *batch, double dt, int nsteps, int max_stages);
+int gw_batch_get_last_step_time(gw_batch *batch, double *ms);
+
 /* Batched independent tridiagonal solves A_s x_s = d_s (the elimination of
  * thomas_I_minus_A!, src/solver.jl:207-218, on arbitrary systems), all
  * arrays on the device in the grouped interleaved layout: systems sorted by

@@ -1,0 +1,54 @@
+"""Ensemble (batched designs): one graph launch per step advances every
+design exactly as its own gw_step does, for every half-step tiling."""
+import numpy as np
+import pytest
+
+from geothermalwells_gb300 import GB300, ODEProblem, ROCK2, create_cache, eigen_estimator, rhs_diffusion_z, solve
+from geothermalwells_gb300.ensemble import Ensemble, TILINGS
+from geothermalwells_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def designs():
+    return [W.small_case(), W.small_case(n_layers=3, inlet="hx", nbh=2),
+            W.small_case(backfill_quirk=True, n_layers=2, nz_cells=16)]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_equals_single_contexts(precision, gwlib):
+    ds = designs()
+    dt, n = 40.0, 5
+    ens = Ensemble(ds, precision=precision)
+    ens.step(dt, n)
+    for d, (design, c) in enumerate(zip(ds, ens.caches)):
+        single = create_cache(backend=GB300(precision=precision), gridx=design["gridx"],
+                              gridy=design["gridy"], gridz=design["gridz"],
+                              materials=design["materials"], boreholes=design["boreholes"],
+                              inlet_model=design["inlet_model"])
+        sol = solve(ODEProblem(rhs_diffusion_z, design["T0"], (0.0, n * dt), single),
+                    ROCK2(max_stages=100, eigen_est=eigen_estimator), dt=dt)
+        assert np.array_equal(c.get_field(), sol.u[-1])
+        assert np.array_equal(ens.outlet_series(d, n), sol.T_outlet)
+    ens.close()
+
+
+@pytest.mark.parametrize("tiling", range(len(TILINGS)))
+def test_every_tiling_gives_the_same_field(tiling, gwlib):
+    ds = designs()
+    a = Ensemble(ds, precision="mixed")
+    a.step(40.0, 3)
+    b = Ensemble(ds, precision="mixed")
+    b.set_tiling(tiling)
+    b.step(40.0, 3)
+    for ca, cb in zip(a.caches, b.caches):
+        assert np.array_equal(ca.get_field(), cb.get_field())
+    a.close(); b.close()
+
+
+def test_autotune_returns_valid_choices(gwlib):
+    ens = Ensemble(designs(), precision="mixed")
+    choice = ens.autotune(40.0, reps=1)
+    assert len(choice) == 3 and all(0 <= t < len(TILINGS) for t in choice)
+    ens.step(40.0, 2)
+    ens.close()
