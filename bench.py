@@ -38,7 +38,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    p.add_argument("--workload", default="large", choices=["large", "2mm", "thomas"])
+    p.add_argument("--workload", default="large", choices=["large", "2mm", "thomas", "ensemble"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-steps", type=int, default=1)
     p.add_argument("--accuracy", type=int, default=0, metavar="NSTEPS",
@@ -354,8 +354,60 @@ def run_thomas(args):
     print(json.dumps(line), flush=True)
 
 
+def run_ensemble(args):
+    """64 heterogeneous 3 x 3 well-array designs (about 1.5e9 cells in all),
+    dt 3600 s, advanced together (one graph launch per step); the autotuned
+    half-step tiling against the fixed default tiling."""
+    from geothermalwells_gb300 import workloads as W
+    from geothermalwells_gb300.ensemble import Ensemble, TILINGS
+    t0 = time.perf_counter()
+    designs = W.ensemble()
+    prec = args.precision
+    ens = Ensemble(designs, precision=prec, initial_field=W.initial_field)
+    setup_s = time.perf_counter() - t0
+    dt = 3600.0
+    choice = ens.autotune(dt, reps=2)
+    ens.step(dt, args.warmup)
+    clocks = Clocks(0)
+    ms_tuned = ens.step(dt, args.steps)
+    ck = clocks.stop()
+    ens.set_tiling(0)
+    ens.step(dt, 1)
+    ms_fixed = ens.step(dt, args.steps)
+    cells = ens.cells
+    finite = all(np.isfinite(ens.outlet_series(d, args.steps)).all() for d in range(len(designs)))
+    value = cells * args.steps / (ms_tuned / 1e3) / 1e6
+    wb = WORD[prec]
+    peak, peak_kind = peaks()
+    achieved = 6 * wb * cells * args.steps / (ms_tuned / 1e3) / 1e9   # 3 field passes of 2 words per step
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_tuned / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == "fp64" else "f32+f64acc", "data": "synthetic",
+            "config": {"workload": "ensemble_64_designs_3x3_arrays", "designs": len(designs),
+                       "cells": cells, "dt_s": dt, "setup_s": setup_s,
+                       "grid_range": [min(len(d["gridx"]) for d in designs),
+                                      max(len(d["gridx"]) for d in designs),
+                                      min(len(d["gridz"]) for d in designs),
+                                      max(len(d["gridz"]) for d in designs)],
+                       "l2": "inputs larger than L2"},
+            "tiling": {"autotuned_ms_per_step": ms_tuned / args.steps,
+                       "fixed_ms_per_step": ms_fixed / args.steps,
+                       "fixed": list(TILINGS[0]),
+                       "chosen_histogram": {str(list(TILINGS[t])): choice.count(t) for t in set(choice)}},
+            "roofline": {"kernel": "whole step (3 field passes)", "bound": "hbm", "achieved": achieved,
+                         "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None},
+            "outlet_finite": finite, "clocks": ck}
+    print(json.dumps(line), flush=True)
+    ens.close()
+
+
 def main():
     args = parse()
+    if args.workload == "ensemble":
+        run_ensemble(args)
+        return
     if args.workload == "thomas":
         run_thomas(args)
         return
