@@ -34,12 +34,15 @@ WORD = {"fp64": 8, "mixed": 4}
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=500)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
+                   help="path timed for `value`; the default run also times the other one")
     p.add_argument("--workload", default="large", choices=["large", "2mm", "thomas", "ensemble"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-compare", action="store_true",
+                   help="skip timing the other precision beside the main one")
     p.add_argument("--cpu-sample-steps", type=int, default=1)
     p.add_argument("--accuracy", type=int, default=0, metavar="NSTEPS",
                    help="run FP64 and mixed for NSTEPS steps and report their differences")
@@ -239,6 +242,22 @@ def run_ours(args):
            "h2d_bytes_per_step": 8 * ncell / args.steps,
            "d2h_bytes_per_step": (8 * ncell + 8 * args.steps * cache.N_bh) / args.steps,
            "path": "gw_set_field + gw_step(K) + gw_get_outlet_series + gw_get_field, pinned host"}
+    cache.close()
+    other = None
+    if not args.no_compare:
+        oprec = "fp64" if args.precision == "mixed" else "mixed"
+        oc = create_cache(backend=GB300(device=local, precision=oprec), gridx=w["gridx"],
+                          gridy=w["gridy"], gridz=w["gridz"], materials=w["materials"],
+                          boreholes=w["boreholes"], inlet_model=w["inlet_model"])
+        oc.set_field(w["T0"])
+        _lib.check(L.gw_step(oc.ctx, 0.0, dt, args.warmup, 100))
+        _lib.check(L.gw_step(oc.ctx, args.warmup * dt, dt, args.steps, 100))
+        oms = ctypes.c_double()
+        _lib.check(L.gw_get_last_step_time(oc.ctx, ctypes.byref(oms)))
+        oc.close()
+        ov = ncell * args.steps * world / (oms.value / 1e3) / 1e6
+        other = {"precision": oprec, "value": ov, "ms_per_step": oms.value / args.steps,
+                 "ratio_mixed_over_fp64": (value / ov) if args.precision == "mixed" else (ov / value)}
     if rank != 0:
         return
     cb = None
@@ -259,6 +278,7 @@ def run_ours(args):
                      "traffic": traffic, "kernel_ms": kms,
                      "alg_bytes_per_launch": alg[dom],
                      "step_share": {k: share[k] / sum(share.values()) for k in share}},
+        "compare": other,
         "cpu_baseline": cb, "e2e": e2e, "gpu_launches": launches_per_step * args.steps,
         "clocks": ck,
     }

@@ -166,8 +166,10 @@ def array_design(rng, n_cells, dt=3600.0, years=10.0, spacing=None, h=None, mdot
     """One 3 x 3 coaxial well array for the ensemble: spacing U(10, 40) m,
     depth U(1500, 3000) m (snapped to the z grid so no sliver cell appears
     at h), flow U(2, 8) kg/s, rock k per 100 m layer U(1.8, 3.5) W/m/K.
-    The x/y refinement is chosen so the grid has about n_cells cells with nz
-    between 300 and 1500."""
+    The x/y refinement (4 mm to 1 cm at the wells, so every inner pipe and
+    annulus holds grid columns; growth 1.6 to cells of at most 20 m) and nz
+    (300 to 1500) are chosen so the grid has about n_cells cells.  Resolving
+    the pipes of a 3 x 3 array needs at least ~150 points per direction."""
     spacing = float(rng.uniform(10.0, 40.0)) if spacing is None else spacing
     h = float(rng.uniform(1500.0, 3000.0)) if h is None else h
     mdot = float(rng.uniform(2.0, 8.0)) if mdot is None else mdot
@@ -187,17 +189,23 @@ def array_design(rng, n_cells, dt=3600.0, years=10.0, spacing=None, h=None, mdot
     bhs = tuple(Borehole(x, y, h, 0.0625, 0.01, 0.088, 0.01, 0.108, mdot, 0.0)
                 for y in pos for x in pos)
     lo, hi = -spacing - 100.0, spacing + 100.0
-    # coarsest refinement whose grid reaches the target point count
-    f_lo, f_hi = 0.002, 0.2
+    # coarsest refinement (at most 1 cm, so the 15 mm annulus and the inner
+    # pipe hold grid columns) whose grid reaches the target point count
+    f_lo, f_hi = 0.004, 0.01
     for _ in range(30):
         f = np.sqrt(f_lo * f_hi)
-        n = len(create_adaptive_grid_1d(xmin=lo, xmax=hi, dx_fine=f, growth_factor=1.2,
-                                        dx_max=8.0, boreholes=bhs, direction="x"))
+        n = len(create_adaptive_grid_1d(xmin=lo, xmax=hi, dx_fine=f, growth_factor=1.6,
+                                        dx_max=20.0, boreholes=bhs, direction="x"))
         if n > nxy_target:
             f_lo = f
         else:
             f_hi = f
-    gx, gy = _xy(lo, hi, f_hi, 1.2, 8.0, bhs)
+    gx, gy = _xy(lo, hi, f_hi, 1.6, 20.0, bhs)
+    # keep the design's cell budget: refit nz to the x/y count obtained
+    nz_target = int(np.clip(n_cells / len(gx) ** 2, 300, 1500))
+    dz = zmax / nz_target
+    h = round(bhs[0].h / dz) * dz
+    bhs = tuple(Borehole(b.xc, b.yc, h, 0.0625, 0.01, 0.088, 0.01, 0.108, mdot, 0.0) for b in bhs)
     gz = create_uniform_gridz_with_borehole_depths(zmin=0.0, zmax=zmax, dz=dz, boreholes=bhs)
     return dict(name="array3x3", gridx=gx, gridy=gy, gridz=gz, boreholes=bhs, materials=mat,
                 inlet_model=ConstantInlet(15.0), dt=dt, nsteps=int(round(years * 365 * 86400 / dt)),
