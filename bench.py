@@ -264,7 +264,7 @@ def run_ours(args):
     if not args.no_cpu_baseline and world == 1:
         cb = cpu_baseline(w, args.cpu_sample_steps)
         cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
-    launches_per_step = 1 + 2 + 2 * 5 + 1   # rock2 columns, 2 half steps, 2 x 5 pipe kernels, record
+    launches_per_step = 1 + 2 + 2 * 3 + 1   # rock2 columns, 2 half steps, 2 x 3 pipe kernels, record
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
