@@ -39,6 +39,8 @@ int prepare(gw_ctx *c, double dt, int max_stages, int nsteps, int *s_out) {
 
 extern "C" {
 
+int gw_batch_step(gw_batch *b, double dt, int nsteps, int max_stages);
+
 int gw_batch_create(gw_ctx *const *ctxs, int n, gw_batch **out) {
     if (!out || !ctxs || n < 1) return gw_fail(GW_ERR_ARG, "need at least one context");
     *out = nullptr;
@@ -88,21 +90,40 @@ int gw_batch_set_tiling(gw_batch *b, int tiling) {
     return GW_OK;
 }
 
-// For every design, time each half-step tiling (x- and y-lines, `reps`
-// launches each, CUDA events on the design's stream) and keep the fastest.
+// Autotuning in two rounds.  Round 1: per design, time each half-step
+// tiling of that design alone (x- and y-lines, `reps` launches, CUDA events
+// on the design's stream) and note its fastest.  Round 2: time the real
+// concurrent ensemble step (2 steps after a capture step) for every uniform
+// tiling and for the per-design choices of round 1, and keep the fastest
+// assignment.  Each design's state, outlet and energy are restored after.
 int gw_batch_autotune(gw_batch *b, double dt, int reps, int *tiling_out) {
     if (!b || !(dt > 0) || reps < 1) return gw_fail(GW_ERR_ARG, "bad arguments");
     int rc;
     GW_CUDA(cudaSetDevice(b->device));
-    for (size_t d = 0; d < b->ctx.size(); ++d) {
+    const int n = (int)b->ctx.size();
+    // save the states (u into the g1 scratch) and the outlet / energy values
+    std::vector<std::vector<double>> outl(n), energy(n);
+    for (int d = 0; d < n; ++d) {
+        gw_ctx *c = b->ctx[d];
+        const size_t N = (size_t)c->nx * c->ny * c->nz;
+        const bool mix = c->precision == GW_PREC_MIXED;
+        GW_CUDA(cudaMemcpyAsync(mix ? (void *)c->f_g1 : (void *)c->d_g1, mix ? (void *)c->f_u : (void *)c->d_u,
+                                N * (mix ? sizeof(float) : sizeof(double)), cudaMemcpyDeviceToDevice, c->stream));
+        outl[d].resize(c->nbh);
+        energy[d].resize(c->nbh);
+        GW_CUDA(cudaMemcpyAsync(outl[d].data(), c->d_outlet, c->nbh * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        GW_CUDA(cudaMemcpyAsync(energy[d].data(), c->d_energy, c->nbh * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        GW_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    // round 1
+    std::vector<int> own(n, 0);
+    for (int d = 0; d < n; ++d) {
         gw_ctx *c = b->ctx[d];
         int s;
         if ((rc = prepare(c, dt, 100, 1, &s))) return rc;
         float best = 1e30f;
-        int arg = 0;
         for (int t = 0; t < GW_TILINGS; ++t) {
             c->half_cfg = t;
-            // one untimed launch of each, then `reps` timed
             if ((rc = gw_fused_time_part(c, dt, s, GW_KERNEL_HALF_X)) ||
                 (rc = gw_fused_time_part(c, dt, s, GW_KERNEL_HALF_Y)))
                 return rc;
@@ -115,11 +136,33 @@ int gw_batch_autotune(gw_batch *b, double dt, int reps, int *tiling_out) {
             GW_CUDA(cudaEventSynchronize(c->ev1));
             float ms = 0.f;
             GW_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-            if (ms < best) { best = ms; arg = t; }
+            if (ms < best) { best = ms; own[d] = t; }
         }
-        c->half_cfg = arg;
+    }
+    // round 2: candidates are the uniform tilings and the round-1 choices
+    std::vector<std::vector<int>> cand;
+    for (int t = 0; t < GW_TILINGS; ++t) cand.push_back(std::vector<int>(n, t));
+    cand.push_back(own);
+    double best = 1e300;
+    size_t arg = 0;
+    for (size_t q = 0; q < cand.size(); ++q) {
+        for (int d = 0; d < n; ++d) { b->ctx[d]->half_cfg = cand[q][d]; b->ctx[d]->graph_dt = -1.0; }
+        b->graph_dt = -1.0;
+        if ((rc = gw_batch_step(b, dt, 1, 100)) || (rc = gw_batch_step(b, dt, 2, 100))) return rc;
+        if (b->last_ms < best) { best = b->last_ms; arg = q; }
+    }
+    for (int d = 0; d < n; ++d) {
+        gw_ctx *c = b->ctx[d];
+        c->half_cfg = cand[arg][d];
         c->graph_dt = -1.0;
-        if (tiling_out) tiling_out[d] = arg;
+        if (tiling_out) tiling_out[d] = cand[arg][d];
+        const size_t N = (size_t)c->nx * c->ny * c->nz;
+        const bool mix = c->precision == GW_PREC_MIXED;
+        GW_CUDA(cudaMemcpyAsync(mix ? (void *)c->f_u : (void *)c->d_u, mix ? (void *)c->f_g1 : (void *)c->d_g1,
+                                N * (mix ? sizeof(float) : sizeof(double)), cudaMemcpyDeviceToDevice, c->stream));
+        GW_CUDA(cudaMemcpyAsync(c->d_outlet, outl[d].data(), c->nbh * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        GW_CUDA(cudaMemcpyAsync(c->d_energy, energy[d].data(), c->nbh * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        GW_CUDA(cudaStreamSynchronize(c->stream));
     }
     b->graph_dt = -1.0;
     return GW_OK;

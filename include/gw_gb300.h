@@ -167,8 +167,11 @@ int gw_batch_create(gw_ctx *const *ctxs, int n, gw_batch **out);
 int gw_batch_destroy(gw_batch *batch);
 /* Use one tiling (0 .. GW_TILINGS-1) for every design (0 is the default). */
 int gw_batch_set_tiling(gw_batch *batch, int tiling);
-/* Per design, time every tiling of the half-step kernels (`reps` launches,
- * CUDA events) and keep the fastest; tiling_out[n] receives the choices. */
+/* Pick the half-step tiling of every design: each design's fastest tiling
+ * alone (`reps` timed launches), then the real concurrent ensemble step
+ * timed for every uniform tiling and for those per-design choices; the
+ * fastest assignment is kept (tiling_out[n]).  The designs' states, outlet
+ * and energy values are restored afterwards. */
 int gw_batch_autotune(gw_batch *batch, double dt, int reps, int *tiling_out);
 /* nsteps fixed steps of size dt for every design (as gw_step per context). */
 int gw_batch_step(gw_batch *batch, double dt, int nsteps, int max_stages);
