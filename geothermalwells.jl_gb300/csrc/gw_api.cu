@@ -366,6 +366,7 @@ int gw_destroy(gw_ctx *c) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    gw_adjoint_release(c);
     for (void *p : c->allocations) if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

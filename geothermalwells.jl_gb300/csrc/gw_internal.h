@@ -129,6 +129,7 @@ struct gw_ctx {
 
     long long device_bytes = 0;
     std::vector<void *> allocations;
+    struct GwAdj *adj = nullptr;      // adjoint tables (gw_adjoint.cu), built on first use
 };
 
 // error reporting
@@ -151,6 +152,11 @@ void gw_build_factors(const gw_ctx *c, double h, int dir, const std::vector<doub
 void gw_build_half_table(const gw_ctx *c, double h, int dir, const std::vector<double> &ecm,
                          const std::vector<double> &ecp, const std::vector<double> &a,
                          const std::vector<double> &ib, std::vector<double> &out4);
+void gw_build_adjoint_tables(const gw_ctx *c, std::vector<double> &wxm, std::vector<double> &wxp,
+                             std::vector<double> &wym, std::vector<double> &wyp,
+                             std::vector<double> &wzm, std::vector<double> &wzp,
+                             std::vector<unsigned char> &rock, std::vector<int> &layer);
+void gw_adjoint_release(gw_ctx *c);
 int gw_rock2_choose(double dt, double eigen_est, int max_stages, int *s, int *covered);
 void gw_rock2_coefs(int s, const double **mu, const double **nu, const double **kappa,
                     double *sigma, double *tau);

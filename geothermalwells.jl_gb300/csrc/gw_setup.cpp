@@ -289,6 +289,77 @@ void gw_build_coefs(const gw_ctx *c, std::vector<double> &cxm, std::vector<doubl
     }
 }
 
+// Tables of the adjoint.  The coefficients above are cp_l = (k_l + k_{l+1}) wp_l
+// and cm_l = (k_l + k_{l-1}) wm_l with wp_l = 0.5 / dp / mid / rho_c_l and
+// wm_l = 0.5 / dm / mid / rho_c_l (0 at the Neumann ends), so the derivative of
+// lambda^T A phi with respect to the conductivity of one cell is a sum of face
+// terms D = (phi_{l+1} - phi_l) (lambda_l wp_l - lambda_{l+1} wm_{l+1}) over
+// the cell's two faces.  rock[(zc * nx + i) * ny + j] = 1 where the cell's
+// conductivity is its rock layer's (src/physics.jl:199-233: no borehole
+// within r_backfill overrides it at that depth), i.e. where it depends on
+// the layer conductivity; layer[k] = the rock layer of level k.
+void gw_build_adjoint_tables(const gw_ctx *c, std::vector<double> &wxm, std::vector<double> &wxp,
+                             std::vector<double> &wym, std::vector<double> &wyp,
+                             std::vector<double> &wzm, std::vector<double> &wzp,
+                             std::vector<unsigned char> &rock, std::vector<int> &layer) {
+    const int nx = c->nx, ny = c->ny, nz = c->nz, nzc = c->n_zclass;
+    std::vector<int> rep(nzc, -1);
+    for (int k = 0; k < nz; ++k)
+        if (rep[c->zclass[k]] < 0) rep[c->zclass[k]] = k;
+    std::vector<double> R((size_t)nzc * nx * ny);
+    rock.assign((size_t)nzc * nx * ny, 0);
+    for (int zc = 0; zc < nzc; ++zc)
+        for (int i = 0; i < nx; ++i)
+            for (int j = 0; j < ny; ++j) {
+                double z = c->gz[rep[zc]];
+                size_t q = ((size_t)zc * nx + i) * ny + j;
+                R[q] = mat_rhoc(c, c->gx[i], c->gy[j], z);
+                bool r = true;
+                for (const GwBorehole &b : c->bh) {
+                    double dx = c->gx[i] - b.xc, dy = c->gy[j] - b.yc;
+                    double r_sq = dx * dx + dy * dy;
+                    if (r_sq > b.r_backfill_sq) continue;
+                    if (z <= b.h || z <= b.h + 3) r = false;
+                }
+                rock[q] = r ? 1 : 0;
+            }
+    auto RI = [&](int zc, int i, int j) { return R[((size_t)zc * nx + i) * ny + j]; };
+    auto unit = [](const double *g, int n, int l, double rc, double *wm, double *wp) {
+        double dp = (l == n - 1) ? (g[l] - g[l - 1]) : (g[l + 1] - g[l]);
+        double dm = (l == 0) ? dp : (g[l] - g[l - 1]);
+        double mid = (dp + dm) * 0.5;
+        *wp = (l == n - 1) ? 0.0 : 0.5 / dp / mid / rc;
+        *wm = (l == 0) ? 0.0 : 0.5 / dm / mid / rc;
+    };
+    wxm.assign((size_t)nzc * ny * nx, 0); wxp.assign((size_t)nzc * ny * nx, 0);
+    wym.assign((size_t)nzc * nx * ny, 0); wyp.assign((size_t)nzc * nx * ny, 0);
+    for (int zc = 0; zc < nzc; ++zc)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                size_t q = ((size_t)zc * ny + j) * nx + i;
+                unit(c->gx.data(), nx, i, RI(zc, i, j), &wxm[q], &wxp[q]);
+            }
+    for (int zc = 0; zc < nzc; ++zc)
+        for (int i = 0; i < nx; ++i)
+            for (int j = 0; j < ny; ++j) {
+                size_t q = ((size_t)zc * nx + i) * ny + j;
+                unit(c->gy.data(), ny, j, RI(zc, i, j), &wym[q], &wyp[q]);
+            }
+    std::vector<int> prof_i(c->n_profiles, -1), prof_j(c->n_profiles, -1);
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j) {
+            int p = c->colprof[(size_t)i * ny + j];
+            if (prof_i[p] < 0) { prof_i[p] = i; prof_j[p] = j; }
+        }
+    wzm.assign((size_t)c->n_profiles * nz, 0); wzp.assign((size_t)c->n_profiles * nz, 0);
+    for (int p = 0; p < c->n_profiles; ++p)
+        for (int k = 0; k < nz; ++k)
+            unit(c->gz.data(), nz, k, RI(c->zclass[k], prof_i[p], prof_j[p]), &wzm[(size_t)p * nz + k],
+                 &wzp[(size_t)p * nz + k]);
+    layer.assign(nz, 0);
+    for (int k = 0; k < nz; ++k) layer[k] = layer_of(c, c->gz[k]);
+}
+
 // LU factors of (I - h A) for every (z-class, line) of one direction, in the
 // scaled form used by the line kernels (src/solver.jl:208-218 elimination).
 void gw_build_factors(const gw_ctx *c, double h, int dir, const std::vector<double> &cm,

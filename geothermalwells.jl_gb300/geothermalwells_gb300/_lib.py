@@ -46,6 +46,12 @@ class Desc(ctypes.Structure):
                 ("device", ctypes.c_int)]
 
 
+class AdjointInfo(ctypes.Structure):
+    _fields_ = [("objective", ctypes.c_double), ("n_params", ctypes.c_int), ("stages", ctypes.c_int),
+                ("checkpoints", ctypes.c_int), ("forward_ms", ctypes.c_double),
+                ("reverse_ms", ctypes.c_double), ("peak_bytes", ctypes.c_longlong)]
+
+
 class Info(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in
                 ("nx", "ny", "nz", "n_boreholes", "countxy_inner", "countxy_outer", "countz",
@@ -84,6 +90,8 @@ SIGNATURES = {
     "gw_batch_step": (_i, [_vp, _d, _i, _i]),
     "gw_batch_get_last_step_time": (_i, [_vp, _dp]),
     "gw_tridiag_batch": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_longlong, _vp]),
+    "gw_adjoint": (_i, [_vp, _d, _i, _i, _i, _d, _d, _dp, _vp, ctypes.POINTER(AdjointInfo)]),
+    "gw_step_vjp": (_i, [_vp, _vp, _vp, _d, _i, _d, _d, _dp]),
 }
 KERNELS = ("rock2_columns", "half_step_x", "half_step_y", "pipe")
 

@@ -227,3 +227,29 @@ def initial_field(d):
     """T0 = T_surface + gradient z for one design (Fortran order, (Nz, Ny, Nx))."""
     return initial_condition_thermal_gradient(None, np.float64, d["gridx"], d["gridy"], d["gridz"],
                                               T_surface=d["T_surface"], gradient=d["gradient"])
+
+
+def adjoint_small(inlet="constant", nbh=1, n_layers=3, backfill_quirk=False, dt=200.0, nsteps=12):
+    """A few-thousand-cell well for checking gradients against central
+    differences of the oracle: the small_case geometry at low flow (0.6 kg/s,
+    + 0.3 per further borehole, so inner cells both interpolate within the
+    pipe and turn around at the bottom) run long enough (12 steps of 200 s)
+    for every rock layer to shape the outlet temperature."""
+    w = small_case(n_layers=n_layers, inlet=inlet, nbh=nbh, backfill_quirk=backfill_quirk, dt=dt)
+    bhs = tuple(b.with_flow(0.6 + 0.3 * q) for q, b in enumerate(w["boreholes"]))
+    return dict(w, name="adjoint_small", boreholes=bhs, nsteps=int(nsteps))
+
+
+def adjoint_well(seed=20261205):
+    """Gradient workload: the single_well_large grid (205 x 205 x 2002) with 22
+    rock layers of 100 m, k ~ U(1.8, 3.5) W/m/K (seeded), rho*c 2.2e6, 5 kg/s,
+    ConstantInlet 20 degC, 7 simulated days at dt = 300 s (2016 steps),
+    checkpoints every 64 steps."""
+    w = single_well_large()
+    rng = np.random.default_rng(seed)
+    ks = tuple(float(v) for v in rng.uniform(1.8, 3.5, 22))
+    depths = tuple(100.0 * (q + 1) for q in range(22))
+    mat = StratifiedMaterialProperties(ks, (2.2e6,) * 22, depths, 0.6, 4.18e6, 45.0, 3.73e6, 0.4,
+                                       1.96e6, 1.5, 1.76e6)
+    return dict(w, name="adjoint_well_205x205x2002_22layers", materials=mat, nsteps=2016,
+                checkpoint_every=64)

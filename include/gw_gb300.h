@@ -216,6 +216,48 @@ int gw_tridiag_batch(int precision, int ngroups, const long long *group_off, con
  * threads at once -- race on it and must be serialised by the caller. */
 int gw_advection_noalloc(gw_ctx *ctx, double *phi_dev, double dt, double t, double *T_outlet_dev);
 
+/* ---- adjoint: reverse-mode gradients of the time-step map ----
+ * No counterpart in the reference, which has no derivatives: these are the
+ * kernels a ChainRulesCore rrule over the solve (the Julia side of a
+ * torch.autograd.Function) calls.  GW_PREC_FP64 contexts only.
+ *
+ * Objective over the steps n = 0 .. nsteps-1 of size dt:
+ *   J = sum_b [ w_energy * E_b + w_outlet * T_out,b(last step) ],
+ *   E_b = sum_n mdot_b c_w (T_out,b^n - T_in,b^n) dt   (as gw_get_energy).
+ * Parameters, in this order in grad[]:
+ *   k_rock_layers[0 .. n_layers-1], mdot[0 .. n_boreholes-1], inlet_param
+ *   (T_const of the constant inlet, or dT of the heat-exchanger inlet).
+ * The derivative holds the branch structure of the advection fixed (which
+ * cells turn around or take the inlet value, the outlet window's levels),
+ * as the derivative of a piecewise map does. */
+typedef struct {
+    double objective;      /* J */
+    int n_params;          /* n_layers + n_boreholes + 1 */
+    int stages;            /* ROCK2 stages per step */
+    int checkpoints;       /* states kept by the forward sweep */
+    double forward_ms;     /* forward sweep with checkpoints, device time */
+    double reverse_ms;     /* recomputation + reverse sweep, device time */
+    long long peak_bytes;  /* device memory held during the call: context + adjoint */
+} gw_adjoint_info_t;
+
+/* Gradient of J over nsteps steps from the context's current field u^0.
+ * The forward sweep keeps u every checkpoint_every steps; the reverse sweep
+ * recomputes each segment's states and each step's intermediates.  grad
+ * receives n_params values; grad_T0_dev (device, N doubles, may be NULL)
+ * receives dJ/du^0.  Afterwards the context's field, outlet and energy are
+ * as after gw_step(ctx, 0, dt, nsteps, max_stages). */
+int gw_adjoint(gw_ctx *ctx, double dt, int nsteps, int max_stages, int checkpoint_every,
+               double w_energy, double w_outlet, double *grad, double *grad_T0_dev,
+               gw_adjoint_info_t *info);
+
+/* One step's vector-Jacobian product: with u_dev = u^n and lam_dev =
+ * dJ/du^{n+1} on entry, lam_dev = dJ/du^n on return, where J includes this
+ * step's objective terms (w_energy * its energy, w_outlet * its outlet
+ * temperature); grad[n_params] is accumulated into (+=).  The context's
+ * field is not touched.  For callers that drive the time loop themselves. */
+int gw_step_vjp(gw_ctx *ctx, const double *u_dev, double *lam_dev, double dt, int max_stages,
+                double w_energy, double w_outlet, double *grad);
+
 #ifdef __cplusplus
 }
 #endif
