@@ -39,7 +39,12 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                    help="path timed for `value`; the default run also times the other one")
-    p.add_argument("--workload", default="large", choices=["large", "2mm", "thomas", "ensemble"])
+    p.add_argument("--workload", default="large",
+                   choices=["large", "2mm", "thomas", "ensemble", "adjoint"])
+    p.add_argument("--fd", default="some", choices=["none", "some", "all"],
+                   help="adjoint workload: parameters checked by central differences")
+    p.add_argument("--adjoint-steps", type=int, default=0,
+                   help="adjoint workload: number of steps (default: the workload's 2016)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-compare", action="store_true",
                    help="skip timing the other precision beside the main one")
@@ -426,8 +431,112 @@ def run_ensemble(args):
     ens.close()
 
 
+def run_adjoint(args):
+    """Gradient workload: d(extracted heat over 7 days)/d(22 rock layer
+    conductivities, flow rate, inlet temperature) on the 205 x 205 x 2002 well
+    (3024 steps of 200 s, FP64), checkpoints every 64 steps.  Reports the
+    adjoint's device time as a multiple of one forward solve, the device
+    memory it holds, and central differences (h = 1e-4 relative) of the FP64
+    forward solve: --fd some checks the largest and the median layer
+    gradient, the flow rate, the inlet temperature and one random direction
+    through all 24 parameters; --fd all checks every parameter.  Each
+    difference is compared with 1e-4 of its value plus its own rounding
+    floor, 16 eps |J| / (2 h)."""
+    from geothermalwells_gb300 import GB300, create_cache, _lib
+    from geothermalwells_gb300 import adjoint as A
+    from geothermalwells_gb300 import workloads as W
+    L = _lib.load()
+    w = W.adjoint_well()
+    dt = args.dt if args.dt > 0 else w["dt"]
+    nsteps = args.adjoint_steps or w["nsteps"]
+    K = w["checkpoint_every"]
+    design = A.Design(w["gridx"], w["gridy"], w["gridz"], w["boreholes"], w["materials"],
+                      w["inlet_model"], w["T0"], dt, nsteps, checkpoint_every=K)
+    p0 = np.concatenate([w["materials"].k_rock_layers, [b.mdot for b in w["boreholes"]],
+                         [w["inlet_model"].param]])
+    nl = len(w["materials"].k_rock_layers)
+
+    def forward(p):
+        c = design.cache(p[:nl], p[nl:-1], p[-1])
+        try:
+            c.set_field(w["T0"])
+            _lib.check(L.gw_reset_energy(c.ctx))
+            _lib.check(L.gw_step(c.ctx, 0.0, dt, nsteps, 100))
+            E = np.zeros(c.N_bh)
+            _lib.check(L.gw_get_energy(c.ctx, _lib.dptr(E)))
+            ms = ctypes_double()
+            _lib.check(L.gw_get_last_step_time(c.ctx, ms))
+            return float(E.sum()), ms.value
+        finally:
+            c.close()
+
+    cache = design.cache(p0[:nl], p0[nl:-1], p0[-1])
+    cache.set_field(w["T0"])
+    _lib.check(L.gw_step(cache.ctx, 0.0, dt, 4, 100))     # warm-up (graph capture, tables)
+    J_fwd, fwd_ms = forward(p0)
+    clocks = Clocks(0)
+    r = A.adjoint(cache, w["T0"], dt, nsteps, checkpoint_every=K)
+    ck = clocks.stop()
+    cache.close()
+    g = r.grad
+    if args.fd == "all":
+        idx = list(range(len(p0)))
+    elif args.fd == "some":
+        order = np.argsort(np.abs(g[:nl]))
+        idx = sorted({int(order[-1]), int(order[nl // 2]), nl, len(p0) - 1})
+    else:
+        idx = []
+    eps = np.finfo(np.float64).eps
+    fd, rel, ok = {}, {}, True
+    for i in idx:
+        hs = 1e-4 * abs(p0[i])
+        pp, pm = p0.copy(), p0.copy()
+        pp[i] += hs
+        pm[i] -= hs
+        v = (forward(pp)[0] - forward(pm)[0]) / (pp[i] - pm[i])
+        fd[str(i)] = v
+        rel[str(i)] = abs(g[i] - v) / abs(v) if v != 0.0 else None
+        ok &= abs(g[i] - v) <= 1e-4 * abs(v) + 16 * eps * abs(J_fwd) / (pp[i] - pm[i])
+    direction = None
+    if args.fd != "none":
+        d = np.random.default_rng(7).choice([-1.0, 1.0], len(p0)) * p0   # relative steps
+        hs = 1e-4
+        v = (forward(p0 + hs * d)[0] - forward(p0 - hs * d)[0]) / (2 * hs)
+        a = float(np.dot(g, d))
+        direction = {"fd": v, "adjoint": a, "rel_err": abs(a - v) / abs(v)}
+        ok &= abs(a - v) <= 1e-4 * abs(v) + 16 * eps * abs(J_fwd) / (2 * hs)
+    finite = bool(np.isfinite(r.objective) and np.all(np.isfinite(g)))
+    cells = len(w["gridx"]) * len(w["gridy"]) * len(w["gridz"])
+    adj_ms = r.forward_ms + r.reverse_ms
+    line = {"metric": "adjoint cost (multiple of one forward solve)", "value": adj_ms / fwd_ms,
+            "unit": "x", "n_gpus": 1, "steps": nsteps, "higher_is_better": False,
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"], "cells": cells, "dt_s": dt, "checkpoint_every": K,
+                       "checkpoints": r.checkpoints, "stages": r.stages,
+                       "params": "k_rock_layers[22], mdot, T_inlet"},
+            "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "adjoint_forward_sweep_ms": r.forward_ms,
+            "adjoint_reverse_ms": r.reverse_ms,
+            "forward_mcell_steps_per_s": cells * nsteps / (fwd_ms / 1e3) / 1e6,
+            "peak_device_gb": r.peak_bytes / 1e9, "objective_J": r.objective,
+            "objective_forward_J": J_fwd, "grad": [float(v) for v in g],
+            "fd_check": {"h_rel": 1e-4, "fd": fd, "rel_err": rel,
+                         "max_rel_err": max([v for v in rel.values() if v is not None], default=None),
+                         "direction": direction, "within_1e-4": bool(ok)},
+            "finite": finite,
+            "clocks": ck}
+    print(json.dumps(line), flush=True)
+
+
+def ctypes_double():
+    import ctypes
+    return ctypes.c_double()
+
+
 def main():
     args = parse()
+    if args.workload == "adjoint":
+        run_adjoint(args)
+        return
     if args.workload == "ensemble":
         run_ensemble(args)
         return
