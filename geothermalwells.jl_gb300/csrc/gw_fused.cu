@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(256) k_rock2_col(T *__restrict__ u, const int 
 __device__ __forceinline__ int spad(int k) { return k + (k >> 5); }
 
 template <typename T, bool INC, int LPT>
-__global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int *__restrict__ order,
+__global__ void __launch_bounds__(256, LPT <= 8 ? 3 : 1) k_rock2_reg(T *__restrict__ u, const int *__restrict__ order,
                                                    const int *__restrict__ colprof,
                                                    const T *__restrict__ czm,
                                                    const T *__restrict__ czp,
@@ -154,37 +154,38 @@ __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *stage = reinterpret_cast<T *>(smem_raw);   // [2][spad(256 * LPT)]
     const int nzs = spad(256 * LPT);
-    __shared__ T s_lo[2][256], s_hi[2][256];
+    // run ends of every thread, shifted by one slot so thread t reads its
+    // neighbours at [t] (left, from s_hi) and [t + 1] (right, from s_lo)
+    // without predicates; the outer slots hold zeros.
+    __shared__ T s_lo[2][257], s_hi[2][257];
     const int t = threadIdx.x;
     const int kb = t * LPT;
-    const int nv = max(0, min(LPT, nz - kb));   // levels this thread owns
-    const bool tail = kb + nv >= nz;            // owns the bottom level of the column
     const int nrec = s - 2;
     int xb = 0;
+    // The column is padded to 256 * LPT levels: pad levels start at zero and
+    // have zero coefficients, so they never feed a real level (the real
+    // bottom level's cp is 0) and every thread owns exactly LPT levels.
+    for (int k = nz + t; k < 256 * LPT; k += 256) { stage[spad(k)] = T(0); stage[nzs + spad(k)] = T(0); }
+    if (t < 2) { s_hi[t][0] = T(0); s_lo[t][256] = T(0); }
     auto fetch = [&](long long col, int buf) {
         T *d = stage + (size_t)buf * nzs;
         const T *g = u + col * nz;
         for (int k = t; k < nz; k += 256) cp_async<sizeof(T)>(d + spad(k), g + k, true);
         cp_async_commit();
     };
-    // neighbours of this thread's run: level kb - 1 and level kb + nv
     auto exchange = [&](const T (&v)[LPT], T &left, T &right) {
-        T last = v[0];
-#pragma unroll
-        for (int i = 1; i < LPT; ++i)
-            if (i < nv) last = v[i];
         s_lo[xb][t] = v[0];
-        s_hi[xb][t] = last;
+        s_hi[xb][t + 1] = v[LPT - 1];
         __syncthreads();
-        left = t > 0 ? s_hi[xb][t - 1] : v[0];
-        right = (!tail && t + 1 < 256) ? s_lo[xb][t + 1] : last;
+        left = s_hi[xb][t];
+        right = s_lo[xb][t + 1];
         xb ^= 1;
     };
     auto apply = [&](const T (&v)[LPT], const T (&cm)[LPT], const T (&cp)[LPT], int i, T left,
                      T right) {
         const T gc = v[i];
         const T gm = i == 0 ? left : v[i > 0 ? i - 1 : 0];
-        const T gp = (i + 1 < nv) ? v[i + 1 < LPT ? i + 1 : i] : right;
+        const T gp = i + 1 < LPT ? v[i + 1 < LPT ? i + 1 : i] : right;
         return cp[i] * (gp - gc) - cm[i] * (gc - gm);
     };
     T cm[LPT], cp[LPT], fr[LPT];
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int 
             pcur = p;
 #pragma unroll
             for (int i = 0; i < LPT; ++i) {
-                const bool ok = i < nv;
+                const bool ok = kb + i < nz;
                 const size_t q = (size_t)p * nz + kb + i;
                 cm[i] = ok ? __ldg(czm + q) : T(0);
                 cp[i] = ok ? __ldg(czp + q) : T(0);
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int 
         T *st = stage + (size_t)buf * nzs;
         T base[LPT], F0[LPT], prev[LPT], cur[LPT];
 #pragma unroll
-        for (int i = 0; i < LPT; ++i) base[i] = i < nv ? st[spad(kb + i)] : T(0);
+        for (int i = 0; i < LPT; ++i) base[i] = st[spad(kb + i)];
         T left, right;
         exchange(base, left, right);
         if (INC) {
@@ -274,7 +275,7 @@ __global__ void __launch_bounds__(256) k_rock2_reg(T *__restrict__ u, const int 
             T a = apply(q, cm, cp, i, left, right);
             if (INC) a += F0[i];
             const T y = q[i] + hts * a + c3 * (q[i] - cur[i]);
-            if (i < nv) st[spad(kb + i)] = INC ? base[i] + y : y;
+            st[spad(kb + i)] = INC ? base[i] + y : y;
         }
         __syncthreads();
         T *uc = u + col * nz;
@@ -299,7 +300,6 @@ __device__ __forceinline__ double absT(T v, const double *Tref, int k) {
 // sums into the outlet mean (src/solver.jl:267-282, 257) and the per-level
 // annulus means (src/solver.jl:322-335).  Fixed summation order: the results
 // do not depend on scheduling.
-constexpr int kPipeChunk = 32;
 
 template <typename T>
 __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *__restrict__ part,
@@ -540,27 +540,43 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     T *dl = dst + k + m * mst;   // row 0 of this thread's line
     const int nchunk = (N + HR - 1) / HR;
 
-    // this warp copies neighbour-line slots mm = warp and warp + HW of each row
+    // this warp copies neighbour-line slots mm = warp and warp + HW of each
+    // row; slot pointers and validity are fixed for the whole line
+    const T *gs[2];
+    bool sok[2];
+#pragma unroll
+    for (int rep = 0; rep < 2; ++rep) {
+        const int mm = warp + rep * HW;
+        const int gm = m0 - 1 + mm;
+        sok[rep] = mm < HW + 2 && kok && gm >= 0 && gm < nl;
+        gs[rep] = sok[rep] ? src + k + (long long)gm * mst : src;
+    }
     auto load_chunk = [&](int ch, int buf) {
         T *t = tile + buf * kTile;
         const int l0 = ch * HR;
+        const bool full = l0 + HR <= N;
 #pragma unroll
         for (int rep = 0; rep < 2; ++rep) {
-            const int mm = warp + rep * HW;
-            if (mm >= HW + 2) break;
-            const int gm = m0 - 1 + mm;
-            const bool lok = kok && gm >= 0 && gm < nl;
-            const T *g = src + k + (long long)gm * mst + (long long)l0 * rst;
-            T *d = t + mm * 32 + lane;
-            for (int r = 0; r < HR; ++r) {
-                const bool ok = lok && l0 + r < N;
-                cp_async<sizeof(T)>(d + r * kRow, ok ? (const void *)(g + (long long)r * rst) : (const void *)src, ok);
+            if (warp + rep * HW >= HW + 2) break;
+            const T *g = gs[rep] + (long long)l0 * rst;
+            T *d = t + (warp + rep * HW) * 32 + lane;
+            if (full) {
+#pragma unroll
+                for (int r = 0; r < HR; ++r) cp_async<sizeof(T)>(d + r * kRow, sok[rep] ? (const void *)(g + r * rst) : (const void *)src, sok[rep]);
+            } else {
+                for (int r = 0; r < HR; ++r) {
+                    const bool ok = sok[rep] && l0 + r < N;
+                    cp_async<sizeof(T)>(d + r * kRow, ok ? (const void *)(g + r * rst) : (const void *)src, ok);
+                }
             }
         }
         cp_async_commit();
     };
+    // warp-uniform: does this line cross a pipe column at any level?
+    const bool line_pipe = __ldg(pipe_line + (size_t)nl * N + mc) != 0;
 
     T y = T(0);
+    T *dr = dl;
     load_chunk(0, 0);
     for (int ch = 0; ch < nchunk; ++ch) {
         if (ch + 1 < nchunk) {
@@ -571,28 +587,37 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
         }
         __syncthreads();
         const T *row = tile + (ch & 1) * kTile + warp * 32 + lane;
-        const int rmax = min(HR, N - ch * HR);
-        for (int r0 = 0; r0 < rmax; r0 += kHG) {
-            // the group's loads are issued before its dependent updates
-            Quad<T> q[kHG];
-            int pq[kHG];
-            T xm[kHG], xc[kHG], xp[kHG];
+        const int l0 = ch * HR;
+        const Quad<T> *qc = hql + l0;
+        if (l0 + HR <= N && !line_pipe) {
+            // full chunk, no pipe column on the line: straight-line rows
 #pragma unroll
-            for (int g = 0; g < kHG; ++g) {
-                const int r = min(r0 + g, rmax - 1);
-                const int l = ch * HR + r;
-                q[g] = hql[l];
-                pq[g] = pipe_levels ? __ldg(pline + l) : -1;
-                const T *rw = row + r * kRow;
-                xm[g] = rw[0]; xc[g] = rw[32]; xp[g] = rw[64];
+            for (int r0 = 0; r0 < HR; r0 += kHG) {
+                Quad<T> q[kHG];
+                T xm[kHG], xc[kHG], xp[kHG];
+#pragma unroll
+                for (int g = 0; g < kHG; ++g) {
+                    q[g] = qc[r0 + g];
+                    const T *rw = row + (r0 + g) * kRow;
+                    xm[g] = rw[0]; xc[g] = rw[32]; xp[g] = rw[64];
+                }
+#pragma unroll
+                for (int g = 0; g < kHG; ++g) {
+                    y = fma(q[g].x, xc[g], fma(q[g].y, xp[g], fma(q[g].z, xm[g], -q[g].w * y)));
+                    if (active) *dr = y;
+                    dr += rst;
+                }
             }
-            T *dr = dl + (long long)(ch * HR + r0) * rst;
-#pragma unroll
-            for (int g = 0; g < kHG; ++g) {
-                if (r0 + g >= rmax) break;
-                const T ay = q[g].w * y;
-                T yn = fma(q[g].x, xc[g], fma(q[g].y, xp[g], fma(q[g].z, xm[g], -ay)));
-                if (pq[g] >= 0) yn = fma(pp[(size_t)pq[g] * countz + k], __ldg(fib + fb + ch * HR + r0 + g), -ay);
+        } else {
+            const int rmax = min(HR, N - l0);
+            for (int r = 0; r < rmax; ++r) {
+                const int l = l0 + r;
+                const Quad<T> q = qc[r];
+                const T *rw = row + r * kRow;
+                const T ay = q.w * y;
+                T yn = fma(q.x, rw[32], fma(q.y, rw[64], fma(q.z, rw[0], -ay)));
+                const int pq = pipe_levels ? __ldg(pline + l) : -1;
+                if (pq >= 0) yn = fma(pp[(size_t)pq * countz + k], __ldg(fib + fb + l), -ay);
                 y = yn;
                 if (active) *dr = y;
                 dr += rst;
@@ -604,29 +629,40 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     // backward sweep: batches of kHB rows are loaded before the previous
     // batch is processed, so the loads overlap the dependent chain
     T x = y;
-    T *col = dst + k + m * mst;
-    T cur[kHB], nxt[kHB], cuc[kHB], cun[kHB];
+    const T *cuf = fcu + fb;
+    T *pc = dl + (long long)(N - 2) * rst;   // row l = N - 2
     int l = N - 2;
-    auto load_batch = [&](T *v, T *cv, int top) {
+    // full batches: rows l .. l - kHB + 1 all exist
+    if (l - kHB + 1 >= 0) {
+        T cur[kHB], cuc[kHB];
 #pragma unroll
-        for (int b = 0; b < kHB; ++b) {
-            const bool ok = top - b >= 0;
-            v[b] = ok ? col[(long long)(top - b) * rst] : T(0);
-            cv[b] = ok ? __ldg(fcu + fb + (top - b)) : T(0);
+        for (int b = 0; b < kHB; ++b) { cur[b] = pc[-(long long)b * rst]; cuc[b] = __ldg(cuf + l - b); }
+        while (l - kHB + 1 >= 0) {
+            const bool more = l - 2 * kHB + 1 >= 0;
+            T nxt[kHB], cun[kHB];
+            if (more) {
+#pragma unroll
+                for (int b = 0; b < kHB; ++b) {
+                    nxt[b] = pc[-(long long)(b + kHB) * rst];
+                    cun[b] = __ldg(cuf + l - kHB - b);
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < kHB; ++b) {
+                x = cur[b] - cuc[b] * x;
+                pc[-(long long)b * rst] = x;
+            }
+            pc -= (long long)kHB * rst;
+            l -= kHB;
+            if (!more) break;
+#pragma unroll
+            for (int b = 0; b < kHB; ++b) { cur[b] = nxt[b]; cuc[b] = cun[b]; }
         }
-    };
-    load_batch(cur, cuc, l);
-    while (l >= 0) {
-        load_batch(nxt, cun, l - kHB);
-#pragma unroll
-        for (int b = 0; b < kHB; ++b) {
-            if (l - b < 0) break;
-            x = cur[b] - cuc[b] * x;
-            col[(long long)(l - b) * rst] = x;
-        }
-#pragma unroll
-        for (int b = 0; b < kHB; ++b) { cur[b] = nxt[b]; cuc[b] = cun[b]; }
-        l -= kHB;
+    }
+    for (; l >= 0; --l) {
+        x = *pc - __ldg(cuf + l) * x;
+        *pc = x;
+        pc -= rst;
     }
 }
 
