@@ -496,11 +496,13 @@ __global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *_
 // batches loaded ahead of their use and overwrites it with x_l.
 // Tilings (lines per block HW, rows per chunk HR); the autotuner picks one
 // per context, the default is the first.
-constexpr int kTilings = 6;
-constexpr int kTileHW[kTilings] = {8, 4, 8, 4, 2, 8};
-constexpr int kTileHR[kTilings] = {16, 16, 8, 32, 16, 32};
+constexpr int kTilings = 7;   // the last one is the segmented kernel (k_half_seg)
+constexpr int kTileHW[kTilings] = {4, 8, 8, 4, 2, 8, 2};
+constexpr int kTileHR[kTilings] = {16, 16, 8, 32, 16, 32, 16};
+constexpr int kSegCfg = 6;
+constexpr int kSegS = 8, kSegR = 32;   // segments per line, rows per segment (lines up to 256)
 constexpr int kHG = 4;    // rows whose coefficients are loaded together
-constexpr int kHB = 8;    // rows per backward batch
+constexpr int kHB = 16;    // rows per backward batch
 
 
 template <typename T>
@@ -666,6 +668,126 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     }
 }
 
+// 3b. the same half step with each line split into S segments, one warp per
+//     (line, segment), 32 levels per warp.  The forward elimination
+//     y_l = b_l + alpha_l y_{l-1} (alpha_l = -a_l ib_l, b_l the explicit
+//     sweep folded with ib_l) and the back substitution x_l = y_l + delta_l
+//     x_{l+1} (delta_l = -cu_l) are first-order linear recurrences: every
+//     segment runs them from a zero start value, keeping its rows in
+//     registers, and the true start values follow from a scan over the
+//     segments' end values and end propagators (products of alpha or delta
+//     over the segment), exchanged through shared memory:
+//       y_l = y0_l + (prod_{s0..l} alpha) Y_in,   x_l = x0_l + (prod_{l..s1-1} delta) X_in.
+//     The forward values never leave the registers, so the field crosses
+//     HBM once in each direction; the neighbour lines of the explicit sweep
+//     are read straight from global memory (L1/L2 serve the reuse).
+template <typename T, bool XL, int HW, int S, int RMAX>
+__global__ void __launch_bounds__(32 * HW * S) k_half_seg(T *__restrict__ dst, const T *__restrict__ src,
+                                                          const T *__restrict__ pp,
+                                                          const int *__restrict__ pipe_line,
+                                                          const int *__restrict__ zclass,
+                                                          const Quad<T> *__restrict__ hq,
+                                                          const T *__restrict__ fib,
+                                                          const T *__restrict__ fcu, int nx, int ny,
+                                                          int nz, int countz) {
+    __shared__ T s_end[HW][S][32], s_prop[HW][S][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lw = warp / S, sg = warp % S;
+    const int nl = XL ? ny : nx;
+    const int N = XL ? nx : ny;
+    const int k = blockIdx.x * 32 + lane;
+    const int m = blockIdx.y * HW + lw;
+    const bool kok = k < nz;
+    const bool active = kok && m < nl;
+    const int kc = kok ? k : nz - 1, mc = m < nl ? m : nl - 1;
+    const long long mst = XL ? (long long)nz : (long long)nz * ny;
+    const long long rst = XL ? (long long)nz * ny : (long long)nz;
+    const int R = (N + S - 1) / S;                 // rows per segment (<= RMAX)
+    const int s0 = sg * R;
+    const int len = max(0, min(R, N - s0));
+    const size_t fb = ((size_t)zclass[kc] * nl + mc) * N + s0;
+    const Quad<T> *q = hq + fb;
+    const T *cu = fcu + fb;
+    // the line and its neighbours (clamped at the domain edge: the folded
+    // coefficient of a missing neighbour is zero)
+    const T *xc = src + kc + (long long)mc * mst + (long long)s0 * rst;
+    const T *xm = mc > 0 ? xc - mst : xc;
+    const T *xp = mc + 1 < nl ? xc + mst : xc;
+    const bool line_pipe = __ldg(pipe_line + (size_t)nl * N + mc) != 0;
+    const bool pipe_levels = line_pipe && k < countz;
+    const int *pline = pipe_line + (size_t)mc * N + s0;
+
+    // forward, local: y0 with a zero start value; P = prod of alpha
+    T v[RMAX];
+    T y = T(0), P = T(1);
+    if (!line_pipe) {
+#pragma unroll
+        for (int r = 0; r < RMAX; ++r) {
+            if (r < len) {
+                const Quad<T> c = q[r];
+                const long long o = (long long)r * rst;
+                y = fma(c.x, xc[o], fma(c.y, xp[o], fma(c.z, xm[o], -c.w * y)));
+                P *= -c.w;
+                v[r] = y;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < RMAX; ++r) {
+            if (r < len) {
+                const Quad<T> c = q[r];
+                const long long o = (long long)r * rst;
+                const int pq = pipe_levels ? __ldg(pline + r) : -1;
+                const T b = pq >= 0 ? pp[(size_t)pq * countz + k] * __ldg(fib + fb + r)
+                                    : fma(c.x, xc[o], fma(c.y, xp[o], c.z * xm[o]));
+                y = fma(-c.w, y, b);
+                P *= -c.w;
+                v[r] = y;
+            }
+        }
+    }
+    s_end[lw][sg][lane] = y;
+    s_prop[lw][sg][lane] = P;
+    __syncthreads();
+    T Y = T(0);
+    for (int g = 0; g < sg; ++g) Y = fma(s_prop[lw][g][lane], Y, s_end[lw][g][lane]);
+    // forward correction and local back substitution from a zero end value
+    T Pl = T(1);
+#pragma unroll
+    for (int r = 0; r < RMAX; ++r) {
+        if (r < len) {
+            Pl *= -q[r].w;
+            v[r] = fma(Pl, Y, v[r]);
+        }
+    }
+    __syncthreads();   // s_end / s_prop are reused below
+    T x = T(0), Q = T(1);
+#pragma unroll
+    for (int r = RMAX - 1; r >= 0; --r) {
+        if (r < len) {
+            const T d = -__ldg(cu + r);
+            x = fma(d, x, v[r]);
+            Q *= d;
+            v[r] = x;
+        }
+    }
+    s_end[lw][sg][lane] = x;     // x0 at the segment's first row
+    s_prop[lw][sg][lane] = Q;    // prod of delta over the segment
+    __syncthreads();
+    T X = T(0);
+    for (int g = S - 1; g > sg; --g) X = fma(s_prop[lw][g][lane], X, s_end[lw][g][lane]);
+    if (!active) return;
+    T *out = dst + k + (long long)m * mst + (long long)s0 * rst;
+    T Ql = T(1);
+#pragma unroll
+    for (int r = RMAX - 1; r >= 0; --r) {
+        if (r < len) {
+            Ql *= -__ldg(cu + r);
+            out[(long long)r * rst] = fma(Ql, X, v[r]);
+        }
+    }
+}
+
 // mixed path field conversion: theta = T - T_ref(z) and back
 __global__ void k_to_theta(float *__restrict__ th, const double *__restrict__ T,
                            const double *__restrict__ Tref, size_t n, int nz) {
@@ -810,15 +932,31 @@ int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h) {
     Bufs<T> B = bufs<T>(c);
     const GwFactors<T> &f = xlines ? B.ct->fx : B.ct->fy;
     const Quad<T> *hq = reinterpret_cast<const Quad<T> *>(xlines ? B.ct->hx : B.ct->hy);
-    const int cfg = c->half_cfg;
+    int cfg = c->half_cfg;
+    const int N = xlines ? c->nx : c->ny;
+    if (cfg == kSegCfg) {
+        if (N <= kSegS * kSegR) {
+            const int nl = xlines ? c->ny : c->nx;
+            dim3 grid((c->nz + 31) / 32, (nl + 1) / 2);
+            if (xlines)
+                k_half_seg<T, true, 2, kSegS, kSegR><<<grid, 32 * 2 * kSegS, 0, c->stream>>>(
+                    dst, src, B.pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
+            else
+                k_half_seg<T, false, 2, kSegS, kSegR><<<grid, 32 * 2 * kSegS, 0, c->stream>>>(
+                    dst, src, B.pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
+            GW_CUDA(cudaGetLastError());
+            return GW_OK;
+        }
+        cfg = 0;   // lines longer than the segments hold: the tiled kernel
+    }
     const size_t sm = half_smem<T>(cfg);
     switch (cfg) {
-        case 1: half_launch<T, 4, 16>(c, dst, src, xlines, hq, f, B.pp, sm); break;
+        case 1: half_launch<T, 8, 16>(c, dst, src, xlines, hq, f, B.pp, sm); break;
         case 2: half_launch<T, 8, 8>(c, dst, src, xlines, hq, f, B.pp, sm); break;
         case 3: half_launch<T, 4, 32>(c, dst, src, xlines, hq, f, B.pp, sm); break;
         case 4: half_launch<T, 2, 16>(c, dst, src, xlines, hq, f, B.pp, sm); break;
         case 5: half_launch<T, 8, 32>(c, dst, src, xlines, hq, f, B.pp, sm); break;
-        default: half_launch<T, 8, 16>(c, dst, src, xlines, hq, f, B.pp, sm); break;
+        default: half_launch<T, 4, 16>(c, dst, src, xlines, hq, f, B.pp, sm); break;
     }
     GW_CUDA(cudaGetLastError());
     return GW_OK;

@@ -12,7 +12,9 @@ import numpy as np
 from . import _lib
 from .cache import GB300, create_cache
 
-TILINGS = ((8, 16), (4, 16), (8, 8), (4, 32), (2, 16), (8, 32))   # (lines per block, rows per chunk)
+# (lines per block, rows per chunk) of the tiled half step; the last entry is
+# the segmented half step (2 lines per block, 8 segments of up to 32 rows)
+TILINGS = ((4, 16), (8, 16), (8, 8), (4, 32), (2, 16), (8, 32), (2, "seg8x32"))
 
 
 class Ensemble:

@@ -162,7 +162,8 @@ int gw_profile_kernels(gw_ctx *ctx, double dt, int reps, double *ms_out);
  * by the caller and must outlive the batch; per-design state, outlet series
  * and energies are read with the single-context getters. */
 typedef struct gw_batch gw_batch;
-#define GW_TILINGS 6   /* half-step tilings (lines per block, rows per chunk) */
+#define GW_TILINGS 7   /* half-step kernels: 0-5 row tiles (lines per block, rows per chunk),
+                          6 lines split into register-resident segments */
 int gw_batch_create(gw_ctx *const *ctxs, int n, gw_batch **out);
 int gw_batch_destroy(gw_batch *batch);
 /* Use one tiling (0 .. GW_TILINGS-1) for every design (0 is the default). */
