@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(256) k_rock2_col(T *__restrict__ u, const int 
 __device__ __forceinline__ int spad(int k) { return k + (k >> 5); }
 
 template <typename T, bool INC, int LPT>
-__global__ void __launch_bounds__(256, LPT <= 8 ? 3 : 1) k_rock2_reg(T *__restrict__ u, const int *__restrict__ order,
+__global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) k_rock2_reg(T *__restrict__ u, const int *__restrict__ order,
                                                    const int *__restrict__ colprof,
                                                    const T *__restrict__ czm,
                                                    const T *__restrict__ czp,
@@ -167,10 +167,14 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? 3 : 1) k_rock2_reg(T *__restri
     // bottom level's cp is 0) and every thread owns exactly LPT levels.
     for (int k = nz + t; k < 256 * LPT; k += 256) { stage[spad(k)] = T(0); stage[nzs + spad(k)] = T(0); }
     if (t < 2) { s_hi[t][0] = T(0); s_lo[t][256] = T(0); }
+    // thread t copies levels t + 256 i, whose padded slots are spad(t) + 264 i
+    const int st0 = spad(t);
     auto fetch = [&](long long col, int buf) {
-        T *d = stage + (size_t)buf * nzs;
-        const T *g = u + col * nz;
-        for (int k = t; k < nz; k += 256) cp_async<sizeof(T)>(d + spad(k), g + k, true);
+        T *d = stage + (size_t)buf * nzs + st0;
+        const T *g = u + col * nz + t;
+#pragma unroll
+        for (int i = 0; i < LPT; ++i)
+            if (t + 256 * i < nz) cp_async<sizeof(T)>(d + 264 * i, g + 256 * i, true);
         cp_async_commit();
     };
     auto exchange = [&](const T (&v)[LPT], T &left, T &right) {
@@ -278,8 +282,10 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? 3 : 1) k_rock2_reg(T *__restri
             st[spad(kb + i)] = INC ? base[i] + y : y;
         }
         __syncthreads();
-        T *uc = u + col * nz;
-        for (int k = t; k < nz; k += 256) uc[k] = st[spad(k)];
+        T *uc = u + col * nz + t;
+#pragma unroll
+        for (int i = 0; i < LPT; ++i)
+            if (t + 256 * i < nz) uc[256 * i] = st[st0 + 264 * i];
         __syncthreads();   // this buffer is refilled by the next iteration's fetch
     }
 }
