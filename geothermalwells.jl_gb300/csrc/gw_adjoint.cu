@@ -1,4 +1,6 @@
-// gw_adjoint.cu -- reverse-mode gradient of the time-step map (double path).
+// gw_adjoint.cu -- reverse-mode gradient of the time-step map, for the double
+// path (GW_PREC_FP64) and the mixed path (GW_PREC_MIXED: float adjoint fields
+// over the float theta = T - T_ref(z) states, double gradient sums).
 //
 // The reference has no derivatives; this is the differentiation layer a
 // ChainRulesCore rrule (or a torch.autograd.Function) binds.  Objective:
@@ -19,25 +21,32 @@
 //                                              the outlet window
 // Parameter derivatives: conductivity face terms summed per level (then per
 // rock layer), departure-point derivatives (flow rate through v_inner and
-// v_outer, src/physics.jl:49-57), inlet cells and the energy balance.
+// v_outer, src/physics.jl:49-57), inlet cells and the energy balance.  In the
+// mixed path T = theta + T_ref(z): A_x and A_y annihilate T_ref, so theta's
+// adjoint is T's, and the z face terms add T_ref's differences.
 //
 // Memory: the forward sweep keeps the state every K steps (checkpoints); the
 // reverse sweep recomputes one segment's states with the fused step, then
-// per step that step's intermediates with the modular kernels, and runs the
-// step's adjoint.  The branch structure of the advection (which cells turn
-// around, which take the inlet value, the outlet window's levels) is held
-// fixed, as any derivative of a piecewise map is.
+// per step the step's intermediates (double: the modular kernels; mixed: the
+// fused kernels, whose pipe passes leave the pre-advection values of the
+// pipe columns in a compact buffer) and runs the step's adjoint.  The branch
+// structure of the advection (which cells turn around, which take the inlet
+// value, the outlet window's levels) is held fixed, as any derivative of a
+// piecewise map is.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <vector>
 
+#include "gw_fused.h"
 #include "gw_internal.h"
 
 struct GwAdj {
     double *wxm = nullptr, *wxp = nullptr, *wym = nullptr, *wyp = nullptr;
     double *wzm = nullptr, *wzp = nullptr;
+    float *fxm = nullptr, *fxp = nullptr, *fym = nullptr, *fyp = nullptr;   // the same, float
+    float *fzm = nullptr, *fzp = nullptr;
     unsigned char *rock = nullptr;
     std::vector<int> layer;     // rock layer of each level
     double *G = nullptr;        // [nz] conductivity derivative per level
@@ -45,7 +54,7 @@ struct GwAdj {
                                 //           the current advection, its sum over calls
     double *osum = nullptr;     // [nbh] sum over steps of T_out - T_in
     double *mbar = nullptr;     // [nbh][nz] adjoint of the turnaround annulus means
-    double *tmp = nullptr;      // [ncol][countz] adjoint of the advected pipe values
+    double *tmp = nullptr;      // [ncol][countz] adjoint of the advected pipe values (8 B slots)
     std::vector<void *> allocs;
     long long bytes = 0;
 };
@@ -82,31 +91,52 @@ int adj_upload(GwAdj *a, T **p, const std::vector<T> &v) {
 // at k, cp_k at k+1 (cm_0 = cp_{nz-1} = 0), so (A_z^T lam)_k = cp_{k-1} lam_{k-1}
 // - (cm_k + cp_k) lam_k + cm_{k+1} lam_{k+1}.  w is read at the cell only, so
 // out may alias w (not lam).
-__global__ void __launch_bounds__(kB) k_zstage_t(double *out, const double *__restrict__ lam,
-                                                 const double *w, const int *__restrict__ colprof,
-                                                 const double *__restrict__ czm,
-                                                 const double *__restrict__ czp, int nz,
-                                                 long long ncell, double a1, double hmu, double a2) {
+template <typename T>
+__global__ void __launch_bounds__(kB) k_zstage_t(T *out, const T *__restrict__ lam, const T *w,
+                                                 const int *__restrict__ colprof,
+                                                 const T *__restrict__ czm, const T *__restrict__ czp,
+                                                 int nz, long long ncell, T a1, T hmu, T a2) {
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
     const int k = (int)(c % nz);
     const size_t base = (size_t)__ldg(colprof + c / nz) * nz;
-    const double lc = lam[c];
-    double at = -(__ldg(czm + base + k) + __ldg(czp + base + k)) * lc;
+    const T lc = lam[c];
+    T at = -(__ldg(czm + base + k) + __ldg(czp + base + k)) * lc;
     if (k > 0) at = fma(__ldg(czp + base + k - 1), lam[c - 1], at);
     if (k < nz - 1) at = fma(__ldg(czm + base + k + 1), lam[c + 1], at);
-    double v = fma(hmu, at, a1 * lc);
-    if (a2 != 0.0) v = fma(a2, w[c], v);
+    T v = fma(hmu, at, a1 * lc);
+    if (a2 != T(0)) v = fma(a2, w[c], v);
+    out[c] = v;
+}
+
+// Mixed path, forward: one ROCK2 stage on theta = T - T_ref with the source
+// fref = A_z T_ref (per profile and level):
+//   out = x + hmu (A_z x + fref) + kap (x - y)      (out may alias y, not x)
+__global__ void __launch_bounds__(kB) k_zstage_theta(float *out, const float *__restrict__ x,
+                                                     const float *y, const int *__restrict__ colprof,
+                                                     const float *__restrict__ czm,
+                                                     const float *__restrict__ czp,
+                                                     const float *__restrict__ fref, int nz,
+                                                     long long ncell, float hmu, float kap) {
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int k = (int)(c % nz);
+    const size_t q = (size_t)__ldg(colprof + c / nz) * nz + k;
+    const float xc = x[c];
+    const float xp = k < nz - 1 ? x[c + 1] : xc;
+    const float xm = k > 0 ? x[c - 1] : xc;
+    const float a = __ldg(czp + q) * (xp - xc) - __ldg(czm + q) * (xc - xm) + __ldg(fref + q);
+    float v = fmaf(hmu, a, xc);
+    if (kap != 0.f) v = fmaf(kap, xc - y[c], v);
     out[c] = v;
 }
 
 // dst = src + h A^T src along x (dir 0, table [zc][j][i]) or y (dir 1, [zc][i][j]).
-__global__ void __launch_bounds__(kB) k_explicit_t(double *__restrict__ dst,
-                                                   const double *__restrict__ src,
+template <typename T>
+__global__ void __launch_bounds__(kB) k_explicit_t(T *__restrict__ dst, const T *__restrict__ src,
                                                    const int *__restrict__ zclass,
-                                                   const double *__restrict__ cmt,
-                                                   const double *__restrict__ cpt, int nx, int ny,
-                                                   int nz, long long ncell, double h, int dir) {
+                                                   const T *__restrict__ cmt, const T *__restrict__ cpt,
+                                                   int nx, int ny, int nz, long long ncell, T h, int dir) {
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
     const int k = (int)(c % nz);
@@ -118,8 +148,8 @@ __global__ void __launch_bounds__(kB) k_explicit_t(double *__restrict__ dst,
     int l, n;
     if (dir == 0) { q = ((size_t)zc * ny + j) * nx + i; s = (long long)nz * ny; l = i; n = nx; }
     else { q = ((size_t)zc * nx + i) * ny + j; s = nz; l = j; n = ny; }
-    const double lc = src[c];
-    double at = -(__ldg(cmt + q) + __ldg(cpt + q)) * lc;
+    const T lc = src[c];
+    T at = -(__ldg(cmt + q) + __ldg(cpt + q)) * lc;
     if (l > 0) at = fma(__ldg(cpt + q - 1), src[c - s], at);
     if (l < n - 1) at = fma(__ldg(cmt + q + 1), src[c + s], at);
     dst[c] = fma(h, at, lc);
@@ -130,13 +160,11 @@ __global__ void __launch_bounds__(kB) k_explicit_t(double *__restrict__ dst,
 // (super-diagonal cu_l), so M^T = Ut^T Lt^T:
 //   forward  z_l = R_l - cu_{l-1} z_{l-1}
 //   backward x_l = (z_l - a_{l+1} x_{l+1}) ib_l
-__global__ void __launch_bounds__(128) k_thomas_t(double *__restrict__ U,
-                                                  const double *__restrict__ R,
-                                                  const int *__restrict__ zclass,
-                                                  const double *__restrict__ fa,
-                                                  const double *__restrict__ fib,
-                                                  const double *__restrict__ fcu, int nx, int ny,
-                                                  int nz, int dir) {
+template <typename T>
+__global__ void __launch_bounds__(128) k_thomas_t(T *__restrict__ U, const T *__restrict__ R,
+                                                  const int *__restrict__ zclass, const T *__restrict__ fa,
+                                                  const T *__restrict__ fib, const T *__restrict__ fcu,
+                                                  int nx, int ny, int nz, int dir) {
     const int nl = dir == 0 ? ny : nx;
     const int N = dir == 0 ? nx : ny;
     long long L = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -147,14 +175,14 @@ __global__ void __launch_bounds__(128) k_thomas_t(double *__restrict__ U,
     long long stride, off0;
     if (dir == 0) { stride = (long long)nz * ny; off0 = k + (long long)nz * m; }
     else { stride = nz; off0 = k + (long long)nz * ny * m; }
-    double z = 0.0, cprev = 0.0;
+    T z = T(0), cprev = T(0);
     for (int l = 0; l < N; ++l) {
         const long long o = off0 + l * stride;
         z = fma(-cprev, z, R[o]);
         U[o] = z;
         cprev = __ldg(fcu + fb + l);
     }
-    double x = z * __ldg(fib + fb + N - 1);
+    T x = z * __ldg(fib + fb + N - 1);
     U[off0 + (long long)(N - 1) * stride] = x;
     for (int l = N - 2; l >= 0; --l) {
         const long long o = off0 + l * stride;
@@ -167,42 +195,43 @@ __global__ void __launch_bounds__(128) k_thomas_t(double *__restrict__ U,
 // conductivity derivatives: G[k] += beta * d(lambda^T A phi)/dk summed over the
 // rock cells of level k (the face terms of gw_build_adjoint_tables).  One
 // thread per level, looping over a strided share of the columns; one atomic
-// per thread.
+// per thread.  Face terms are formed in the storage type and summed in double.
+// Tref (mixed path, z only): phi is theta and T_ref's differences are added.
 
-__global__ void __launch_bounds__(128) k_param_z(double *__restrict__ G, const double *__restrict__ lam,
-                                                 const double *__restrict__ phi,
-                                                 const int *__restrict__ colprof,
-                                                 const double *__restrict__ wzm,
-                                                 const double *__restrict__ wzp,
-                                                 const int *__restrict__ zclass,
+template <typename T>
+__global__ void __launch_bounds__(128) k_param_z(double *__restrict__ G, const T *__restrict__ lam,
+                                                 const T *__restrict__ phi, const double *__restrict__ Tref,
+                                                 const int *__restrict__ colprof, const T *__restrict__ wzm,
+                                                 const T *__restrict__ wzp, const int *__restrict__ zclass,
                                                  const unsigned char *__restrict__ rock, long long ncol,
                                                  int nz, double beta) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nz) return;
     const unsigned char *rk = rock + (size_t)__ldg(zclass + k) * ncol;   // [(zc * nx + i) * ny + j]
+    const T dtp = (Tref && k < nz - 1) ? T(Tref[k + 1] - Tref[k]) : T(0);
+    const T dtm = (Tref && k > 0) ? T(Tref[k] - Tref[k - 1]) : T(0);
     double acc = 0.0;
     for (long long col = blockIdx.y; col < ncol; col += gridDim.y) {
         if (!__ldg(rk + col)) continue;
         const long long c = col * nz + k;
         const size_t pb = (size_t)__ldg(colprof + col) * nz + k;
-        const double lk = lam[c], fk = phi[c];
-        double d = 0.0;
-        if (k < nz - 1) d = (phi[c + 1] - fk) * (lk * __ldg(wzp + pb) - lam[c + 1] * __ldg(wzm + pb + 1));
-        if (k > 0) d += (fk - phi[c - 1]) * (lam[c - 1] * __ldg(wzp + pb - 1) - lk * __ldg(wzm + pb));
-        acc += d;
+        const T lk = lam[c], fk = phi[c];
+        T d = T(0);
+        if (k < nz - 1) d = (phi[c + 1] - fk + dtp) * (lk * __ldg(wzp + pb) - lam[c + 1] * __ldg(wzm + pb + 1));
+        if (k > 0) d += (fk - phi[c - 1] + dtm) * (lam[c - 1] * __ldg(wzp + pb - 1) - lk * __ldg(wzm + pb));
+        acc += (double)d;
     }
     if (acc != 0.0) atomicAdd(G + k, beta * acc);
 }
 
 // x (dir 0) and y (dir 1): each face (l, l+1) of the level counted once, its
 // term attributed to both cells (same level).
-__global__ void __launch_bounds__(128) k_param_xy(double *__restrict__ G, const double *__restrict__ lam,
-                                                  const double *__restrict__ phi,
-                                                  const int *__restrict__ zclass,
-                                                  const double *__restrict__ wm,
-                                                  const double *__restrict__ wp,
-                                                  const unsigned char *__restrict__ rock, int nx,
-                                                  int ny, int nz, double beta, int dir) {
+template <typename T>
+__global__ void __launch_bounds__(128) k_param_xy(double *__restrict__ G, const T *__restrict__ lam,
+                                                  const T *__restrict__ phi, const int *__restrict__ zclass,
+                                                  const T *__restrict__ wm, const T *__restrict__ wp,
+                                                  const unsigned char *__restrict__ rock, int nx, int ny,
+                                                  int nz, double beta, int dir) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nz) return;
     const long long ncol = (long long)nx * ny;
@@ -225,7 +254,7 @@ __global__ void __launch_bounds__(128) k_param_xy(double *__restrict__ G, const 
         const int r = (int)__ldg(rk + col) + (int)__ldg(rk + col2);
         if (!r) continue;
         const long long c = col * nz + k, c2 = col2 * nz + k;
-        acc += r * ((phi[c2] - phi[c]) * (lam[c] * __ldg(wp + q) - lam[c2] * __ldg(wm + q + 1)));
+        acc += (double)(r * ((phi[c2] - phi[c]) * (lam[c] * __ldg(wp + q) - lam[c2] * __ldg(wm + q + 1))));
     }
     if (acc != 0.0) atomicAdd(G + k, beta * acc);
 }
@@ -249,23 +278,38 @@ __device__ __forceinline__ void interp(const double *__restrict__ g, int n, doub
     alpha = __ddiv_rn(__dsub_rn(dep, g[il]), __dsub_rn(g[ir], g[il]));
 }
 
+// The field the forward advection read, at pipe column q and level k, as an
+// absolute temperature: from the full field (double path) or from the compact
+// swept pipe columns [q][nz] plus T_ref (mixed path).
+template <typename T>
+struct PipeField {
+    const T *full;        // full field, or null
+    const T *tp;          // [ncol][nz], or null
+    const double *Tref;   // with tp
+    const int *pi, *pj;
+    int ny, nz;
+    __device__ __forceinline__ double at(int q, int k) const {
+        if (tp) return (double)tp[(size_t)q * nz + k] + Tref[k];
+        return (double)full[k + (long long)nz * (pj[q] + (long long)ny * pi[q])];
+    }
+};
+
 // The advected cells (pipe columns, levels < countz, z <= h) take no part of
 // their own old value: move their adjoint to tmp and clear it in the field.
-__global__ void __launch_bounds__(kB) k_adv_t_gather(double *__restrict__ tmp, double *__restrict__ a,
-                                                     const double *__restrict__ gz,
-                                                     const int *__restrict__ pi,
-                                                     const int *__restrict__ pj,
-                                                     const int *__restrict__ pb,
-                                                     const GwBhDev *__restrict__ bh, int ncol, int ny,
-                                                     int nz, int countz) {
+template <typename T>
+__global__ void __launch_bounds__(kB) k_adv_t_gather(double *__restrict__ tmp, T *__restrict__ a,
+                                                     const double *__restrict__ gz, const int *__restrict__ pi,
+                                                     const int *__restrict__ pj, const int *__restrict__ pb,
+                                                     const GwBhDev *__restrict__ bh, int ncol, int ny, int nz,
+                                                     int countz) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)ncol * countz) return;
     const int k = (int)(e % countz);
     const int q = (int)(e / countz);
     if (gz[k] > bh[pb[q]].h) { tmp[e] = 0.0; return; }
     const long long cell = k + (long long)nz * (pj[q] + (long long)ny * pi[q]);
-    tmp[e] = a[cell];
-    a[cell] = 0.0;
+    tmp[e] = (double)a[cell];
+    a[cell] = T(0);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -278,12 +322,12 @@ __device__ __forceinline__ double warp_sum(double v) {
 // with respect to v_inner / v_outer (through the departure points) and the
 // inlet adjoint.  phi is the field the forward advection read, mean its
 // annulus means.
+template <typename T>
 __global__ void __launch_bounds__(kB) k_adv_t_scatter(
-    double *__restrict__ a, const double *__restrict__ tmp, const double *__restrict__ phi,
-    const double *__restrict__ mean, const double *__restrict__ gz, const int *__restrict__ pi,
-    const int *__restrict__ pj, const int *__restrict__ pb, const GwBhDev *__restrict__ bh,
-    double *__restrict__ mbar, double *__restrict__ sc, int n_inner, int ncol, int ny, int nz,
-    int countz, double dt) {
+    T *__restrict__ a, const double *__restrict__ tmp, PipeField<T> phi, const double *__restrict__ mean,
+    const double *__restrict__ gz, const int *__restrict__ pi, const int *__restrict__ pj,
+    const int *__restrict__ pb, const GwBhDev *__restrict__ bh, double *__restrict__ mbar,
+    double *__restrict__ sc, int n_inner, int ncol, int ny, int nz, int countz, double dt) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double dvi = 0.0, dvo = 0.0, ib = 0.0;
     int b = -1;
@@ -314,9 +358,9 @@ __global__ void __launch_bounds__(kB) k_adv_t_scatter(
                     }
                 } else {
                     interp(gz, nz, zd, il, ir, al);
-                    atomicAdd(a + col + ir, al * ab);
-                    atomicAdd(a + col + il, (1.0 - al) * ab);
-                    if (ir != il) dvi += (phi[col + ir] - phi[col + il]) / (gz[ir] - gz[il]) * ab * dt;
+                    atomicAdd(a + col + ir, T(al * ab));
+                    atomicAdd(a + col + il, T((1.0 - al) * ab));
+                    if (ir != il) dvi += (phi.at(q, ir) - phi.at(q, il)) / (gz[ir] - gz[il]) * ab * dt;
                 }
             } else {
                 const double zd = __fma_rn(-B.v_outer, dt, z);
@@ -324,9 +368,9 @@ __global__ void __launch_bounds__(kB) k_adv_t_scatter(
                     ib += ab;
                 } else {
                     interp(gz, nz, zd, il, ir, al);
-                    atomicAdd(a + col + ir, al * ab);
-                    atomicAdd(a + col + il, (1.0 - al) * ab);
-                    if (ir != il) dvo -= (phi[col + ir] - phi[col + il]) / (gz[ir] - gz[il]) * ab * dt;
+                    atomicAdd(a + col + ir, T(al * ab));
+                    atomicAdd(a + col + il, T((1.0 - al) * ab));
+                    if (ir != il) dvo -= (phi.at(q, ir) - phi.at(q, il)) / (gz[ir] - gz[il]) * ab * dt;
                 }
             }
         }
@@ -352,15 +396,13 @@ __global__ void __launch_bounds__(kB) k_adv_t_scatter(
 // cells in the outlet window (z <= v_inner dt, src/solver.jl:273-281) their
 // share of the outlet adjoint  ob_scale * mdot_b + ob_add  plus, for the
 // heat-exchanger inlet (T_in = T_out - dT), the inlet adjoint of this call.
-__global__ void __launch_bounds__(kB) k_adv_t_fin(double *__restrict__ a, const double *__restrict__ mbar,
-                                                  const double *__restrict__ sc,
-                                                  const double *__restrict__ gz,
-                                                  const int *__restrict__ pi,
-                                                  const int *__restrict__ pj,
-                                                  const int *__restrict__ pb,
-                                                  const GwBhDev *__restrict__ bh, int n_inner,
-                                                  int ncol, int ny, int nz, double dt, int inlet_kind,
-                                                  double ob_scale, double ob_add) {
+template <typename T>
+__global__ void __launch_bounds__(kB) k_adv_t_fin(T *__restrict__ a, const double *__restrict__ mbar,
+                                                  const double *__restrict__ sc, const double *__restrict__ gz,
+                                                  const int *__restrict__ pi, const int *__restrict__ pj,
+                                                  const int *__restrict__ pb, const GwBhDev *__restrict__ bh,
+                                                  int n_inner, int ncol, int ny, int nz, double dt,
+                                                  int inlet_kind, double ob_scale, double ob_add) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)ncol * nz) return;
     const int k = (int)(e % nz);
@@ -378,10 +420,10 @@ __global__ void __launch_bounds__(kB) k_adv_t_fin(double *__restrict__ a, const 
         }
         double ob = ob_scale * B.mdot + ob_add;
         if (inlet_kind == GW_INLET_HEAT_EXCHANGER) ob += sc[4 * b + 2];
-        if (ob != 0.0) a[cell] += ob / ((double)B.inner_count * (double)lo);
+        if (ob != 0.0) a[cell] += T(ob / ((double)B.inner_count * (double)lo));
     } else {
         const double mb = mbar[(size_t)b * nz + k];
-        if (mb != 0.0) a[cell] += mb / (double)B.outer_count;
+        if (mb != 0.0) a[cell] += T(mb / (double)B.outer_count);
     }
 }
 
@@ -404,6 +446,24 @@ __global__ void k_osum(double *osum, const double *outlet, int nbh, int inlet_ki
     }
 }
 
+// Annulus means per borehole and level of the field the forward advection read.
+template <typename T>
+__global__ void __launch_bounds__(128) k_ann_mean(double *__restrict__ mean, PipeField<T> phi,
+                                                  const GwBhDev *__restrict__ bh, int nz) {
+    const int b = blockIdx.y;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nz) return;
+    const GwBhDev B = bh[b];
+    double s = 0.0;
+    for (int q = B.outer_begin; q < B.outer_begin + B.outer_count; ++q) s += phi.at(q, k);
+    mean[(size_t)b * nz + k] = s / (double)B.outer_count;
+}
+
+__global__ void k_to_double(double *__restrict__ out, const float *__restrict__ in, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (double)in[i];
+}
+
 // ---------------------------------------------------------------------------
 // host side
 
@@ -414,11 +474,15 @@ int ensure_adj(gw_ctx *c) {
     std::vector<double> wxm, wxp, wym, wyp, wzm, wzp;
     std::vector<unsigned char> rock;
     gw_build_adjoint_tables(c, wxm, wxp, wym, wyp, wzm, wzp, rock, a->layer);
+    auto f = [](const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); };
     const int ncol = c->n_inner + c->n_outer;
     int rc;
     if ((rc = adj_upload(a, &a->wxm, wxm)) || (rc = adj_upload(a, &a->wxp, wxp)) ||
         (rc = adj_upload(a, &a->wym, wym)) || (rc = adj_upload(a, &a->wyp, wyp)) ||
         (rc = adj_upload(a, &a->wzm, wzm)) || (rc = adj_upload(a, &a->wzp, wzp)) ||
+        (rc = adj_upload(a, &a->fxm, f(wxm))) || (rc = adj_upload(a, &a->fxp, f(wxp))) ||
+        (rc = adj_upload(a, &a->fym, f(wym))) || (rc = adj_upload(a, &a->fyp, f(wyp))) ||
+        (rc = adj_upload(a, &a->fzm, f(wzm))) || (rc = adj_upload(a, &a->fzp, f(wzp))) ||
         (rc = adj_upload(a, &a->rock, rock)) || (rc = adj_alloc(a, &a->G, (size_t)c->nz)) ||
         (rc = adj_alloc(a, &a->sc, (size_t)4 * c->nbh)) || (rc = adj_alloc(a, &a->osum, (size_t)c->nbh)) ||
         (rc = adj_alloc(a, &a->mbar, (size_t)c->nbh * c->nz)) ||
@@ -446,89 +510,97 @@ dim3 param_grid(const gw_ctx *c) {
     return dim3((unsigned)bx, (unsigned)by);
 }
 
-int launch_param(gw_ctx *c, const double *lam, const double *phi, double beta, int dir) {
+// Per-precision views of the context's tables.
+template <typename T>
+struct Tabs {
+    const GwCoefTables<T> *ct;
+    const T *wxm, *wxp, *wym, *wyp, *wzm, *wzp;
+    const double *Tref;    // mixed path: T_ref, for the z face terms
+};
+Tabs<double> tabs(gw_ctx *c, double *) {
     GwAdj *a = c->adj;
+    return {&c->c64, a->wxm, a->wxp, a->wym, a->wyp, a->wzm, a->wzp, nullptr};
+}
+Tabs<float> tabs(gw_ctx *c, float *) {
+    GwAdj *a = c->adj;
+    return {&c->c32, a->fxm, a->fxp, a->fym, a->fyp, a->fzm, a->fzp, c->d_Tref};
+}
+
+template <typename T>
+int launch_param(gw_ctx *c, const T *lam, const T *phi, double beta, int dir) {
+    GwAdj *a = c->adj;
+    Tabs<T> tb = tabs(c, (T *)nullptr);
     dim3 g = param_grid(c);
     if (dir == GW_DIR_Z)
-        k_param_z<<<g, 128, 0, c->stream>>>(a->G, lam, phi, c->d_colprof, a->wzm, a->wzp, c->d_zclass,
-                                            a->rock, (long long)c->nx * c->ny, c->nz, beta);
+        k_param_z<T><<<g, 128, 0, c->stream>>>(a->G, lam, phi, tb.Tref, c->d_colprof, tb.wzm, tb.wzp,
+                                               c->d_zclass, a->rock, (long long)c->nx * c->ny, c->nz, beta);
     else
-        k_param_xy<<<g, 128, 0, c->stream>>>(a->G, lam, phi, c->d_zclass,
-                                             dir == GW_DIR_X ? a->wxm : a->wym,
-                                             dir == GW_DIR_X ? a->wxp : a->wyp, a->rock, c->nx, c->ny,
-                                             c->nz, beta, dir);
+        k_param_xy<T><<<g, 128, 0, c->stream>>>(a->G, lam, phi, c->d_zclass, dir == GW_DIR_X ? tb.wxm : tb.wym,
+                                                dir == GW_DIR_X ? tb.wxp : tb.wyp, a->rock, c->nx, c->ny,
+                                                c->nz, beta, dir);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }
 
-int launch_zstage_t(gw_ctx *c, double *out, const double *lam, const double *w, double a1, double hmu,
-                    double a2) {
+template <typename T>
+int launch_zstage_t(gw_ctx *c, T *out, const T *lam, const T *w, double a1, double hmu, double a2) {
     const long long n = (long long)c->nx * c->ny * c->nz;
-    k_zstage_t<<<nblocks(n, kB), kB, 0, c->stream>>>(out, lam, w, c->d_colprof, c->c64.czm, c->c64.czp,
-                                                    c->nz, n, a1, hmu, a2);
+    Tabs<T> tb = tabs(c, (T *)nullptr);
+    k_zstage_t<T><<<nblocks(n, kB), kB, 0, c->stream>>>(out, lam, w, c->d_colprof, tb.ct->czm, tb.ct->czp,
+                                                       c->nz, n, (T)a1, (T)hmu, (T)a2);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }
 
-int launch_explicit_t(gw_ctx *c, double *dst, const double *src, double h, int dir) {
+template <typename T>
+int launch_explicit_t(gw_ctx *c, T *dst, const T *src, double h, int dir) {
     const long long n = (long long)c->nx * c->ny * c->nz;
-    const double *cm = dir == GW_DIR_X ? c->c64.cxm : c->c64.cym;
-    const double *cp = dir == GW_DIR_X ? c->c64.cxp : c->c64.cyp;
-    k_explicit_t<<<nblocks(n, kB), kB, 0, c->stream>>>(dst, src, c->d_zclass, cm, cp, c->nx, c->ny, c->nz,
-                                                      n, h, dir);
+    Tabs<T> tb = tabs(c, (T *)nullptr);
+    const T *cm = dir == GW_DIR_X ? tb.ct->cxm : tb.ct->cym;
+    const T *cp = dir == GW_DIR_X ? tb.ct->cxp : tb.ct->cyp;
+    k_explicit_t<T><<<nblocks(n, kB), kB, 0, c->stream>>>(dst, src, c->d_zclass, cm, cp, c->nx, c->ny,
+                                                         c->nz, n, (T)h, dir);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }
 
-int launch_thomas_t(gw_ctx *c, double *U, const double *R, int dir) {
+template <typename T>
+int launch_thomas_t(gw_ctx *c, T *U, const T *R, int dir) {
     const long long lines = (long long)c->nz * (dir == GW_DIR_X ? c->ny : c->nx);
-    const GwFactors<double> &f = dir == GW_DIR_X ? c->c64.fx : c->c64.fy;
-    k_thomas_t<<<nblocks(lines, 128), 128, 0, c->stream>>>(U, R, c->d_zclass, f.a, f.ib, f.cu, c->nx,
-                                                          c->ny, c->nz, dir);
+    Tabs<T> tb = tabs(c, (T *)nullptr);
+    const GwFactors<T> &f = dir == GW_DIR_X ? tb.ct->fx : tb.ct->fy;
+    k_thomas_t<T><<<nblocks(lines, 128), 128, 0, c->stream>>>(U, R, c->d_zclass, f.a, f.ib, f.cu, c->nx,
+                                                             c->ny, c->nz, dir);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
-}
-
-// Annulus means of phi per borehole and level (the forward's turnaround input).
-__global__ void __launch_bounds__(128) k_ann_mean(double *__restrict__ mean, const double *__restrict__ phi,
-                                                  const int *__restrict__ pi, const int *__restrict__ pj,
-                                                  const GwBhDev *__restrict__ bh, int ny, int nz) {
-    const int b = blockIdx.y;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nz) return;
-    const GwBhDev B = bh[b];
-    double s = 0.0;
-    for (int q = B.outer_begin; q < B.outer_begin + B.outer_count; ++q)
-        s += phi[k + (long long)nz * (pj[q] + (long long)ny * pi[q])];
-    mean[(size_t)b * nz + k] = s / (double)B.outer_count;
 }
 
 // Transpose of one advection call (half step h) in place on a; phi = the
 // field the forward call read.
-int advection_t(gw_ctx *c, double *a, const double *phi, double h, double ob_scale, double ob_add) {
+template <typename T>
+int advection_t(gw_ctx *c, T *a, PipeField<T> phi, double h, double ob_scale, double ob_add) {
     GwAdj *ad = c->adj;
     const int ncol = c->n_inner + c->n_outer;
     if (ncol == 0) return GW_OK;
     dim3 gm((c->nz + 127) / 128, c->nbh);
-    k_ann_mean<<<gm, 128, 0, c->stream>>>(c->d_annmean, phi, c->d_pipe_i, c->d_pipe_j, c->d_bh, c->ny,
-                                          c->nz);
+    k_ann_mean<T><<<gm, 128, 0, c->stream>>>(c->d_annmean, phi, c->d_bh, c->nz);
     GW_CUDA(cudaGetLastError());
     GW_CUDA(cudaMemsetAsync(ad->mbar, 0, sizeof(double) * c->nbh * c->nz, c->stream));
     if (c->countz > 0) {
         const long long n = (long long)ncol * c->countz;
-        k_adv_t_gather<<<nblocks(n, kB), kB, 0, c->stream>>>(ad->tmp, a, c->d_gz, c->d_pipe_i, c->d_pipe_j,
-                                                            c->d_pipe_b, c->d_bh, ncol, c->ny, c->nz,
-                                                            c->countz);
+        k_adv_t_gather<T><<<nblocks(n, kB), kB, 0, c->stream>>>(ad->tmp, a, c->d_gz, c->d_pipe_i, c->d_pipe_j,
+                                                               c->d_pipe_b, c->d_bh, ncol, c->ny, c->nz,
+                                                               c->countz);
         GW_CUDA(cudaGetLastError());
-        k_adv_t_scatter<<<nblocks(n, kB), kB, 0, c->stream>>>(
-            a, ad->tmp, phi, c->d_annmean, c->d_gz, c->d_pipe_i, c->d_pipe_j, c->d_pipe_b, c->d_bh,
-            ad->mbar, ad->sc, c->n_inner, ncol, c->ny, c->nz, c->countz, h);
+        k_adv_t_scatter<T><<<nblocks(n, kB), kB, 0, c->stream>>>(
+            a, ad->tmp, phi, c->d_annmean, c->d_gz, c->d_pipe_i, c->d_pipe_j, c->d_pipe_b, c->d_bh, ad->mbar,
+            ad->sc, c->n_inner, ncol, c->ny, c->nz, c->countz, h);
         GW_CUDA(cudaGetLastError());
     }
     const long long nf = (long long)ncol * c->nz;
-    k_adv_t_fin<<<nblocks(nf, kB), kB, 0, c->stream>>>(a, ad->mbar, ad->sc, c->d_gz, c->d_pipe_i,
-                                                      c->d_pipe_j, c->d_pipe_b, c->d_bh, c->n_inner, ncol,
-                                                      c->ny, c->nz, h, c->inlet_kind, ob_scale, ob_add);
+    k_adv_t_fin<T><<<nblocks(nf, kB), kB, 0, c->stream>>>(a, ad->mbar, ad->sc, c->d_gz, c->d_pipe_i,
+                                                         c->d_pipe_j, c->d_pipe_b, c->d_bh, c->n_inner, ncol,
+                                                         c->ny, c->nz, h, c->inlet_kind, ob_scale, ob_add);
     GW_CUDA(cudaGetLastError());
     k_adv_t_close<<<1, ((c->nbh + 31) / 32) * 32, 0, c->stream>>>(ad->sc, c->nbh);
     GW_CUDA(cudaGetLastError());
@@ -536,16 +608,28 @@ int advection_t(gw_ctx *c, double *a, const double *phi, double h, double ob_sca
 }
 
 // Buffers of one step's forward intermediates.
+template <typename T>
 struct StepStore {
-    std::vector<double *> g;   // ROCK2 stages g_1 .. g_{s-2}, then g_q (s - 1 fields)
-    double *ustar, *tA, *u1, *tC, *work;
+    std::vector<T *> g;   // ROCK2 stages g_1 .. g_{s-2}, then g_q (s - 1 fields)
+    T *ustar, *u1;        // after ROCK2, after the x half step
+    T *tA, *tC, *work;    // double path: the fields the two advections read, scratch
+    T *tpA, *tpC;         // mixed path: those fields at the pipe columns ([ncol][nz])
+    PipeField<T> pA, pC;
 };
 
-// Recompute the step from un with the modular kernels, keeping what the
-// adjoint reads: the ROCK2 stages, u* (after ROCK2), tA (before the first
-// advection), u1 (after the x solve), tC (before the second advection).
-// un1 (optional) receives u^{n+1}.  Adds the step's T_out - T_in to osum.
-int forward_store(gw_ctx *c, const double *un, StepStore &S, double dt, int s, double *un1) {
+int launch_osum(gw_ctx *c) {
+    k_osum<<<1, ((c->nbh + 31) / 32) * 32, 0, c->stream>>>(c->adj->osum, c->d_outlet, c->nbh, c->inlet_kind,
+                                                          c->inlet_param);
+    GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}
+
+// Double path: recompute the step from un with the modular kernels, keeping
+// what the adjoint reads: the ROCK2 stages, u* (after ROCK2), tA (before the
+// first advection), u1 (after the x solve), tC (before the second
+// advection).  un1 (optional) receives u^{n+1}.  Adds the step's T_out - T_in
+// to osum.
+int forward_store(gw_ctx *c, const double *un, StepStore<double> &S, double dt, int s, double *un1) {
     const double *mu, *nu, *kappa;
     double sigma, tau;
     gw_rock2_coefs(s, &mu, &nu, &kappa, &sigma, &tau);
@@ -570,56 +654,88 @@ int forward_store(gw_ctx *c, const double *un, StepStore &S, double dt, int s, d
         (rc = gw_launch_explicit(c, S.tC, S.u1, h, GW_DIR_X)))
         return rc;
     GW_CUDA(cudaMemcpyAsync(S.work, S.tC, bytes, cudaMemcpyDeviceToDevice, c->stream));
-    if ((rc = gw_launch_advection(c, S.work, h))) return rc;
-    k_osum<<<1, ((c->nbh + 31) / 32) * 32, 0, c->stream>>>(c->adj->osum, c->d_outlet, c->nbh, c->inlet_kind,
-                                                          c->inlet_param);
-    GW_CUDA(cudaGetLastError());
+    if ((rc = gw_launch_advection(c, S.work, h)) || (rc = launch_osum(c))) return rc;
     if (un1 && (rc = gw_launch_thomas(c, un1, S.work, GW_DIR_Y))) return rc;
     return GW_OK;
+}
+
+// Mixed path: the ROCK2 stages of theta from un (for the conductivity terms),
+// then the fused ROCK2 columns and first half step on the context's state
+// (u* and u1 copied out, the pipe columns of the two advections' inputs kept
+// in tpA / tpC).
+int forward_store(gw_ctx *c, const float *un, StepStore<float> &S, double dt, int s, float *) {
+    const double *mu, *nu, *kappa;
+    double sigma, tau;
+    gw_rock2_coefs(s, &mu, &nu, &kappa, &sigma, &tau);
+    const long long n = (long long)c->nx * c->ny * c->nz;
+    const size_t bytes = (size_t)n * sizeof(float);
+    const unsigned nb = nblocks(n, kB);
+    const float *gm2 = nullptr, *gm1 = un;
+    for (int j = 1; j <= s - 2; ++j) {
+        float *out = S.g[j - 1];
+        k_zstage_theta<<<nb, kB, 0, c->stream>>>(out, gm1, gm2, c->d_colprof, c->c32.czm, c->c32.czp, c->f_fref,
+                                                 c->nz, n, (float)(dt * mu[j - 1]),
+                                                 (float)(j == 1 ? 0.0 : kappa[j - 1]));
+        GW_CUDA(cudaGetLastError());
+        gm2 = gm1;
+        gm1 = out;
+    }
+    k_zstage_theta<<<nb, kB, 0, c->stream>>>(S.g[s - 2], gm1, nullptr, c->d_colprof, c->c32.czm, c->c32.czp,
+                                             c->f_fref, c->nz, n, (float)(dt * sigma), 0.f);
+    GW_CUDA(cudaGetLastError());
+    GW_CUDA(cudaMemcpyAsync(c->f_u, un, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    int rc;
+    if ((rc = gw_fused_adjoint_store(c, dt, s, S.tpA, S.tpC))) return rc;
+    GW_CUDA(cudaMemcpyAsync(S.ustar, c->f_u, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    GW_CUDA(cudaMemcpyAsync(S.u1, c->f_temp, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    return launch_osum(c);
 }
 
 // Adjoint of one step.  B[0] holds dJ/du^{n+1} on entry; B[1], B[2] are
 // scratch.  On return *res is the index of the buffer holding dJ/du^n.
 // un = u^n, un1 = u^{n+1}; ob_scale / ob_add: the second advection's outlet
 // adjoint (energy and final-outlet terms).
-int adjoint_step(gw_ctx *c, const double *un, const double *un1, StepStore &S, double *B[3], double dt,
-                 int s, double ob_scale, double ob_add, int *res) {
+template <typename T>
+int adjoint_step(gw_ctx *c, const T *un, const T *un1, StepStore<T> &S, T *B[3], double dt, int s,
+                 double ob_scale, double ob_add, int *res) {
     const double *mu, *nu, *kappa;
     double sigma, tau;
     gw_rock2_coefs(s, &mu, &nu, &kappa, &sigma, &tau);
     const double h = dt / 2;
     int rc;
     // u^{n+1} = (I - h A_y)^{-1} t4
-    if ((rc = launch_thomas_t(c, B[1], B[0], GW_DIR_Y)) || (rc = launch_param(c, B[1], un1, h, GW_DIR_Y)))
+    if ((rc = launch_thomas_t<T>(c, B[1], B[0], GW_DIR_Y)) || (rc = launch_param<T>(c, B[1], un1, h, GW_DIR_Y)))
         return rc;
     // t4 = advection(tC)
-    if ((rc = advection_t(c, B[1], S.tC, h, ob_scale, ob_add))) return rc;
+    if ((rc = advection_t<T>(c, B[1], S.pC, h, ob_scale, ob_add))) return rc;
     // tC = (I + h A_x) u1 ; u1 = (I - h A_x)^{-1} t2
-    if ((rc = launch_explicit_t(c, B[2], B[1], h, GW_DIR_X)) || (rc = launch_param(c, B[1], S.u1, h, GW_DIR_X)) ||
-        (rc = launch_thomas_t(c, B[0], B[2], GW_DIR_X)) || (rc = launch_param(c, B[0], S.u1, h, GW_DIR_X)))
+    if ((rc = launch_explicit_t<T>(c, B[2], B[1], h, GW_DIR_X)) ||
+        (rc = launch_param<T>(c, B[1], S.u1, h, GW_DIR_X)) || (rc = launch_thomas_t<T>(c, B[0], B[2], GW_DIR_X)) ||
+        (rc = launch_param<T>(c, B[0], S.u1, h, GW_DIR_X)))
         return rc;
     // t2 = advection(tA)
-    if ((rc = advection_t(c, B[0], S.tA, h, 0.0, 0.0))) return rc;
+    if ((rc = advection_t<T>(c, B[0], S.pA, h, 0.0, 0.0))) return rc;
     // tA = (I + h A_y) u*
-    if ((rc = launch_explicit_t(c, B[1], B[0], h, GW_DIR_Y)) || (rc = launch_param(c, B[0], S.ustar, h, GW_DIR_Y)))
+    if ((rc = launch_explicit_t<T>(c, B[1], B[0], h, GW_DIR_Y)) ||
+        (rc = launch_param<T>(c, B[0], S.ustar, h, GW_DIR_Y)))
         return rc;
     // ROCK2: u* = gq + (dt tau/sigma) A gq + cc (gq - gp);  gq = gp + dt sigma A gp
     const double cc = 1.0 - tau / (sigma * sigma);
-    const double *gq = S.g[s - 2];
-    const double *gp = S.g[s - 3];
-    if ((rc = launch_zstage_t(c, B[2], B[1], nullptr, 1.0 + cc, dt * tau / sigma, 0.0)) ||
-        (rc = launch_param(c, B[1], gq, dt * tau / sigma, GW_DIR_Z)) ||
-        (rc = launch_zstage_t(c, B[1], B[2], B[1], 1.0, dt * sigma, -cc)) ||
-        (rc = launch_param(c, B[2], gp, dt * sigma, GW_DIR_Z)))
+    const T *gq = S.g[s - 2];
+    const T *gp = S.g[s - 3];
+    if ((rc = launch_zstage_t<T>(c, B[2], B[1], nullptr, 1.0 + cc, dt * tau / sigma, 0.0)) ||
+        (rc = launch_param<T>(c, B[1], gq, dt * tau / sigma, GW_DIR_Z)) ||
+        (rc = launch_zstage_t<T>(c, B[1], B[2], B[1], 1.0, dt * sigma, -cc)) ||
+        (rc = launch_param<T>(c, B[2], gp, dt * sigma, GW_DIR_Z)))
         return rc;
     // recurrence g_j = (1 + kappa_j) g_{j-1} + dt mu_j A g_{j-1} - kappa_j g_{j-2}, backwards
     int cur = 1, old = 2;
     for (int j = s - 2; j >= 1; --j) {
-        const double *gprev = j == 1 ? un : S.g[j - 2];
+        const T *gprev = j == 1 ? un : S.g[j - 2];
         const double kj = j == 1 ? 0.0 : kappa[j - 1];
-        if ((rc = launch_param(c, B[cur], gprev, dt * mu[j - 1], GW_DIR_Z))) return rc;
-        if (j == s - 2) rc = launch_zstage_t(c, B[old], B[cur], nullptr, 1.0 + kj, dt * mu[j - 1], 0.0);
-        else rc = launch_zstage_t(c, B[old], B[cur], B[old], 1.0 + kj, dt * mu[j - 1], -kappa[j]);
+        if ((rc = launch_param<T>(c, B[cur], gprev, dt * mu[j - 1], GW_DIR_Z))) return rc;
+        if (j == s - 2) rc = launch_zstage_t<T>(c, B[old], B[cur], nullptr, 1.0 + kj, dt * mu[j - 1], 0.0);
+        else rc = launch_zstage_t<T>(c, B[old], B[cur], B[old], 1.0 + kj, dt * mu[j - 1], -kappa[j]);
         if (rc) return rc;
         std::swap(cur, old);
     }
@@ -656,8 +772,6 @@ int finish_grad(gw_ctx *c, double dt, int nsteps, double wE, double *grad) {
 }
 
 int check_common(gw_ctx *c, double dt, int max_stages, int *s) {
-    if (c->precision != GW_PREC_FP64)
-        return gw_fail(GW_ERR_UNSUPPORTED, "the adjoint runs on GW_PREC_FP64 contexts");
     if (!(dt > 0) || !std::isfinite(dt)) return gw_fail(GW_ERR_ARG, "dt must be positive and finite");
     int covered, rc;
     GW_CUDA(cudaSetDevice(c->device));
@@ -667,72 +781,52 @@ int check_common(gw_ctx *c, double dt, int max_stages, int *s) {
 }
 
 struct DevBlock {
-    double *p = nullptr;
+    void *p = nullptr;
     ~DevBlock() { if (p) cudaFree(p); }
 };
 
-}  // namespace
+template <typename T>
+T *state_of(gw_ctx *c);
+template <>
+double *state_of<double>(gw_ctx *c) { return c->d_u; }
+template <>
+float *state_of<float>(gw_ctx *c) { return c->f_u; }
 
-void gw_adjoint_release(gw_ctx *c) {
-    if (!c || !c->adj) return;
-    for (void *p : c->adj->allocs) if (p) cudaFree(p);
-    delete c->adj;
-    c->adj = nullptr;
-}
-
-extern "C" int gw_step_vjp(gw_ctx *c, const double *u, double *lam, double dt, int max_stages,
-                           double w_energy, double w_outlet, double *grad) {
-    if (!c || !u || !lam || !grad) return gw_fail(GW_ERR_ARG, "NULL argument");
-    if ((const void *)u == (const void *)lam) return gw_fail(GW_ERR_ARG, "lam must not alias u");
-    int s, rc;
-    if ((rc = check_common(c, dt, max_stages, &s))) return rc;
+// The checkpointed adjoint for one storage type (see gw_adjoint).
+template <typename T>
+int adjoint_run(gw_ctx *c, double dt, int nsteps, int max_stages, int s, int checkpoint_every, double w_energy,
+                double w_outlet, double *grad, double *grad_T0, gw_adjoint_info_t *info) {
     const size_t N = (size_t)c->nx * c->ny * c->nz;
-    const int nbuf = (s - 1) + 5 + 2 + 1;
-    DevBlock blk;
-    cudaError_t e = cudaMalloc((void **)&blk.p, (size_t)nbuf * N * sizeof(double));
-    if (e != cudaSuccess) return gw_cuda_fail(e, "cudaMalloc (step adjoint buffers)");
-    double *p = blk.p;
-    StepStore S;
-    for (int q = 0; q < s - 1; ++q, p += N) S.g.push_back(p);
-    S.ustar = p; p += N; S.tA = p; p += N; S.u1 = p; p += N; S.tC = p; p += N; S.work = p; p += N;
-    double *B[3] = {lam, p, p + N};
-    double *un1 = p + 2 * N;
-    if ((rc = zero_acc(c)) || (rc = forward_store(c, u, S, dt, s, un1))) return rc;
-    const double c_w = c->rho_c_water / kRhoWater;
-    const double ob_scale = c->inlet_kind == GW_INLET_CONSTANT ? w_energy * c_w * dt : 0.0;
-    int res = 0;
-    if ((rc = adjoint_step(c, u, un1, S, B, dt, s, ob_scale, w_outlet, &res))) return rc;
-    if (res != 0) GW_CUDA(cudaMemcpyAsync(lam, B[res], N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-    return finish_grad(c, dt, 1, w_energy, grad);
-}
-
-extern "C" int gw_adjoint(gw_ctx *c, double dt, int nsteps, int max_stages, int checkpoint_every,
-                          double w_energy, double w_outlet, double *grad, double *grad_T0,
-                          gw_adjoint_info_t *info) {
-    if (!c || !grad) return gw_fail(GW_ERR_ARG, "NULL argument");
-    if (nsteps < 1) return gw_fail(GW_ERR_ARG, "nsteps must be >= 1");
-    if (checkpoint_every < 1) return gw_fail(GW_ERR_ARG, "checkpoint_every must be >= 1");
-    int s, rc;
-    if ((rc = check_common(c, dt, max_stages, &s))) return rc;
-    const size_t N = (size_t)c->nx * c->ny * c->nz;
-    const size_t bytes = N * sizeof(double);
+    const size_t bytes = N * sizeof(T);
+    const bool mix = sizeof(T) == 4;
+    const int ncol = c->n_inner + c->n_outer;
+    const size_t tpn = (size_t)std::max(ncol, 1) * c->nz;
     const int K = std::min(checkpoint_every, nsteps);
     const int nseg = (nsteps + K - 1) / K;
     // checkpoints, one segment's states, the step store, adjoint buffers, final state
-    const size_t nbuf = (size_t)nseg + (K + 1) + (s - 1) + 5 + 3 + 1;
+    const size_t nbuf = (size_t)nseg + (K + 1) + (s - 1) + (mix ? 2 : 5) + 3 + 1;
+    const size_t total = nbuf * bytes + (mix ? 2 * tpn * sizeof(T) : 0);
     DevBlock blk;
-    cudaError_t e = cudaMalloc((void **)&blk.p, nbuf * bytes);
+    cudaError_t e = cudaMalloc(&blk.p, total);
     if (e != cudaSuccess) return gw_cuda_fail(e, "cudaMalloc (adjoint checkpoints and buffers)");
-    double *p = blk.p;
-    std::vector<double *> ckpt(nseg), seg(K + 1);
+    T *p = (T *)blk.p;
+    std::vector<T *> ckpt(nseg), seg(K + 1);
     for (int q = 0; q < nseg; ++q, p += N) ckpt[q] = p;
     for (int q = 0; q <= K; ++q, p += N) seg[q] = p;
-    StepStore S;
+    StepStore<T> S;
     for (int q = 0; q < s - 1; ++q, p += N) S.g.push_back(p);
-    S.ustar = p; p += N; S.tA = p; p += N; S.u1 = p; p += N; S.tC = p; p += N; S.work = p; p += N;
-    double *B[3] = {p, p + N, p + 2 * N};
+    S.ustar = p; p += N; S.u1 = p; p += N;
+    if (!mix) { S.tA = p; p += N; S.tC = p; p += N; S.work = p; p += N; }
+    else { S.tA = S.tC = S.work = nullptr; }
+    T *B[3] = {p, p + N, p + 2 * N};
     p += 3 * N;
-    double *uN = p;
+    T *uN = p;
+    p += N;
+    S.tpA = mix ? p : nullptr;
+    S.tpC = mix ? p + tpn : nullptr;
+    S.pA = {S.tA, S.tpA, mix ? c->d_Tref : nullptr, c->d_pipe_i, c->d_pipe_j, c->ny, c->nz};
+    S.pC = {S.tC, S.tpC, mix ? c->d_Tref : nullptr, c->d_pipe_i, c->d_pipe_j, c->ny, c->nz};
+    T *u = state_of<T>(c);
 
     cudaEvent_t e0, e1, e2;
     GW_CUDA(cudaEventCreate(&e0));
@@ -746,12 +840,13 @@ extern "C" int gw_adjoint(gw_ctx *c, double dt, int nsteps, int max_stages, int 
     GW_CUDA(cudaStreamSynchronize(c->stream));
     GW_CUDA(cudaMemsetAsync(c->d_energy, 0, sizeof(double) * c->nbh, c->stream));
     GW_CUDA(cudaEventRecord(e0, c->stream));
+    int rc;
     for (int q = 0; q < nseg; ++q) {
-        GW_CUDA(cudaMemcpyAsync(ckpt[q], c->d_u, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        GW_CUDA(cudaMemcpyAsync(ckpt[q], u, bytes, cudaMemcpyDeviceToDevice, c->stream));
         const int n = std::min(K, nsteps - q * K);
         if ((rc = gw_step(c, (double)q * K * dt, dt, n, max_stages))) return rc;
     }
-    GW_CUDA(cudaMemcpyAsync(uN, c->d_u, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    GW_CUDA(cudaMemcpyAsync(uN, u, bytes, cudaMemcpyDeviceToDevice, c->stream));
     GW_CUDA(cudaEventRecord(e1, c->stream));
     GW_CUDA(cudaMemcpyAsync(E.data(), c->d_energy, sizeof(double) * c->nbh, cudaMemcpyDeviceToHost, c->stream));
     GW_CUDA(cudaMemcpyAsync(O.data(), c->d_outlet, sizeof(double) * c->nbh, cudaMemcpyDeviceToHost, c->stream));
@@ -767,24 +862,31 @@ extern "C" int gw_adjoint(gw_ctx *c, double dt, int nsteps, int max_stages, int 
     for (int q = nseg - 1; q >= 0; --q) {
         const int n = std::min(K, nsteps - q * K);
         GW_CUDA(cudaMemcpyAsync(seg[0], ckpt[q], bytes, cudaMemcpyDeviceToDevice, c->stream));
-        GW_CUDA(cudaMemcpyAsync(c->d_u, ckpt[q], bytes, cudaMemcpyDeviceToDevice, c->stream));
+        GW_CUDA(cudaMemcpyAsync(u, ckpt[q], bytes, cudaMemcpyDeviceToDevice, c->stream));
         for (int m = 1; m <= n; ++m) {
             if ((rc = gw_step(c, (double)(q * K + m - 1) * dt, dt, 1, max_stages))) return rc;
-            GW_CUDA(cudaMemcpyAsync(seg[m], c->d_u, bytes, cudaMemcpyDeviceToDevice, c->stream));
+            GW_CUDA(cudaMemcpyAsync(seg[m], u, bytes, cudaMemcpyDeviceToDevice, c->stream));
         }
         for (int m = n - 1; m >= 0; --m) {
             const bool last = q * K + m == nsteps - 1;
             int res = 0;
-            if ((rc = forward_store(c, seg[m], S, dt, s, nullptr)) ||
-                (rc = adjoint_step(c, seg[m], seg[m + 1], S, B, dt, s, ob_scale, last ? w_outlet : 0.0, &res)))
+            if ((rc = forward_store(c, seg[m], S, dt, s, (T *)nullptr)) ||
+                (rc = adjoint_step<T>(c, seg[m], seg[m + 1], S, B, dt, s, ob_scale, last ? w_outlet : 0.0, &res)))
                 return rc;
             if (res != 0) std::swap(B[0], B[res]);
         }
     }
     GW_CUDA(cudaEventRecord(e2, c->stream));
-    if (grad_T0) GW_CUDA(cudaMemcpyAsync(grad_T0, B[0], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    if (grad_T0) {
+        if (mix) {
+            k_to_double<<<nblocks((long long)N, kB), kB, 0, c->stream>>>(grad_T0, (const float *)B[0], (long long)N);
+            GW_CUDA(cudaGetLastError());
+        } else {
+            GW_CUDA(cudaMemcpyAsync(grad_T0, B[0], bytes, cudaMemcpyDeviceToDevice, c->stream));
+        }
+    }
     // leave the context as gw_step over nsteps would (field, outlet, energy)
-    GW_CUDA(cudaMemcpyAsync(c->d_u, uN, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    GW_CUDA(cudaMemcpyAsync(u, uN, bytes, cudaMemcpyDeviceToDevice, c->stream));
     for (int b = 0; b < c->nbh; ++b) E[b] += E0[b];
     GW_CUDA(cudaMemcpyAsync(c->d_energy, E.data(), sizeof(double) * c->nbh, cudaMemcpyHostToDevice, c->stream));
     GW_CUDA(cudaMemcpyAsync(c->d_outlet, O.data(), sizeof(double) * c->nbh, cudaMemcpyHostToDevice, c->stream));
@@ -801,7 +903,62 @@ extern "C" int gw_adjoint(gw_ctx *c, double dt, int nsteps, int max_stages, int 
         info->checkpoints = nseg;
         info->forward_ms = f_ms;
         info->reverse_ms = r_ms;
-        info->peak_bytes = c->device_bytes + c->adj->bytes + (long long)(nbuf * bytes);
+        info->peak_bytes = c->device_bytes + c->adj->bytes + (long long)total;
     }
     return GW_OK;
+}
+
+}  // namespace
+
+void gw_adjoint_release(gw_ctx *c) {
+    if (!c || !c->adj) return;
+    for (void *p : c->adj->allocs) if (p) cudaFree(p);
+    delete c->adj;
+    c->adj = nullptr;
+}
+
+extern "C" int gw_step_vjp(gw_ctx *c, const double *u, double *lam, double dt, int max_stages,
+                           double w_energy, double w_outlet, double *grad) {
+    if (!c || !u || !lam || !grad) return gw_fail(GW_ERR_ARG, "NULL argument");
+    if ((const void *)u == (const void *)lam) return gw_fail(GW_ERR_ARG, "lam must not alias u");
+    if (c->precision != GW_PREC_FP64)
+        return gw_fail(GW_ERR_UNSUPPORTED, "gw_step_vjp works on double fields of a GW_PREC_FP64 context");
+    int s, rc;
+    if ((rc = check_common(c, dt, max_stages, &s))) return rc;
+    const size_t N = (size_t)c->nx * c->ny * c->nz;
+    const int nbuf = (s - 1) + 5 + 2 + 1;
+    DevBlock blk;
+    cudaError_t e = cudaMalloc(&blk.p, (size_t)nbuf * N * sizeof(double));
+    if (e != cudaSuccess) return gw_cuda_fail(e, "cudaMalloc (step adjoint buffers)");
+    double *p = (double *)blk.p;
+    StepStore<double> S;
+    for (int q = 0; q < s - 1; ++q, p += N) S.g.push_back(p);
+    S.ustar = p; p += N; S.tA = p; p += N; S.u1 = p; p += N; S.tC = p; p += N; S.work = p; p += N;
+    S.tpA = S.tpC = nullptr;
+    S.pA = {S.tA, nullptr, nullptr, c->d_pipe_i, c->d_pipe_j, c->ny, c->nz};
+    S.pC = {S.tC, nullptr, nullptr, c->d_pipe_i, c->d_pipe_j, c->ny, c->nz};
+    double *B[3] = {lam, p, p + N};
+    double *un1 = p + 2 * N;
+    if ((rc = zero_acc(c)) || (rc = forward_store(c, u, S, dt, s, un1))) return rc;
+    const double c_w = c->rho_c_water / kRhoWater;
+    const double ob_scale = c->inlet_kind == GW_INLET_CONSTANT ? w_energy * c_w * dt : 0.0;
+    int res = 0;
+    if ((rc = adjoint_step<double>(c, u, un1, S, B, dt, s, ob_scale, w_outlet, &res))) return rc;
+    if (res != 0) GW_CUDA(cudaMemcpyAsync(lam, B[res], N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    return finish_grad(c, dt, 1, w_energy, grad);
+}
+
+extern "C" int gw_adjoint(gw_ctx *c, double dt, int nsteps, int max_stages, int checkpoint_every,
+                          double w_energy, double w_outlet, double *grad, double *grad_T0,
+                          gw_adjoint_info_t *info) {
+    if (!c || !grad) return gw_fail(GW_ERR_ARG, "NULL argument");
+    if (nsteps < 1) return gw_fail(GW_ERR_ARG, "nsteps must be >= 1");
+    if (checkpoint_every < 1) return gw_fail(GW_ERR_ARG, "checkpoint_every must be >= 1");
+    int s, rc;
+    if ((rc = check_common(c, dt, max_stages, &s))) return rc;
+    if (c->precision == GW_PREC_MIXED)
+        return adjoint_run<float>(c, dt, nsteps, max_stages, s, checkpoint_every, w_energy, w_outlet, grad,
+                                  grad_T0, info);
+    return adjoint_run<double>(c, dt, nsteps, max_stages, s, checkpoint_every, w_energy, w_outlet, grad, grad_T0,
+                               info);
 }

@@ -1069,6 +1069,29 @@ int gw_fused_set_dt(gw_ctx *c, double dt) {
     return GW_OK;
 }
 
+// The first half of a step for the adjoint's forward store: ROCK2 columns on
+// u (u <- u*), the pipe pass of the explicit y sweep, the x half step into
+// temp (temp <- u1) and the pipe pass of the explicit x sweep (outlet of
+// the step's second advection); the swept pipe columns of both passes
+// ([column][level], as k_pipe_sweep leaves them) are copied to tpA / tpC.
+template <typename T>
+int adjoint_store(gw_ctx *c, double dt, int s, T *tpA, T *tpC) {
+    Bufs<T> B = bufs<T>(c);
+    const size_t tb = (size_t)(c->n_inner + c->n_outer) * c->nz * sizeof(T);
+    int rc;
+    if ((rc = launch_rock2<T>(c, s)) || (rc = launch_pipe<T>(c, B.u, GW_DIR_Y, dt / 2))) return rc;
+    if (tb) GW_CUDA(cudaMemcpyAsync(tpA, B.tp, tb, cudaMemcpyDeviceToDevice, c->stream));
+    if ((rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2)) || (rc = launch_pipe<T>(c, B.temp, GW_DIR_X, dt / 2)))
+        return rc;
+    if (tb) GW_CUDA(cudaMemcpyAsync(tpC, B.tp, tb, cudaMemcpyDeviceToDevice, c->stream));
+    return GW_OK;
+}
+
+int gw_fused_adjoint_store(gw_ctx *c, double dt, int s, void *tpA, void *tpC) {
+    return c->precision == GW_PREC_MIXED ? adjoint_store<float>(c, dt, s, (float *)tpA, (float *)tpC)
+                                         : adjoint_store<double>(c, dt, s, (double *)tpA, (double *)tpC);
+}
+
 int gw_fused_step(gw_ctx *c, double dt, int s) {
     return c->precision == GW_PREC_MIXED ? fused_step<float>(c, dt, s) : fused_step<double>(c, dt, s);
 }

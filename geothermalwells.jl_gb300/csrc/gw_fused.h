@@ -11,6 +11,10 @@ int gw_fused_set_dt(gw_ctx *c, double dt);
 // Enqueue one full step (ROCK2 columns, two half steps, record) on c->stream.
 // Requires the Thomas factors for dt/2 and the stage table c->d_stage for s.
 int gw_fused_step(gw_ctx *c, double dt, int s);
+// The adjoint's forward store: ROCK2 and the first half step on the
+// context's state (u <- u*, temp <- u1), with the swept pipe columns of the
+// step's two pipe passes copied to tpA / tpC ([column][level], storage type).
+int gw_fused_adjoint_store(gw_ctx *c, double dt, int s, void *tpA, void *tpC);
 // Enqueue one kernel class of the step (GW_KERNEL_*), for timing.
 int gw_fused_time_part(gw_ctx *c, double dt, int s, int part);
 // Mixed path: upload a double field as theta / download theta as a double

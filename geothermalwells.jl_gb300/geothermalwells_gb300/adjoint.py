@@ -46,8 +46,9 @@ def _split(cache, g):
 def adjoint(cache, T0, dt, nsteps, *, max_stages=100, checkpoint_every=64, w_energy=1.0,
             w_outlet=0.0, want_T0=False):
     """J and its gradient over ``nsteps`` steps of size ``dt`` from the field
-    ``T0`` (host array, (Nz, Ny, Nx)).  The cache must be an FP64 cache; it
-    is left at the final state, as after the forward solve."""
+    ``T0`` (host array, (Nz, Ny, Nx)).  FP64 caches run the adjoint in double,
+    mixed caches with float adjoint fields over the mixed step.  The cache is
+    left at the final state, as after the forward solve."""
     L = _lib.load()
     cache.set_field(T0)
     npar = len(cache.materials.k_rock_layers) + cache.N_bh + 1
@@ -89,7 +90,8 @@ class Design:
     material templates, inlet kind, initial field and step schedule."""
 
     def __init__(self, gridx, gridy, gridz, boreholes, materials, inlet_model, T0, dt, nsteps,
-                 device=0, checkpoint_every=64, w_energy=1.0, w_outlet=0.0, max_stages=100):
+                 device=0, checkpoint_every=64, w_energy=1.0, w_outlet=0.0, max_stages=100,
+                 precision="fp64"):
         self.gridx, self.gridy, self.gridz = gridx, gridy, gridz
         self.boreholes = tuple(boreholes)
         self.materials = materials
@@ -100,6 +102,7 @@ class Design:
         self.checkpoint_every = int(checkpoint_every)
         self.w_energy, self.w_outlet = float(w_energy), float(w_outlet)
         self.max_stages = int(max_stages)
+        self.precision = precision
 
     def cache(self, k_layers, mdot, inlet_param):
         m = self.materials
@@ -108,7 +111,7 @@ class Design:
         bhs = tuple(b.with_flow(float(q)) for b, q in zip(self.boreholes, mdot))
         inlet = (ConstantInlet(float(inlet_param)) if self.inlet_model.kind == 0
                  else HeatExchangerInlet(float(inlet_param)))
-        return create_cache(backend=GB300(device=self.device, precision="fp64"), gridx=self.gridx,
+        return create_cache(backend=GB300(device=self.device, precision=self.precision), gridx=self.gridx,
                             gridy=self.gridy, gridz=self.gridz, materials=mat, boreholes=bhs,
                             inlet_model=inlet)
 

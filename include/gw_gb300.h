@@ -220,7 +220,9 @@ int gw_advection_noalloc(gw_ctx *ctx, double *phi_dev, double dt, double t, doub
 /* ---- adjoint: reverse-mode gradients of the time-step map ----
  * No counterpart in the reference, which has no derivatives: these are the
  * kernels a ChainRulesCore rrule over the solve (the Julia side of a
- * torch.autograd.Function) calls.  GW_PREC_FP64 contexts only.
+ * torch.autograd.Function) calls.  GW_PREC_FP64 contexts run it in double;
+ * GW_PREC_MIXED contexts keep float adjoint fields over the float states of
+ * the mixed step (gradient sums in double). 
  *
  * Objective over the steps n = 0 .. nsteps-1 of size dt:
  *   J = sum_b [ w_energy * E_b + w_outlet * T_out,b(last step) ],
@@ -255,7 +257,8 @@ int gw_adjoint(gw_ctx *ctx, double dt, int nsteps, int max_stages, int checkpoin
  * dJ/du^{n+1} on entry, lam_dev = dJ/du^n on return, where J includes this
  * step's objective terms (w_energy * its energy, w_outlet * its outlet
  * temperature); grad[n_params] is accumulated into (+=).  The context's
- * field is not touched.  For callers that drive the time loop themselves. */
+ * field is not touched.  For callers that drive the time loop themselves;
+ * double fields, GW_PREC_FP64 contexts. */
 int gw_step_vjp(gw_ctx *ctx, const double *u_dev, double *lam_dev, double dt, int max_stages,
                 double w_energy, double w_outlet, double *grad);
 

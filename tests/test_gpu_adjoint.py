@@ -176,11 +176,42 @@ def test_autograd_function(gwlib, torch_cuda):
     assert abs(float(t.grad) - r.dinlet) <= 1e-12 * abs(r.dinlet)
 
 
-def test_mixed_context_is_refused(gwlib):
+def mixed_cache(w):
+    return create_cache(backend=GB300(precision="mixed"), gridx=w["gridx"], gridy=w["gridy"],
+                        gridz=w["gridz"], materials=w["materials"], boreholes=w["boreholes"],
+                        inlet_model=w["inlet_model"])
+
+
+MIXED_RTOL = 1e-3   # float adjoint fields over the mixed step, against the double adjoint
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_mixed_adjoint_against_fp64_adjoint(name, gwlib):
+    """The mixed path's adjoint (float fields, double sums) against the FP64
+    GPU adjoint and the oracle's central differences."""
+    kw, obj = CASES[name]
+    w = W.adjoint_small(**kw)
+    r64 = A.adjoint(fp64_cache(w), w["T0"], w["dt"], w["nsteps"], checkpoint_every=5, **obj)
+    r32 = A.adjoint(mixed_cache(w), w["T0"], w["dt"], w["nsteps"], checkpoint_every=5, **obj)
+    scale = np.max(np.abs(r64.grad))
+    err = np.abs(r32.grad - r64.grad)
+    assert np.all(err <= MIXED_RTOL * np.abs(r64.grad) + 1e-6 * scale), (r32.grad, r64.grad, err / np.abs(r64.grad))
+    assert abs(r32.objective - r64.objective) <= 1e-5 * abs(r64.objective)
+
+
+def test_mixed_initial_field_gradient(gwlib, torch_cuda):
+    """dJ/du^0 of the mixed adjoint against the FP64 one."""
+    w = W.adjoint_small(n_layers=3)
+    r64 = A.adjoint(fp64_cache(w), w["T0"], w["dt"], 6, checkpoint_every=4, want_T0=True)
+    r32 = A.adjoint(mixed_cache(w), w["T0"], w["dt"], 6, checkpoint_every=4, want_T0=True)
+    assert np.max(np.abs(r32.dT0 - r64.dT0)) <= 1e-3 * np.max(np.abs(r64.dT0))
+
+
+def test_step_vjp_needs_fp64_context(gwlib, torch_cuda):
+    torch = torch_cuda
     w = W.adjoint_small()
-    cache = create_cache(backend=GB300(precision="mixed"), gridx=w["gridx"], gridy=w["gridy"],
-                         gridz=w["gridz"], materials=w["materials"], boreholes=w["boreholes"],
-                         inlet_model=w["inlet_model"])
+    cache = mixed_cache(w)
+    d = torch.zeros(cache.N, dtype=torch.float64, device="cuda")
     with pytest.raises(_lib.GWError) as e:
-        A.adjoint(cache, w["T0"], w["dt"], 2)
+        A.step_vjp(cache, d, d.clone(), w["dt"])
     assert e.value.code == _lib.GW_ERR_UNSUPPORTED
