@@ -434,8 +434,10 @@ def run_ensemble(args):
 def run_adjoint(args):
     """Gradient workload: d(extracted heat over 7 days)/d(22 rock layer
     conductivities, flow rate, inlet temperature) on the 205 x 205 x 2002 well
-    (3024 steps of 200 s, FP64), checkpoints every 64 steps.  Reports the
-    adjoint's device time as a multiple of one forward solve, the device
+    (3024 steps of 200 s), checkpoints every 64 steps, in the selected
+    precision (mixed: float adjoint fields over the mixed step), with the FP64
+    adjoint beside it (--no-compare skips it).  Reports the adjoint's device
+    time as a multiple of one forward solve of the same precision, the device
     memory it holds, and central differences (h = 1e-4 relative) of the FP64
     forward solve: --fd some checks the largest and the median layer
     gradient, the flow rate, the inlet temperature and one random direction
@@ -443,7 +445,7 @@ def run_adjoint(args):
     takes central differences at h = 1e-4 and h / 2 (relative) and their
     Richardson extrapolation; the adjoint must be within 1e-4 of the latter
     (plus the differences' rounding floor, 16 eps |J| / h)."""
-    from geothermalwells_gb300 import GB300, create_cache, _lib
+    from geothermalwells_gb300 import _lib
     from geothermalwells_gb300 import adjoint as A
     from geothermalwells_gb300 import workloads as W
     L = _lib.load()
@@ -451,14 +453,17 @@ def run_adjoint(args):
     dt = args.dt if args.dt > 0 else w["dt"]
     nsteps = args.adjoint_steps or w["nsteps"]
     K = w["checkpoint_every"]
-    design = A.Design(w["gridx"], w["gridy"], w["gridz"], w["boreholes"], w["materials"],
-                      w["inlet_model"], w["T0"], dt, nsteps, checkpoint_every=K)
+
+    def design(prec):
+        return A.Design(w["gridx"], w["gridy"], w["gridz"], w["boreholes"], w["materials"],
+                        w["inlet_model"], w["T0"], dt, nsteps, checkpoint_every=K, precision=prec)
+
     p0 = np.concatenate([w["materials"].k_rock_layers, [b.mdot for b in w["boreholes"]],
                          [w["inlet_model"].param]])
     nl = len(w["materials"].k_rock_layers)
 
-    def forward(p):
-        c = design.cache(p[:nl], p[nl:-1], p[-1])
+    def forward(p, prec="fp64"):
+        c = design(prec).cache(p[:nl], p[nl:-1], p[-1])
         try:
             c.set_field(w["T0"])
             _lib.check(L.gw_reset_energy(c.ctx))
@@ -471,15 +476,25 @@ def run_adjoint(args):
         finally:
             c.close()
 
-    cache = design.cache(p0[:nl], p0[nl:-1], p0[-1])
-    cache.set_field(w["T0"])
-    _lib.check(L.gw_step(cache.ctx, 0.0, dt, 4, 100))     # warm-up (graph capture, tables)
-    J_fwd, fwd_ms = forward(p0)
-    clocks = Clocks(0)
-    r = A.adjoint(cache, w["T0"], dt, nsteps, checkpoint_every=K)
-    ck = clocks.stop()
-    cache.close()
+    def run_adj(prec):
+        cache = design(prec).cache(p0[:nl], p0[nl:-1], p0[-1])
+        cache.set_field(w["T0"])
+        _lib.check(L.gw_step(cache.ctx, 0.0, dt, 4, 100))     # warm-up (graph capture, tables)
+        J_fwd, fwd_ms = forward(p0, prec)
+        clocks = Clocks(0)
+        r = A.adjoint(cache, w["T0"], dt, nsteps, checkpoint_every=K)
+        ck = clocks.stop()
+        cache.close()
+        return r, J_fwd, fwd_ms, ck
+
+    prec = args.precision
+    r, J_fwd, fwd_ms, ck = run_adj(prec)
     g = r.grad
+    g64 = None
+    if prec != "fp64" and not args.no_compare:
+        r64, J64, fwd64_ms, _ = run_adj("fp64")
+        g64 = r64.grad
+    J_ref = J_fwd if g64 is None else J64
     if args.fd == "all":
         idx = list(range(len(p0)))
     elif args.fd == "some":
@@ -490,51 +505,64 @@ def run_adjoint(args):
     eps = np.finfo(np.float64).eps
 
     def central(d, hs):
-        """Central difference of J along p0 * (1 + hs d)."""
+        """Central difference of the FP64 J along p0 * (1 + hs d)."""
         return (forward(p0 * (1 + hs * d))[0] - forward(p0 * (1 - hs * d))[0]) / (2 * hs)
 
-    def check(d, a):
-        """Directional derivative a = g . (p0 * d) against central differences
-        at h = 1e-4 and h / 2 and their Richardson extrapolation (which
-        removes the h^2 term: J is strongly curved in the flow rate, whose
-        h = 1e-4 difference alone carries a ~1e-3 truncation error)."""
+    def check(d):
+        """Directional derivative g . (p0 * d) against central differences at
+        h = 1e-4 and h / 2 and their Richardson extrapolation (which removes
+        the h^2 term: J is strongly curved in the flow rate, whose h = 1e-4
+        difference alone carries a ~1e-3 truncation error)."""
         f1, f2 = central(d, 1e-4), central(d, 5e-5)
         rich = (4 * f2 - f1) / 3
-        floor = 16 * eps * abs(J_fwd) / 1e-4
-        return {"adjoint": a, "fd_h": f1, "fd_h2": f2, "fd_richardson": rich,
-                "rel_err_fd_h": abs(a - f1) / abs(f1) if f1 else None,
-                "rel_err_richardson": abs(a - rich) / abs(rich) if rich else None,
-                "ok": bool(abs(a - rich) <= 1e-4 * abs(rich) + floor)}
+        floor = 16 * eps * abs(J_ref) / 1e-4
+        out = {"fd_h": f1, "fd_h2": f2, "fd_richardson": rich}
+        for tag, gg in (("adjoint", g), ("adjoint_fp64", g64)):
+            if gg is None:
+                continue
+            a = float(np.dot(gg, p0 * d))
+            out[tag] = a
+            out["rel_err_" + tag] = abs(a - rich) / abs(rich) if rich else None
+            out["ok_" + tag] = bool(abs(a - rich) <= 1e-4 * abs(rich) + floor)
+        return out
 
     checks = {}
     for i in idx:
         d = np.zeros(len(p0))
         d[i] = 1.0
-        checks[str(i)] = check(d, float(g[i] * p0[i]))
+        checks[str(i)] = check(d)
     if args.fd != "none":
-        d = np.random.default_rng(7).choice([-1.0, 1.0], len(p0))
-        checks["direction"] = check(d, float(np.dot(g, p0 * d)))
-    ok = all(v["ok"] for v in checks.values())
+        checks["direction"] = check(np.random.default_rng(7).choice([-1.0, 1.0], len(p0)))
+    ok = all(v["ok_adjoint"] for v in checks.values())
     finite = bool(np.isfinite(r.objective) and np.all(np.isfinite(g)))
     cells = len(w["gridx"]) * len(w["gridy"]) * len(w["gridz"])
     adj_ms = r.forward_ms + r.reverse_ms
+    compare = None
+    if g64 is not None:
+        rel = np.abs(g - g64) / np.maximum(np.abs(g64), 1e-300)
+        big = np.abs(g64) > 1e-6 * np.max(np.abs(g64))
+        compare = {"precision": "fp64", "grad": [float(v) for v in g64],
+                   "objective_J": r64.objective,
+                   "adjoint_ms": r64.forward_ms + r64.reverse_ms, "forward_ms": fwd64_ms,
+                   "max_rel_diff_mixed_vs_fp64": float(np.max(rel[big])),
+                   "peak_device_gb": r64.peak_bytes / 1e9}
     line = {"metric": "adjoint cost (multiple of one forward solve)", "value": adj_ms / fwd_ms,
             "unit": "x", "n_gpus": 1, "steps": nsteps, "higher_is_better": False,
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32+f64acc", "data": "synthetic",
             "config": {"workload": w["name"], "cells": cells, "dt_s": dt, "checkpoint_every": K,
-                       "checkpoints": r.checkpoints, "stages": r.stages,
+                       "checkpoints": r.checkpoints, "stages": r.stages, "precision": prec,
                        "params": "k_rock_layers[22], mdot, T_inlet"},
             "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "adjoint_forward_sweep_ms": r.forward_ms,
             "adjoint_reverse_ms": r.reverse_ms,
             "forward_mcell_steps_per_s": cells * nsteps / (fwd_ms / 1e3) / 1e6,
             "peak_device_gb": r.peak_bytes / 1e9, "objective_J": r.objective,
             "objective_forward_J": J_fwd, "grad": [float(v) for v in g],
-            "fd_check": {"h_rel": 1e-4, "derivatives": "d J / d ln p (p * dJ/dp)", "checks": checks,
-                         "max_rel_err_richardson": max([v["rel_err_richardson"] for v in checks.values()
-                                                        if v["rel_err_richardson"] is not None], default=None),
+            "fd_check": {"h_rel": 1e-4, "of": "FP64 forward solve",
+                         "derivatives": "d J / d ln p (p * dJ/dp)", "checks": checks,
+                         "max_rel_err_richardson": max([v["rel_err_adjoint"] for v in checks.values()
+                                                        if v.get("rel_err_adjoint") is not None], default=None),
                          "within_1e-4": bool(ok)},
-            "finite": finite,
-            "clocks": ck}
+            "compare": compare, "finite": finite, "clocks": ck}
     print(json.dumps(line), flush=True)
 
 

@@ -170,7 +170,7 @@ def test_autograd_function(gwlib, torch_cuda):
     J.backward()
     r = d.run(p[:3], p[3:4], p[4])
     # two separate solves: the gradient sums use atomics, so equal to rounding
-    assert abs(float(J) - r.objective) <= 1e-12 * abs(r.objective)
+    assert abs(J.item() - r.objective) <= 1e-12 * abs(r.objective)
     assert np.allclose(k.grad.numpy(), r.dk_layers, rtol=1e-12, atol=0)
     assert np.allclose(m.grad.numpy(), r.dmdot, rtol=1e-12, atol=0)
     assert abs(float(t.grad) - r.dinlet) <= 1e-12 * abs(r.dinlet)
