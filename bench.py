@@ -128,6 +128,19 @@ def dist_init(args):
     return 0, 1, 0, None
 
 
+def reduce_replicas(dist, t_ms, units, device="cuda"):
+    """Whole-job figures of independent replicas (one per rank, no data
+    exchange): the slowest rank's time and the units all ranks processed."""
+    if not dist:
+        return t_ms, float(units)
+    import torch
+    t = torch.tensor([t_ms], dtype=torch.float64, device=device)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
 def cpu_baseline(w, sample_steps):
     """The oracle (CPU FP64 restatement of the reference) on all host cores,
     timed on a bounded sample: sample_steps full time steps of the workload."""
@@ -191,13 +204,8 @@ def run_ours(args):
     ms = ctypes.c_double()
     _lib.check(L.gw_get_last_step_time(cache.ctx, ctypes.byref(ms)))
     ck = clocks.stop()
-    t_ms = ms.value
-    if dist:
-        import torch
-        tt = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ms = float(tt.item())
-    value = ncell * args.steps * world / (t_ms / 1e3) / 1e6
+    t_ms, units = reduce_replicas(dist, ms.value, ncell * args.steps)
+    value = units / (t_ms / 1e3) / 1e6
 
     # per-kernel timing for the roofline of the dominant kernel
     prof = (ctypes.c_double * len(_lib.KERNELS))()
@@ -237,13 +245,8 @@ def run_ours(args):
     _lib.check(L.gw_step(cache.ctx, 0.0, dt, args.steps, 100))
     _lib.check(L.gw_get_outlet_series(cache.ctx, _lib.dptr(series), args.steps))
     _lib.check(L.gw_get_field(cache.ctx, _lib.dptr(out_pin)))
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        import torch
-        tt = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e = {"value": ncell * args.steps * world / e2e_s / 1e6, "unit": METRIC,
+    e2e_ms, e2e_units = reduce_replicas(dist, (time.perf_counter() - t0) * 1e3, ncell * args.steps)
+    e2e = {"value": e2e_units / (e2e_ms / 1e3) / 1e6, "unit": METRIC,
            "h2d_bytes_per_step": 8 * ncell / args.steps,
            "d2h_bytes_per_step": (8 * ncell + 8 * args.steps * cache.N_bh) / args.steps,
            "path": "gw_set_field + gw_step(K) + gw_get_outlet_series + gw_get_field, pinned host"}
@@ -260,7 +263,8 @@ def run_ours(args):
         oms = ctypes.c_double()
         _lib.check(L.gw_get_last_step_time(oc.ctx, ctypes.byref(oms)))
         oc.close()
-        ov = ncell * args.steps * world / (oms.value / 1e3) / 1e6
+        o_ms, o_units = reduce_replicas(dist, oms.value, ncell * args.steps)
+        ov = o_units / (o_ms / 1e3) / 1e6
         other = {"precision": oprec, "value": ov, "ms_per_step": oms.value / args.steps,
                  "ratio_mixed_over_fp64": (value / ov) if args.precision == "mixed" else (ov / value)}
     if rank != 0:
