@@ -254,6 +254,31 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
     std::stable_sort(order.begin(), order.end(),
                      [&](int x, int y) { return c->colprof[x] < c->colprof[y]; });
     if ((rc = upload(c, &c->d_colorder, order))) return fail(rc);
+    {
+        // rows holding pipe columns; their +-1 neighbourhood first
+        const int ncol = c->n_inner + c->n_outer;
+        if (ncol > 0) {
+            c->jlo = *std::min_element(c->pipe_j.begin(), c->pipe_j.end());
+            c->jhi = *std::max_element(c->pipe_j.begin(), c->pipe_j.end());
+        }
+        std::vector<int> ab;
+        ab.reserve(order.size());
+        auto in_a = [&](int q) {
+            const int j = q % c->ny;
+            return ncol > 0 && j >= c->jlo - 1 && j <= c->jhi + 1;
+        };
+        for (int q : order) if (in_a(q)) ab.push_back(q);
+        c->ncol_a = (int)ab.size();
+        for (int q : order) if (!in_a(q)) ab.push_back(q);
+        c->ncol_b = (int)ab.size() - c->ncol_a;
+        if ((rc = upload(c, &c->d_colorder_ab, ab))) return fail(rc);
+        // worth it when the pipe rows are a minority of the domain
+        c->overlap = ncol > 0 && 2 * (long long)c->ncol_a <= (long long)order.size();
+        if ((e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&c->ev_px, cudaEventDisableTiming)) != cudaSuccess)
+            return fail(gw_cuda_fail(e, "stream / event"));
+    }
     if ((rc = upload(c, &c->d_gz, c->gz)) || (rc = upload(c, &c->d_zclass, c->zclass)) ||
         (rc = upload(c, &c->d_colprof, c->colprof)) || (rc = upload(c, &c->d_pipe_i, c->pipe_i)) ||
         (rc = upload(c, &c->d_pipe_j, c->pipe_j)) || (rc = upload(c, &c->d_pipe_b, c->pipe_b)))
@@ -366,6 +391,9 @@ int gw_destroy(gw_ctx *c) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->ev_a) cudaEventDestroy(c->ev_a);
+    if (c->ev_px) cudaEventDestroy(c->ev_px);
+    if (c->stream2) { cudaStreamSynchronize(c->stream2); cudaStreamDestroy(c->stream2); }
     gw_adjoint_release(c);
     for (void *p : c->allocations) if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);

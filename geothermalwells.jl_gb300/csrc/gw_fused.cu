@@ -524,7 +524,7 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                                                         const Quad<T> *__restrict__ hq,
                                                         const T *__restrict__ fib,
                                                         const T *__restrict__ fcu, int nx, int ny,
-                                                        int nz, int countz) {
+                                                        int nz, int countz, int m_begin, int m_end) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *tile = reinterpret_cast<T *>(smem_raw);   // [2][HR][HW + 2][32]
     constexpr int kRow = (HW + 2) * 32;
@@ -532,11 +532,11 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nl = XL ? ny : nx;   // lines per level
     const int N = XL ? nx : ny;    // line length
-    const int k0 = blockIdx.x * 32, m0 = blockIdx.y * HW;
+    const int k0 = blockIdx.x * 32, m0 = m_begin + blockIdx.y * HW;   // lines m_begin .. m_end - 1
     const int k = k0 + lane, m = m0 + warp;
     const bool kok = k < nz;
-    const bool active = kok && m < nl;
-    const int kc = kok ? k : nz - 1, mc = m < nl ? m : nl - 1;   // clamped for table reads
+    const bool active = kok && m < m_end;
+    const int kc = kok ? k : nz - 1, mc = m < m_end ? m : m_end - 1;   // clamped for table reads
     // element (k, line m, row l): x-lines (k, j=m, i=l), y-lines (k, i=m, j=l)
     const long long mst = XL ? (long long)nz : (long long)nz * ny;
     const long long rst = XL ? (long long)nz * ny : (long long)nz;
@@ -695,17 +695,17 @@ __global__ void __launch_bounds__(32 * HW * S) k_half_seg(T *__restrict__ dst, c
                                                           const Quad<T> *__restrict__ hq,
                                                           const T *__restrict__ fib,
                                                           const T *__restrict__ fcu, int nx, int ny,
-                                                          int nz, int countz) {
+                                                          int nz, int countz, int m_begin, int m_end) {
     __shared__ T s_end[HW][S][32], s_prop[HW][S][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int lw = warp / S, sg = warp % S;
     const int nl = XL ? ny : nx;
     const int N = XL ? nx : ny;
     const int k = blockIdx.x * 32 + lane;
-    const int m = blockIdx.y * HW + lw;
+    const int m = m_begin + blockIdx.y * HW + lw;
     const bool kok = k < nz;
-    const bool active = kok && m < nl;
-    const int kc = kok ? k : nz - 1, mc = m < nl ? m : nl - 1;
+    const bool active = kok && m < m_end;
+    const int kc = kok ? k : nz - 1, mc = m < m_end ? m : m_end - 1;
     const long long mst = XL ? (long long)nz : (long long)nz * ny;
     const long long rst = XL ? (long long)nz * ny : (long long)nz;
     const int R = (N + S - 1) / S;                 // rows per segment (<= RMAX)
@@ -861,15 +861,18 @@ template <>
 const float *stage_table<float>(gw_ctx *c) { return c->f_stage; }
 
 template <typename T, bool INC>
-int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *fref) {
-    const long long ncols = (long long)c->nx * c->ny;
+int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *fref,
+                   const int *order = nullptr, long long ncols = -1) {
+    if (!order) order = c->d_colorder;
+    if (ncols < 0) ncols = (long long)c->nx * c->ny;
+    if (ncols == 0) return GW_OK;
     const int lpt = rock2_lpt(c->nz);
     unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid ? ncols : c->rock2_grid);
     switch (lpt) {
-        case 2: k_rock2_reg<T, INC, 2><<<grid, 256, reg_smem<T>(2), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 4: k_rock2_reg<T, INC, 4><<<grid, 256, reg_smem<T>(4), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 8: k_rock2_reg<T, INC, 8><<<grid, 256, reg_smem<T>(8), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 16: k_rock2_reg<T, INC, 16><<<grid, 256, reg_smem<T>(16), c->stream>>>(u, c->d_colorder, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 2: k_rock2_reg<T, INC, 2><<<grid, 256, reg_smem<T>(2), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 4: k_rock2_reg<T, INC, 4><<<grid, 256, reg_smem<T>(4), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 8: k_rock2_reg<T, INC, 8><<<grid, 256, reg_smem<T>(8), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 16: k_rock2_reg<T, INC, 16><<<grid, 256, reg_smem<T>(16), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
         default:
             k_rock2_col<T, INC><<<grid, 256, rock2_smem<T>(c->nz), c->stream>>>(u, c->d_colprof, czm, czp, fref,
                                                                             c->d_stage, s, c->nz, ncols);
@@ -879,36 +882,37 @@ int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *
 }
 
 template <typename T>
-int launch_rock2(gw_ctx *c, int s) {
+int launch_rock2(gw_ctx *c, int s, const int *order = nullptr, long long ncols = -1) {
     Bufs<T> B = bufs<T>(c);
     if (sizeof(T) == 4)
         return launch_rock2_t<float, true>(c, s, (float *)B.u, (const float *)B.ct->czm,
-                                           (const float *)B.ct->czp, (const float *)B.fref);
+                                           (const float *)B.ct->czp, (const float *)B.fref, order, ncols);
     return launch_rock2_t<double, false>(c, s, (double *)B.u, (const double *)B.ct->czm,
-                                         (const double *)B.ct->czp, nullptr);
+                                         (const double *)B.ct->czp, nullptr, order, ncols);
 }
 
 // explicit sweep along edir at the pipe columns, outlet/annulus means, advection
 template <typename T>
-int launch_pipe(gw_ctx *c, const T *src, int edir, double h) {
+int launch_pipe(gw_ctx *c, const T *src, int edir, double h, cudaStream_t st = nullptr) {
     Bufs<T> B = bufs<T>(c);
+    if (!st) st = c->stream;
     const int ncol = c->n_inner + c->n_outer;
     const T *cm = edir == GW_DIR_X ? B.ct->cxm : B.ct->cym;
     const T *cp = edir == GW_DIR_X ? B.ct->cxp : B.ct->cyp;
     if (c->n_pipe_chunks > 0) {
         dim3 g(grid_for(c->nz, 128), c->n_pipe_chunks);
-        k_pipe_sweep<T><<<g, 128, 0, c->stream>>>(B.tp, c->d_pipepart, src, c->d_pipe_chunks,
+        k_pipe_sweep<T><<<g, 128, 0, st>>>(B.tp, c->d_pipepart, src, c->d_pipe_chunks,
                                                   c->d_pipe_i, c->d_pipe_j, c->d_zclass, cm, cp,
                                                   B.Tref, c->nx, c->ny, c->nz, h, edir);
         GW_CUDA(cudaGetLastError());
     }
     dim3 gr(grid_for(c->nz, 128), c->nbh);
-    k_pipe_reduce<<<gr, 128, 0, c->stream>>>(c->d_outlet, c->d_annmean, c->d_pipepart, c->d_bchunk,
+    k_pipe_reduce<<<gr, 128, 0, st>>>(c->d_outlet, c->d_annmean, c->d_pipepart, c->d_bchunk,
                                              c->d_gz, c->d_bh, c->nz, h);
     GW_CUDA(cudaGetLastError());
     long long na = (long long)ncol * c->countz;
     if (na > 0) {
-        k_advect_c<T><<<grid_for(na, 256), 256, 0, c->stream>>>(
+        k_advect_c<T><<<grid_for(na, 256), 256, 0, st>>>(
             B.pp, B.tp, c->d_advtab, c->d_pipe_b, c->d_annmean, c->d_outlet, B.Tref, c->n_inner,
             ncol, c->nz, c->countz, c->inlet_kind, c->inlet_param);
         GW_CUDA(cudaGetLastError());
@@ -920,36 +924,41 @@ template <typename T>
 size_t half_smem(int cfg) { return 2 * (size_t)kTileHR[cfg] * (kTileHW[cfg] + 2) * 32 * sizeof(T); }
 
 template <typename T, int HW, int HR>
-void half_launch(gw_ctx *c, T *dst, const T *src, int xlines, const Quad<T> *hq, const GwFactors<T> &f,
-                 const T *pp, size_t smem) {
-    const int nl = xlines ? c->ny : c->nx;
-    dim3 grid((c->nz + 31) / 32, (nl + HW - 1) / HW);
+void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, const Quad<T> *hq,
+                 const GwFactors<T> &f, const T *pp, size_t smem, int mb, int me) {
+    dim3 grid((c->nz + 31) / 32, (me - mb + HW - 1) / HW);
     if (xlines)
-        k_half_tile<T, true, HW, HR><<<grid, 32 * HW, smem, c->stream>>>(
-            dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
+        k_half_tile<T, true, HW, HR><<<grid, 32 * HW, smem, st>>>(
+            dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz, mb, me);
     else
-        k_half_tile<T, false, HW, HR><<<grid, 32 * HW, smem, c->stream>>>(
-            dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
+        k_half_tile<T, false, HW, HR><<<grid, 32 * HW, smem, st>>>(
+            dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz, mb, me);
 }
 
 template <typename T>
-int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h) {
+int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h, int mb = 0, int me = -1,
+                cudaStream_t st = nullptr) {
     (void)h;   // folded into the half-step tables
     Bufs<T> B = bufs<T>(c);
     const GwFactors<T> &f = xlines ? B.ct->fx : B.ct->fy;
     const Quad<T> *hq = reinterpret_cast<const Quad<T> *>(xlines ? B.ct->hx : B.ct->hy);
+    const int nl = xlines ? c->ny : c->nx;
+    if (me < 0) me = nl;                       // lines mb .. me - 1
+    if (!st) st = c->stream;
+    if (me <= mb) return GW_OK;
     int cfg = c->half_cfg;
     const int N = xlines ? c->nx : c->ny;
     if (cfg == kSegCfg) {
         if (N <= kSegS * kSegR) {
-            const int nl = xlines ? c->ny : c->nx;
-            dim3 grid((c->nz + 31) / 32, (nl + 1) / 2);
+            dim3 grid((c->nz + 31) / 32, (me - mb + 1) / 2);
             if (xlines)
-                k_half_seg<T, true, 2, kSegS, kSegR><<<grid, 32 * 2 * kSegS, 0, c->stream>>>(
-                    dst, src, B.pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
+                k_half_seg<T, true, 2, kSegS, kSegR><<<grid, 32 * 2 * kSegS, 0, st>>>(
+                    dst, src, B.pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz,
+                    mb, me);
             else
-                k_half_seg<T, false, 2, kSegS, kSegR><<<grid, 32 * 2 * kSegS, 0, c->stream>>>(
-                    dst, src, B.pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz);
+                k_half_seg<T, false, 2, kSegS, kSegR><<<grid, 32 * 2 * kSegS, 0, st>>>(
+                    dst, src, B.pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz,
+                    mb, me);
             GW_CUDA(cudaGetLastError());
             return GW_OK;
         }
@@ -957,12 +966,12 @@ int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h) {
     }
     const size_t sm = half_smem<T>(cfg);
     switch (cfg) {
-        case 1: half_launch<T, 8, 16>(c, dst, src, xlines, hq, f, B.pp, sm); break;
-        case 2: half_launch<T, 8, 8>(c, dst, src, xlines, hq, f, B.pp, sm); break;
-        case 3: half_launch<T, 4, 32>(c, dst, src, xlines, hq, f, B.pp, sm); break;
-        case 4: half_launch<T, 2, 16>(c, dst, src, xlines, hq, f, B.pp, sm); break;
-        case 5: half_launch<T, 8, 32>(c, dst, src, xlines, hq, f, B.pp, sm); break;
-        default: half_launch<T, 4, 16>(c, dst, src, xlines, hq, f, B.pp, sm); break;
+        case 1: half_launch<T, 8, 16>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
+        case 2: half_launch<T, 8, 8>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
+        case 3: half_launch<T, 4, 32>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
+        case 4: half_launch<T, 2, 16>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
+        case 5: half_launch<T, 8, 32>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
+        default: half_launch<T, 4, 16>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
     }
     GW_CUDA(cudaGetLastError());
     return GW_OK;
@@ -990,6 +999,30 @@ template <typename T>
 int fused_step(gw_ctx *c, double dt, int s) {
     Bufs<T> B = bufs<T>(c);
     int rc;
+    if (c->overlap && rock2_lpt(c->nz) > 0) {
+        // The pipe passes need only the rows around the pipes: ROCK2 first
+        // does the columns of rows jlo-1..jhi+1; then a second stream runs
+        // the y pipe pass, the x-lines through the pipes (rows jlo..jhi) and
+        // the x pipe pass while the first finishes ROCK2 and the other
+        // x-lines; the y-lines wait for both.
+        const int *ab = c->d_colorder_ab;
+        cudaStream_t s1 = c->stream, s2 = c->stream2;
+        if ((rc = launch_rock2<T>(c, s, ab, c->ncol_a))) return rc;
+        GW_CUDA(cudaEventRecord(c->ev_a, s1));
+        GW_CUDA(cudaStreamWaitEvent(s2, c->ev_a, 0));
+        if ((rc = launch_pipe<T>(c, B.u, GW_DIR_Y, dt / 2, s2)) ||
+            (rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2, c->jlo, c->jhi + 1, s2)) ||
+            (rc = launch_pipe<T>(c, B.temp, GW_DIR_X, dt / 2, s2)))
+            return rc;
+        GW_CUDA(cudaEventRecord(c->ev_px, s2));
+        if ((rc = launch_rock2<T>(c, s, ab + c->ncol_a, c->ncol_b)) ||
+            (rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2, 0, c->jlo, s1)) ||
+            (rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2, c->jhi + 1, c->ny, s1)))
+            return rc;
+        GW_CUDA(cudaStreamWaitEvent(s1, c->ev_px, 0));
+        if ((rc = launch_half<T>(c, B.u, B.temp, 0, dt / 2))) return rc;
+        return gw_launch_record(c, dt);
+    }
     if ((rc = launch_rock2<T>(c, s))) return rc;
     if ((rc = launch_pipe<T>(c, B.u, GW_DIR_Y, dt / 2))) return rc;
     if ((rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2))) return rc;

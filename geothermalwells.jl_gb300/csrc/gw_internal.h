@@ -74,6 +74,15 @@ struct gw_ctx {
     double *d_gz = nullptr;
     int *d_zclass = nullptr, *d_colprof = nullptr;
     int *d_colorder = nullptr;        // columns sorted by profile
+    // Overlap of the pipe passes with the bulk of the step: the rows jlo..jhi
+    // hold every pipe column; d_colorder_ab lists the columns of rows
+    // jlo-1..jhi+1 (ncol_a, the ones the pipe passes and the x-lines through
+    // the pipes read) and then the rest (ncol_b), each sorted by profile.
+    int *d_colorder_ab = nullptr;
+    int ncol_a = 0, ncol_b = 0, jlo = -1, jhi = -1;
+    bool overlap = false;
+    cudaStream_t stream2 = nullptr;   // the pipe passes' stream inside the step graph
+    cudaEvent_t ev_a = nullptr, ev_px = nullptr;
     int *d_pipe_i = nullptr, *d_pipe_j = nullptr, *d_pipe_b = nullptr;
     GwBhDev *d_bh = nullptr;
     GwCoefTables<double> c64;

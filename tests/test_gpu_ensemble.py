@@ -35,6 +35,10 @@ def test_batch_equals_single_contexts(precision, gwlib):
 
 @pytest.mark.parametrize("tiling", range(len(TILINGS)))
 def test_every_tiling_gives_the_same_field(tiling, gwlib):
+    """The row-tile tilings run the same elimination order: bitwise equal.
+    The segmented tiling re-associates the line recurrences (segment scans):
+    equal to float rounding, 1e-5 of the field's magnitude (float epsilon
+    1.2e-7 times the ~200-row recurrences)."""
     ds = designs()
     a = Ensemble(ds, precision="mixed")
     a.step(40.0, 3)
@@ -42,7 +46,11 @@ def test_every_tiling_gives_the_same_field(tiling, gwlib):
     b.set_tiling(tiling)
     b.step(40.0, 3)
     for ca, cb in zip(a.caches, b.caches):
-        assert np.array_equal(ca.get_field(), cb.get_field())
+        fa, fb = ca.get_field(), cb.get_field()
+        if TILINGS[tiling][1] == "seg8x32":
+            assert np.max(np.abs(fa - fb)) <= 1e-5 * np.max(np.abs(fa))
+        else:
+            assert np.array_equal(fa, fb)
     a.close(); b.close()
 
 
