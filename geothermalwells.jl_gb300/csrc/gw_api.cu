@@ -408,6 +408,15 @@ int gw_get_info(gw_ctx *c, gw_info_t *o) {
     o->n_zclass = c->n_zclass; o->n_profiles = c->n_profiles;
     o->eigen_estimate = c->eigen_estimate;
     o->device_bytes = c->device_bytes;
+    o->overlap = c->overlap ? 1 : 0;
+    return GW_OK;
+}
+
+int gw_set_overlap(gw_ctx *c, int on) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
+    if (on && c->n_inner + c->n_outer == 0) return gw_fail(GW_ERR_ARG, "no pipe columns to overlap");
+    c->overlap = on != 0;
+    c->graph_dt = -1.0;   // recapture the step graph
     return GW_OK;
 }
 

@@ -56,7 +56,8 @@ class Info(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in
                 ("nx", "ny", "nz", "n_boreholes", "countxy_inner", "countxy_outer", "countz",
                  "n_zclass", "n_profiles")] + \
-               [("eigen_estimate", ctypes.c_double), ("device_bytes", ctypes.c_longlong)]
+               [("eigen_estimate", ctypes.c_double), ("device_bytes", ctypes.c_longlong),
+                ("overlap", ctypes.c_int)]
 
 
 SIGNATURES = {
@@ -74,6 +75,7 @@ SIGNATURES = {
     "gw_advection": (_i, [_vp, _vp, _d, _d]),
     "gw_adi_adv": (_i, [_vp, _vp, _vp, _d, _d]),
     "gw_step": (_i, [_vp, _d, _d, _i, _i]),
+    "gw_set_overlap": (_i, [_vp, _i]),
     "gw_rock2_stages": (_i, [_vp, _d, _i, _ip, _ip]),
     "gw_get_outlet": (_i, [_vp, _dp]),
     "gw_get_outlet_series": (_i, [_vp, _dp, _i]),

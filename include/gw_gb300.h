@@ -83,6 +83,7 @@ typedef struct gw_info_t {
     int n_zclass, n_profiles;
     double eigen_estimate;           /* src/solver.jl:474-488 */
     long long device_bytes;          /* device memory held by the context */
+    int overlap;                     /* pipe passes on a second stream (gw_set_overlap) */
 } gw_info_t;
 
 typedef struct gw_ctx gw_ctx;
@@ -123,6 +124,12 @@ int gw_adi_adv(gw_ctx *ctx, double *u_dev, double *temp_dev, double t, double dt
  * step is captured once in a CUDA graph and replayed.  Records the outlet
  * temperature and extracted heat after every step. */
 int gw_step(gw_ctx *ctx, double t0, double dt, int nsteps, int max_stages);
+/* Run the step's two pipe passes (and the x-lines through the pipes) on a
+ * second stream, overlapping the rest of the step (on = 1; the default where
+ * the rows holding pipe columns are at most half of the domain), or in line
+ * (on = 0).  Both give bitwise identical results.  gw_get_info reports the
+ * setting (overlap). */
+int gw_set_overlap(gw_ctx *ctx, int on);
 /* Stage count gw_step uses for dt (and whether its interval covers dt*lambda). */
 int gw_rock2_stages(gw_ctx *ctx, double dt, int max_stages, int *stages, int *covered);
 

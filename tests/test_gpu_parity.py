@@ -235,3 +235,28 @@ def test_aliasing_rejected(gwlib, torch_cuda):
         thomas_I_minus_A(d, d, cache, 1.0, "x")
     with pytest.raises(_lib.GWError):
         rhs_diffusion_z(d, d, cache, 0.0)
+
+
+@pytest.mark.parametrize("case", ["small_const", "two_wells_layers_hx", "example", "2mm"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_overlapped_step_is_bitwise_the_in_line_step(case, precision, gwlib):
+    """The step with its pipe passes on a second stream (gw_set_overlap) gives
+    exactly the in-line step's field and outlet series."""
+    from geothermalwells_gb300 import _lib
+    w = {"small_const": lambda: W.small_case(), "two_wells_layers_hx": lambda: W.small_case(n_layers=3, inlet="hx", nbh=2),
+         "example": W.example_single_borehole, "2mm": W.single_well_2mm}[case]()
+    L = _lib.load()
+    out = []
+    for on in (1, 0):
+        cache = create_cache(backend=GB300(precision=precision), gridx=w["gridx"], gridy=w["gridy"],
+                             gridz=w["gridz"], materials=w["materials"], boreholes=w["boreholes"],
+                             inlet_model=w["inlet_model"])
+        _lib.check(L.gw_set_overlap(cache.ctx, on))
+        info = _lib.Info()
+        _lib.check(L.gw_get_info(cache.ctx, info))
+        assert info.overlap == on
+        sol = gpu_run(w, cache, 3)
+        out.append((sol.u[-1], sol.T_outlet))
+        cache.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
