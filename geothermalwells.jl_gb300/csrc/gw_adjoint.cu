@@ -195,7 +195,8 @@ __global__ void __launch_bounds__(128) k_thomas_t(T *__restrict__ U, const T *__
 // conductivity derivatives: G[k] += beta * d(lambda^T A phi)/dk summed over the
 // rock cells of level k (the face terms of gw_build_adjoint_tables).  One
 // thread per level, looping over a strided share of the columns; one atomic
-// per thread.  Face terms are formed in the storage type and summed in double.
+// per thread.  Face terms are formed and summed per thread in the storage
+// type (a few hundred columns each); the per-level totals are double.
 // Tref (mixed path, z only): phi is theta and T_ref's differences are added.
 
 template <typename T>
@@ -210,7 +211,7 @@ __global__ void __launch_bounds__(128) k_param_z(double *__restrict__ G, const T
     const unsigned char *rk = rock + (size_t)__ldg(zclass + k) * ncol;   // [(zc * nx + i) * ny + j]
     const T dtp = (Tref && k < nz - 1) ? T(Tref[k + 1] - Tref[k]) : T(0);
     const T dtm = (Tref && k > 0) ? T(Tref[k] - Tref[k - 1]) : T(0);
-    double acc = 0.0;
+    T acc = T(0);
     for (long long col = blockIdx.y; col < ncol; col += gridDim.y) {
         if (!__ldg(rk + col)) continue;
         const long long c = col * nz + k;
@@ -219,9 +220,9 @@ __global__ void __launch_bounds__(128) k_param_z(double *__restrict__ G, const T
         T d = T(0);
         if (k < nz - 1) d = (phi[c + 1] - fk + dtp) * (lk * __ldg(wzp + pb) - lam[c + 1] * __ldg(wzm + pb + 1));
         if (k > 0) d += (fk - phi[c - 1] + dtm) * (lam[c - 1] * __ldg(wzp + pb - 1) - lk * __ldg(wzm + pb));
-        acc += (double)d;
+        acc += d;
     }
-    if (acc != 0.0) atomicAdd(G + k, beta * acc);
+    if (acc != T(0)) atomicAdd(G + k, beta * (double)acc);
 }
 
 // x (dir 0) and y (dir 1): each face (l, l+1) of the level counted once, its
@@ -237,7 +238,7 @@ __global__ void __launch_bounds__(128) k_param_xy(double *__restrict__ G, const 
     const long long ncol = (long long)nx * ny;
     const int zc = __ldg(zclass + k);
     const unsigned char *rk = rock + (size_t)zc * ncol;
-    double acc = 0.0;
+    T acc = T(0);
     for (long long col = blockIdx.y; col < ncol; col += gridDim.y) {
         const int i = (int)(col / ny), j = (int)(col % ny);
         long long col2;
@@ -254,9 +255,9 @@ __global__ void __launch_bounds__(128) k_param_xy(double *__restrict__ G, const 
         const int r = (int)__ldg(rk + col) + (int)__ldg(rk + col2);
         if (!r) continue;
         const long long c = col * nz + k, c2 = col2 * nz + k;
-        acc += (double)(r * ((phi[c2] - phi[c]) * (lam[c] * __ldg(wp + q) - lam[c2] * __ldg(wm + q + 1))));
+        acc += T(r) * ((phi[c2] - phi[c]) * (lam[c] * __ldg(wp + q) - lam[c2] * __ldg(wm + q + 1)));
     }
-    if (acc != 0.0) atomicAdd(G + k, beta * acc);
+    if (acc != T(0)) atomicAdd(G + k, beta * (double)acc);
 }
 
 // ---------------------------------------------------------------------------
