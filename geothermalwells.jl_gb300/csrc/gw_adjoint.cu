@@ -55,6 +55,7 @@ struct GwAdj {
     double *osum = nullptr;     // [nbh] sum over steps of T_out - T_in
     double *mbar = nullptr;     // [nbh][nz] adjoint of the turnaround annulus means
     double *tmp = nullptr;      // [ncol][countz] adjoint of the advected pipe values (8 B slots)
+    double *S = nullptr;        // [nbh][countz] its sum over each borehole's inner columns
     std::vector<void *> allocs;
     long long bytes = 0;
 };
@@ -95,18 +96,21 @@ template <typename T>
 __global__ void __launch_bounds__(kB) k_zstage_t(T *out, const T *__restrict__ lam, const T *w,
                                                  const int *__restrict__ colprof,
                                                  const T *__restrict__ czm, const T *__restrict__ czp,
-                                                 int nz, long long ncell, T a1, T hmu, T a2) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    const int k = (int)(c % nz);
-    const size_t base = (size_t)__ldg(colprof + c / nz) * nz;
-    const T lc = lam[c];
-    T at = -(__ldg(czm + base + k) + __ldg(czp + base + k)) * lc;
-    if (k > 0) at = fma(__ldg(czp + base + k - 1), lam[c - 1], at);
-    if (k < nz - 1) at = fma(__ldg(czm + base + k + 1), lam[c + 1], at);
-    T v = fma(hmu, at, a1 * lc);
-    if (a2 != T(0)) v = fma(a2, w[c], v);
-    out[c] = v;
+                                                 int nz, long long ncol, T a1, T hmu, T a2) {
+    // block: kB levels (blockIdx.y) of every gridDim.x-th column
+    const int k = blockIdx.y * kB + threadIdx.x;
+    if (k >= nz) return;
+    for (long long col = blockIdx.x; col < ncol; col += gridDim.x) {
+        const long long c = col * nz + k;
+        const size_t base = (size_t)__ldg(colprof + col) * nz;
+        const T lc = lam[c];
+        T at = -(__ldg(czm + base + k) + __ldg(czp + base + k)) * lc;
+        if (k > 0) at = fma(__ldg(czp + base + k - 1), lam[c - 1], at);
+        if (k < nz - 1) at = fma(__ldg(czm + base + k + 1), lam[c + 1], at);
+        T v = fma(hmu, at, a1 * lc);
+        if (a2 != T(0)) v = fma(a2, w[c], v);
+        out[c] = v;
+    }
 }
 
 // Mixed path, forward: one ROCK2 stage on theta = T - T_ref with the source
@@ -116,19 +120,21 @@ __global__ void __launch_bounds__(kB) k_zstage_theta(float *out, const float *__
                                                      const float *y, const int *__restrict__ colprof,
                                                      const float *__restrict__ czm,
                                                      const float *__restrict__ czp,
-                                                     const float *__restrict__ fref, int nz,
-                                                     long long ncell, float hmu, float kap) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    const int k = (int)(c % nz);
-    const size_t q = (size_t)__ldg(colprof + c / nz) * nz + k;
-    const float xc = x[c];
-    const float xp = k < nz - 1 ? x[c + 1] : xc;
-    const float xm = k > 0 ? x[c - 1] : xc;
-    const float a = __ldg(czp + q) * (xp - xc) - __ldg(czm + q) * (xc - xm) + __ldg(fref + q);
-    float v = fmaf(hmu, a, xc);
-    if (kap != 0.f) v = fmaf(kap, xc - y[c], v);
-    out[c] = v;
+                                                     const float *__restrict__ fref, int nz, long long ncol,
+                                                     float hmu, float kap) {
+    const int k = blockIdx.y * kB + threadIdx.x;
+    if (k >= nz) return;
+    for (long long col = blockIdx.x; col < ncol; col += gridDim.x) {
+        const long long c = col * nz + k;
+        const size_t q = (size_t)__ldg(colprof + col) * nz + k;
+        const float xc = x[c];
+        const float xp = k < nz - 1 ? x[c + 1] : xc;
+        const float xm = k > 0 ? x[c - 1] : xc;
+        const float a = __ldg(czp + q) * (xp - xc) - __ldg(czm + q) * (xc - xm) + __ldg(fref + q);
+        float v = fmaf(hmu, a, xc);
+        if (kap != 0.f) v = fmaf(kap, xc - y[c], v);
+        out[c] = v;
+    }
 }
 
 // dst = src + h A^T src along x (dir 0, table [zc][j][i]) or y (dir 1, [zc][i][j]).
@@ -136,23 +142,25 @@ template <typename T>
 __global__ void __launch_bounds__(kB) k_explicit_t(T *__restrict__ dst, const T *__restrict__ src,
                                                    const int *__restrict__ zclass,
                                                    const T *__restrict__ cmt, const T *__restrict__ cpt,
-                                                   int nx, int ny, int nz, long long ncell, T h, int dir) {
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    const int k = (int)(c % nz);
-    const long long r = c / nz;
-    const int j = (int)(r % ny), i = (int)(r / ny);
+                                                   int nx, int ny, int nz, T h, int dir) {
+    const int k = blockIdx.y * kB + threadIdx.x;
+    if (k >= nz) return;
     const int zc = __ldg(zclass + k);
-    size_t q;
-    long long s;
-    int l, n;
-    if (dir == 0) { q = ((size_t)zc * ny + j) * nx + i; s = (long long)nz * ny; l = i; n = nx; }
-    else { q = ((size_t)zc * nx + i) * ny + j; s = nz; l = j; n = ny; }
-    const T lc = src[c];
-    T at = -(__ldg(cmt + q) + __ldg(cpt + q)) * lc;
-    if (l > 0) at = fma(__ldg(cpt + q - 1), src[c - s], at);
-    if (l < n - 1) at = fma(__ldg(cmt + q + 1), src[c + s], at);
-    dst[c] = fma(h, at, lc);
+    const int ncol = nx * ny;
+    for (int col = blockIdx.x; col < ncol; col += gridDim.x) {
+        const int j = col % ny, i = col / ny;
+        const long long c = (long long)col * nz + k;
+        size_t q;
+        long long s;
+        int l, n;
+        if (dir == 0) { q = ((size_t)zc * ny + j) * nx + i; s = (long long)nz * ny; l = i; n = nx; }
+        else { q = ((size_t)zc * nx + i) * ny + j; s = nz; l = j; n = ny; }
+        const T lc = src[c];
+        T at = -(__ldg(cmt + q) + __ldg(cpt + q)) * lc;
+        if (l > 0) at = fma(__ldg(cpt + q - 1), src[c - s], at);
+        if (l < n - 1) at = fma(__ldg(cmt + q + 1), src[c + s], at);
+        dst[c] = fma(h, at, lc);
+    }
 }
 
 // (I - h A_dir)^T U = R on every line.  The factors give M = Lt Ut with Lt
@@ -239,45 +247,31 @@ __global__ void __launch_bounds__(128) k_param_xy(double *__restrict__ G, const 
     const int zc = __ldg(zclass + k);
     const unsigned char *rk = rock + (size_t)zc * ncol;
     T acc = T(0);
-    for (long long col = blockIdx.y; col < ncol; col += gridDim.y) {
-        const int i = (int)(col / ny), j = (int)(col % ny);
-        long long col2;
-        size_t q;
-        if (dir == 0) {
-            if (i == nx - 1) continue;
-            col2 = col + ny;
-            q = ((size_t)zc * ny + j) * nx + i;
-        } else {
-            if (j == ny - 1) continue;
-            col2 = col + 1;
-            q = ((size_t)zc * nx + i) * ny + j;
+    constexpr int U = 4;
+    for (long long c0 = blockIdx.y; c0 < ncol; c0 += (long long)U * gridDim.y) {
+        T d[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long col = c0 + (long long)u * gridDim.y;
+            const int i = (int)(col / ny), j = (int)(col % ny);
+            // the face (l, l+1) exists when l is not the last point of the line
+            const bool ok = col < ncol && (dir == 0 ? i < nx - 1 : j < ny - 1);
+            const long long cc = ok ? col : 0;
+            const long long col2 = ok ? (dir == 0 ? cc + ny : cc + 1) : 0;
+            const int ii = ok ? i : 0, jj = ok ? j : 0;
+            const size_t q = dir == 0 ? ((size_t)zc * ny + jj) * nx + ii : ((size_t)zc * nx + ii) * ny + jj;
+            const long long c = cc * nz + k, c2 = col2 * nz + k;
+            const T r = ok ? T((int)__ldg(rk + cc) + (int)__ldg(rk + col2)) : T(0);
+            d[u] = r * ((phi[c2] - phi[c]) * (lam[c] * __ldg(wp + q) - lam[c2] * __ldg(wm + q + 1)));
         }
-        const int r = (int)__ldg(rk + col) + (int)__ldg(rk + col2);
-        if (!r) continue;
-        const long long c = col * nz + k, c2 = col2 * nz + k;
-        acc += T(r) * ((phi[c2] - phi[c]) * (lam[c] * __ldg(wp + q) - lam[c2] * __ldg(wm + q + 1)));
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc += d[u];
     }
     if (acc != T(0)) atomicAdd(G + k, beta * (double)acc);
 }
 
 // ---------------------------------------------------------------------------
 // advection transpose
-
-// gpu_searchsortedfirst + interpolation_helper (src/solver.jl:362-389), 0-based,
-// as the forward kernels evaluate it.
-__device__ __forceinline__ void interp(const double *__restrict__ g, int n, double dep, int &il,
-                                       int &ir, double &alpha) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        int mid = lo + ((hi - lo) >> 1);
-        if (g[mid] < dep) lo = mid + 1; else hi = mid;
-    }
-    ir = lo;
-    il = lo - 1;
-    if (il < 0) il = 0;
-    if (ir > n - 1) ir = n - 1;
-    alpha = __ddiv_rn(__dsub_rn(dep, g[il]), __dsub_rn(g[ir], g[il]));
-}
 
 // The field the forward advection read, at pipe column q and level k, as an
 // absolute temperature: from the full field (double path) or from the compact
@@ -318,17 +312,17 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Scatter-add of every advected value's adjoint onto the cells (or the
-// turnaround annulus means) it was interpolated from, plus the derivatives
-// with respect to v_inner / v_outer (through the departure points) and the
-// inlet adjoint.  phi is the field the forward advection read, mean its
-// annulus means.
+// Scatter-add of every advected value's adjoint onto the cells it was
+// interpolated from, plus the derivatives with respect to v_inner / v_outer
+// (through the departure points) and the inlet adjoint, with the departure
+// records of the forward (k_adv_table).  phi is the field the forward
+// advection read.  Turnaround cells are left to k_turn_apply.
 template <typename T>
 __global__ void __launch_bounds__(kB) k_adv_t_scatter(
-    T *__restrict__ a, const double *__restrict__ tmp, PipeField<T> phi, const double *__restrict__ mean,
+    T *__restrict__ a, const double *__restrict__ tmp, PipeField<T> phi, const GwAdvRec *__restrict__ tab,
     const double *__restrict__ gz, const int *__restrict__ pi, const int *__restrict__ pj,
-    const int *__restrict__ pb, const GwBhDev *__restrict__ bh, double *__restrict__ mbar,
-    double *__restrict__ sc, int n_inner, int ncol, int ny, int nz, int countz, double dt) {
+    const int *__restrict__ pb, double *__restrict__ sc, int n_inner, int ncol, int ny, int nz, int countz,
+    double dt) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double dvi = 0.0, dvo = 0.0, ib = 0.0;
     int b = -1;
@@ -336,44 +330,23 @@ __global__ void __launch_bounds__(kB) k_adv_t_scatter(
         const int k = (int)(e % countz);
         const int q = (int)(e / countz);
         b = pb[q];
-        const GwBhDev B = bh[b];
-        const double z = gz[k];
         const double ab = tmp[e];
-        if (z <= B.h && ab != 0.0) {
-            const long long col = (long long)nz * (pj[q] + (long long)ny * pi[q]);
-            int il, ir;
-            double al;
-            if (q < n_inner) {
-                const double zd = __fma_rn(B.v_inner, dt, z);
-                if (zd > B.h) {
-                    const double dt1 = __ddiv_rn(__dsub_rn(B.h, z), B.v_inner);
-                    const double dt2 = __dsub_rn(dt, dt1);
-                    interp(gz, nz, __fma_rn(-B.v_outer, dt2, B.h), il, ir, al);
-                    const double *m = mean + (size_t)b * nz;
-                    atomicAdd(mbar + (size_t)b * nz + ir, al * ab);
-                    atomicAdd(mbar + (size_t)b * nz + il, (1.0 - al) * ab);
-                    if (ir != il) {
-                        const double s = (m[ir] - m[il]) / (gz[ir] - gz[il]) * ab;
-                        dvo -= s * dt2;                           // d zd2 / d v_outer = -dt2
-                        dvi -= s * B.v_outer * dt1 / B.v_inner;   // d zd2 / d v_inner
-                    }
-                } else {
-                    interp(gz, nz, zd, il, ir, al);
-                    atomicAdd(a + col + ir, T(al * ab));
-                    atomicAdd(a + col + il, T((1.0 - al) * ab));
-                    if (ir != il) dvi += (phi.at(q, ir) - phi.at(q, il)) / (gz[ir] - gz[il]) * ab * dt;
-                }
-            } else {
-                const double zd = __fma_rn(-B.v_outer, dt, z);
-                if (zd <= 0.0) {
-                    ib += ab;
-                } else {
-                    interp(gz, nz, zd, il, ir, al);
-                    atomicAdd(a + col + ir, T(al * ab));
-                    atomicAdd(a + col + il, T((1.0 - al) * ab));
-                    if (ir != il) dvo -= (phi.at(q, ir) - phi.at(q, il)) / (gz[ir] - gz[il]) * ab * dt;
+        const bool inner = q < n_inner;
+        const GwAdvRec r = tab[((size_t)b * countz + k) * 2 + (inner ? 0 : 1)];
+        if (ab != 0.0) {
+            if (r.type == kAdvInlet) {
+                ib += ab;
+            } else if (r.type == kAdvInterp) {
+                const long long col = (long long)nz * (pj[q] + (long long)ny * pi[q]);
+                atomicAdd(a + col + r.ir, T(r.alpha * ab));
+                atomicAdd(a + col + r.il, T((1.0 - r.alpha) * ab));
+                if (r.ir != r.il) {
+                    const double s = (phi.at(q, r.ir) - phi.at(q, r.il)) / (gz[r.ir] - gz[r.il]) * ab * dt;
+                    if (inner) dvi += s;   // d zd / d v_inner = dt
+                    else dvo -= s;         // d zd / d v_outer = -dt
                 }
             }
+            // kAdvTurn: summed over the inner columns per level (k_turn_apply); kAdvKeep: z > h
         }
     }
     const int b0 = __shfl_sync(0xffffffffu, b, 0);
@@ -447,17 +420,84 @@ __global__ void k_osum(double *osum, const double *outlet, int nbh, int inlet_ki
     }
 }
 
-// Annulus means per borehole and level of the field the forward advection read.
+// Annulus means per borehole and level of the field the forward advection
+// read: 32 levels x 8 column groups per block, then a sum over the groups.
 template <typename T>
-__global__ void __launch_bounds__(128) k_ann_mean(double *__restrict__ mean, PipeField<T> phi,
+__global__ void __launch_bounds__(256) k_ann_mean(double *__restrict__ mean, PipeField<T> phi,
                                                   const GwBhDev *__restrict__ bh, int nz) {
+    __shared__ double red[8][32];
     const int b = blockIdx.y;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nz) return;
+    const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    const int k = blockIdx.x * 32 + lane;
     const GwBhDev B = bh[b];
     double s = 0.0;
-    for (int q = B.outer_begin; q < B.outer_begin + B.outer_count; ++q) s += phi.at(q, k);
-    mean[(size_t)b * nz + k] = s / (double)B.outer_count;
+    if (k < nz)
+        for (int q = B.outer_begin + grp; q < B.outer_begin + B.outer_count; q += 8) s += phi.at(q, k);
+    red[grp][lane] = s;
+    __syncthreads();
+    if (grp == 0 && k < nz) {
+        double t = 0.0;
+#pragma unroll
+        for (int g = 0; g < 8; ++g) t += red[g][lane];
+        mean[(size_t)b * nz + k] = t / (double)B.outer_count;
+    }
+}
+
+// Sum over a borehole's inner columns of the advected values' adjoint, per
+// level (the turnaround cells of one level share their interpolation).
+__global__ void __launch_bounds__(256) k_inner_sum(double *__restrict__ S, const double *__restrict__ tmp,
+                                                   const GwBhDev *__restrict__ bh, int countz) {
+    __shared__ double red[8][32];
+    const int b = blockIdx.y;
+    const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    const int k = blockIdx.x * 32 + lane;
+    const GwBhDev B = bh[b];
+    double s = 0.0;
+    if (k < countz)
+        for (int q = B.inner_begin + grp; q < B.inner_begin + B.inner_count; q += 8) s += tmp[(size_t)q * countz + k];
+    red[grp][lane] = s;
+    __syncthreads();
+    if (grp == 0 && k < countz) {
+        double t = 0.0;
+#pragma unroll
+        for (int g = 0; g < 8; ++g) t += red[g][lane];
+        S[(size_t)b * countz + k] = t;
+    }
+}
+
+// Turnaround cells, per borehole and level: the level's summed adjoint goes
+// to the annulus means it was interpolated from, and the v_inner / v_outer
+// derivatives through the turnaround departure point.
+__global__ void k_turn_apply(double *__restrict__ mbar, double *__restrict__ sc, const double *__restrict__ S,
+                             const double *__restrict__ mean, const GwAdvRec *__restrict__ tab,
+                             const double *__restrict__ gz, const GwBhDev *__restrict__ bh, int nz, int countz,
+                             double dt) {
+    const int b = blockIdx.y;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double dvi = 0.0, dvo = 0.0;
+    if (k < countz) {
+        const GwAdvRec r = tab[((size_t)b * countz + k) * 2];
+        const double ab = S[(size_t)b * countz + k];
+        if (r.type == kAdvTurn && ab != 0.0) {
+            const GwBhDev B = bh[b];
+            const double dt1 = __ddiv_rn(__dsub_rn(B.h, gz[k]), B.v_inner);
+            const double dt2 = __dsub_rn(dt, dt1);
+            atomicAdd(mbar + (size_t)b * nz + r.ir, r.alpha * ab);
+            atomicAdd(mbar + (size_t)b * nz + r.il, (1.0 - r.alpha) * ab);
+            if (r.ir != r.il) {
+                const double *m = mean + (size_t)b * nz;
+                const double sl = (m[r.ir] - m[r.il]) / (gz[r.ir] - gz[r.il]) * ab;
+                dvo = -sl * dt2;                           // d zd2 / d v_outer = -dt2
+                dvi = -sl * B.v_outer * dt1 / B.v_inner;   // d zd2 / d v_inner
+            }
+        }
+    }
+    dvi = warp_sum(dvi);
+    dvo = warp_sum(dvo);
+    if ((threadIdx.x & 31) == 0) {
+        if (dvi != 0.0) atomicAdd(sc + 4 * b + 0, dvi);
+        if (dvo != 0.0) atomicAdd(sc + 4 * b + 1, dvo);
+    }
 }
 
 __global__ void k_to_double(double *__restrict__ out, const float *__restrict__ in, long long n) {
@@ -487,7 +527,8 @@ int ensure_adj(gw_ctx *c) {
         (rc = adj_upload(a, &a->rock, rock)) || (rc = adj_alloc(a, &a->G, (size_t)c->nz)) ||
         (rc = adj_alloc(a, &a->sc, (size_t)4 * c->nbh)) || (rc = adj_alloc(a, &a->osum, (size_t)c->nbh)) ||
         (rc = adj_alloc(a, &a->mbar, (size_t)c->nbh * c->nz)) ||
-        (rc = adj_alloc(a, &a->tmp, (size_t)std::max(ncol, 1) * std::max(c->countz, 1)))) {
+        (rc = adj_alloc(a, &a->tmp, (size_t)std::max(ncol, 1) * std::max(c->countz, 1))) ||
+        (rc = adj_alloc(a, &a->S, (size_t)c->nbh * std::max(c->countz, 1)))) {
         gw_adjoint_release(c);
         return rc;
     }
@@ -500,6 +541,15 @@ int zero_acc(gw_ctx *c) {
     GW_CUDA(cudaMemsetAsync(a->sc, 0, sizeof(double) * 4 * c->nbh, c->stream));
     GW_CUDA(cudaMemsetAsync(a->osum, 0, sizeof(double) * c->nbh, c->stream));
     return GW_OK;
+}
+
+// per-cell kernels: blocks of kB levels (y) walking a strided share of the
+// columns (x), about 8 resident blocks per SM
+dim3 cell_grid(const gw_ctx *c) {
+    const int by = (c->nz + kB - 1) / kB;
+    long long bx = std::max(1LL, (152LL * 8) / by);
+    bx = std::min(bx, (long long)c->nx * c->ny);
+    return dim3((unsigned)bx, (unsigned)by);
 }
 
 dim3 param_grid(const gw_ctx *c) {
@@ -545,22 +595,20 @@ int launch_param(gw_ctx *c, const T *lam, const T *phi, double beta, int dir) {
 
 template <typename T>
 int launch_zstage_t(gw_ctx *c, T *out, const T *lam, const T *w, double a1, double hmu, double a2) {
-    const long long n = (long long)c->nx * c->ny * c->nz;
     Tabs<T> tb = tabs(c, (T *)nullptr);
-    k_zstage_t<T><<<nblocks(n, kB), kB, 0, c->stream>>>(out, lam, w, c->d_colprof, tb.ct->czm, tb.ct->czp,
-                                                       c->nz, n, (T)a1, (T)hmu, (T)a2);
+    k_zstage_t<T><<<cell_grid(c), kB, 0, c->stream>>>(out, lam, w, c->d_colprof, tb.ct->czm, tb.ct->czp, c->nz,
+                                                     (long long)c->nx * c->ny, (T)a1, (T)hmu, (T)a2);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }
 
 template <typename T>
 int launch_explicit_t(gw_ctx *c, T *dst, const T *src, double h, int dir) {
-    const long long n = (long long)c->nx * c->ny * c->nz;
     Tabs<T> tb = tabs(c, (T *)nullptr);
     const T *cm = dir == GW_DIR_X ? tb.ct->cxm : tb.ct->cym;
     const T *cp = dir == GW_DIR_X ? tb.ct->cxp : tb.ct->cyp;
-    k_explicit_t<T><<<nblocks(n, kB), kB, 0, c->stream>>>(dst, src, c->d_zclass, cm, cp, c->nx, c->ny,
-                                                         c->nz, n, (T)h, dir);
+    k_explicit_t<T><<<cell_grid(c), kB, 0, c->stream>>>(dst, src, c->d_zclass, cm, cp, c->nx, c->ny, c->nz,
+                                                       (T)h, dir);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }
@@ -583,8 +631,8 @@ int advection_t(gw_ctx *c, T *a, PipeField<T> phi, double h, double ob_scale, do
     GwAdj *ad = c->adj;
     const int ncol = c->n_inner + c->n_outer;
     if (ncol == 0) return GW_OK;
-    dim3 gm((c->nz + 127) / 128, c->nbh);
-    k_ann_mean<T><<<gm, 128, 0, c->stream>>>(c->d_annmean, phi, c->d_bh, c->nz);
+    dim3 gm((c->nz + 31) / 32, c->nbh);
+    k_ann_mean<T><<<gm, 256, 0, c->stream>>>(c->d_annmean, phi, c->d_bh, c->nz);
     GW_CUDA(cudaGetLastError());
     GW_CUDA(cudaMemsetAsync(ad->mbar, 0, sizeof(double) * c->nbh * c->nz, c->stream));
     if (c->countz > 0) {
@@ -593,9 +641,14 @@ int advection_t(gw_ctx *c, T *a, PipeField<T> phi, double h, double ob_scale, do
                                                                c->d_pipe_b, c->d_bh, ncol, c->ny, c->nz,
                                                                c->countz);
         GW_CUDA(cudaGetLastError());
+        k_inner_sum<<<dim3((c->countz + 31) / 32, c->nbh), 256, 0, c->stream>>>(ad->S, ad->tmp, c->d_bh, c->countz);
+        GW_CUDA(cudaGetLastError());
         k_adv_t_scatter<T><<<nblocks(n, kB), kB, 0, c->stream>>>(
-            a, ad->tmp, phi, c->d_annmean, c->d_gz, c->d_pipe_i, c->d_pipe_j, c->d_pipe_b, c->d_bh, ad->mbar,
-            ad->sc, c->n_inner, ncol, c->ny, c->nz, c->countz, h);
+            a, ad->tmp, phi, c->d_advtab, c->d_gz, c->d_pipe_i, c->d_pipe_j, c->d_pipe_b, ad->sc, c->n_inner,
+            ncol, c->ny, c->nz, c->countz, h);
+        GW_CUDA(cudaGetLastError());
+        k_turn_apply<<<dim3((c->countz + 127) / 128, c->nbh), 128, 0, c->stream>>>(
+            ad->mbar, ad->sc, ad->S, c->d_annmean, c->d_advtab, c->d_gz, c->d_bh, c->nz, c->countz, h);
         GW_CUDA(cudaGetLastError());
     }
     const long long nf = (long long)ncol * c->nz;
@@ -670,19 +723,19 @@ int forward_store(gw_ctx *c, const float *un, StepStore<float> &S, double dt, in
     gw_rock2_coefs(s, &mu, &nu, &kappa, &sigma, &tau);
     const long long n = (long long)c->nx * c->ny * c->nz;
     const size_t bytes = (size_t)n * sizeof(float);
-    const unsigned nb = nblocks(n, kB);
+    const dim3 nb = cell_grid(c);
     const float *gm2 = nullptr, *gm1 = un;
     for (int j = 1; j <= s - 2; ++j) {
         float *out = S.g[j - 1];
         k_zstage_theta<<<nb, kB, 0, c->stream>>>(out, gm1, gm2, c->d_colprof, c->c32.czm, c->c32.czp, c->f_fref,
-                                                 c->nz, n, (float)(dt * mu[j - 1]),
+                                                 c->nz, (long long)c->nx * c->ny, (float)(dt * mu[j - 1]),
                                                  (float)(j == 1 ? 0.0 : kappa[j - 1]));
         GW_CUDA(cudaGetLastError());
         gm2 = gm1;
         gm1 = out;
     }
     k_zstage_theta<<<nb, kB, 0, c->stream>>>(S.g[s - 2], gm1, nullptr, c->d_colprof, c->c32.czm, c->c32.czp,
-                                             c->f_fref, c->nz, n, (float)(dt * sigma), 0.f);
+                                             c->f_fref, c->nz, (long long)c->nx * c->ny, (float)(dt * sigma), 0.f);
     GW_CUDA(cudaGetLastError());
     GW_CUDA(cudaMemcpyAsync(c->f_u, un, bytes, cudaMemcpyDeviceToDevice, c->stream));
     int rc;
@@ -778,7 +831,8 @@ int check_common(gw_ctx *c, double dt, int max_stages, int *s) {
     GW_CUDA(cudaSetDevice(c->device));
     if ((rc = gw_rock2_choose(dt, c->eigen_estimate, max_stages, s, &covered))) return rc;
     if ((rc = ensure_adj(c)) || (rc = gw_ensure_factors(c, dt / 2))) return rc;
-    return GW_OK;
+    // the half step's departure table (gw_step keeps it for its own dt)
+    return gw_fused_set_dt(c, dt);
 }
 
 struct DevBlock {

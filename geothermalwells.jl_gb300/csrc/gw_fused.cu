@@ -402,7 +402,6 @@ __global__ void __launch_bounds__(128) k_pipe_reduce(double *__restrict__ outlet
 // the grid, the velocities and dt, so it is built once per step size with the
 // same floating-point operations (fused multiply-adds as the reference's
 // @muladd) the per-cell evaluation would use.
-enum : int { kAdvKeep = 0, kAdvInterp = 1, kAdvTurn = 2, kAdvInlet = 3 };
 
 __global__ void k_adv_table(GwAdvRec *__restrict__ tab, const double *__restrict__ gz,
                             const GwBhDev *__restrict__ bh, const double *__restrict__ Tref, int nbh,

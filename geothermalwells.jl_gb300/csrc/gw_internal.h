@@ -15,7 +15,9 @@ struct GwBorehole {
     double v_inner, v_outer, insulation_depth;
 };
 
-// One departure record of the semi-Lagrangian advection (see k_adv_table).
+// One departure record of the semi-Lagrangian advection (see k_adv_table):
+// per (borehole, level, inner pipe / annulus), for a half step.
+enum : int { kAdvKeep = 0, kAdvInterp = 1, kAdvTurn = 2, kAdvInlet = 3 };
 struct GwAdvRec {
     double alpha;
     double dref;   // mixed path: alpha T_ref(ir) + (1 - alpha) T_ref(il) - T_ref(k)
