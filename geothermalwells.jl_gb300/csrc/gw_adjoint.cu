@@ -168,18 +168,22 @@ __global__ void __launch_bounds__(kB) k_explicit_t(T *__restrict__ dst, const T 
 // (super-diagonal cu_l), so M^T = Ut^T Lt^T:
 //   forward  z_l = R_l - cu_{l-1} z_{l-1}
 //   backward x_l = (z_l - a_{l+1} x_{l+1}) ib_l
-template <typename T>
+template <typename T, bool PARAM>
 __global__ void __launch_bounds__(128) k_thomas_t(T *__restrict__ U, const T *__restrict__ R,
                                                   const int *__restrict__ zclass, const T *__restrict__ fa,
                                                   const T *__restrict__ fib, const T *__restrict__ fcu,
-                                                  int nx, int ny, int nz, int dir) {
+                                                  int nx, int ny, int nz, int dir, double *__restrict__ G,
+                                                  const T *__restrict__ phi, const T *__restrict__ lam2,
+                                                  const T *__restrict__ wm, const T *__restrict__ wp,
+                                                  const unsigned char *__restrict__ rock, double beta) {
     const int nl = dir == 0 ? ny : nx;
     const int N = dir == 0 ? nx : ny;
     long long L = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= (long long)nz * nl) return;
     const int k = (int)(L % nz);
     const int m = (int)(L / nz);
-    const size_t fb = ((size_t)__ldg(zclass + k) * nl + m) * N;
+    const int zc = __ldg(zclass + k);
+    const size_t fb = ((size_t)zc * nl + m) * N;
     long long stride, off0;
     if (dir == 0) { stride = (long long)nz * ny; off0 = k + (long long)nz * m; }
     else { stride = nz; off0 = k + (long long)nz * ny * m; }
@@ -190,13 +194,36 @@ __global__ void __launch_bounds__(128) k_thomas_t(T *__restrict__ U, const T *__
         U[o] = z;
         cprev = __ldg(fcu + fb + l);
     }
+    // rock flags along the line: rock[(zc * nx + i) * ny + j]
+    const unsigned char *rk = rock + (size_t)zc * nx * ny;
+    const long long rst = dir == 0 ? (long long)ny : 1;
+    const long long r0 = dir == 0 ? m : (long long)m * ny;
+    const long long oN = off0 + (long long)(N - 1) * stride;
     T x = z * __ldg(fib + fb + N - 1);
-    U[off0 + (long long)(N - 1) * stride] = x;
+    U[oN] = x;
+    T acc = T(0), lnext = T(0), fnext = T(0);
+    int rnext = 0;
+    if (PARAM) {
+        lnext = x + (lam2 ? lam2[oN] : T(0));
+        fnext = phi[oN];
+        rnext = __ldg(rk + r0 + (N - 1) * rst);
+    }
     for (int l = N - 2; l >= 0; --l) {
         const long long o = off0 + l * stride;
         x = fma(-__ldg(fa + fb + l + 1), x, U[o]) * __ldg(fib + fb + l);
         U[o] = x;
+        if (PARAM) {
+            // face (l, l+1): (phi_{l+1} - phi_l)(L_l wp_l - L_{l+1} wm_{l+1}), both cells' rock flags
+            const T lc = x + (lam2 ? lam2[o] : T(0));
+            const T fc = phi[o];
+            const int rc = __ldg(rk + r0 + l * rst);
+            acc += T(rc + rnext) * ((fnext - fc) * (lc * __ldg(wp + fb + l) - lnext * __ldg(wm + fb + l + 1)));
+            lnext = lc;
+            fnext = fc;
+            rnext = rc;
+        }
     }
+    if (PARAM && acc != T(0)) atomicAdd(G + k, beta * (double)acc);
 }
 
 // ---------------------------------------------------------------------------
@@ -614,12 +641,22 @@ int launch_explicit_t(gw_ctx *c, T *dst, const T *src, double h, int dir) {
 }
 
 template <typename T>
-int launch_thomas_t(gw_ctx *c, T *U, const T *R, int dir) {
+int launch_thomas_t(gw_ctx *c, T *U, const T *R, int dir, const T *phi = nullptr, const T *lam2 = nullptr,
+                    double beta = 0.0) {
     const long long lines = (long long)c->nz * (dir == GW_DIR_X ? c->ny : c->nx);
     Tabs<T> tb = tabs(c, (T *)nullptr);
     const GwFactors<T> &f = dir == GW_DIR_X ? tb.ct->fx : tb.ct->fy;
-    k_thomas_t<T><<<nblocks(lines, 128), 128, 0, c->stream>>>(U, R, c->d_zclass, f.a, f.ib, f.cu, c->nx,
-                                                             c->ny, c->nz, dir);
+    const T *wm = dir == GW_DIR_X ? tb.wxm : tb.wym;
+    const T *wp = dir == GW_DIR_X ? tb.wxp : tb.wyp;
+    // with phi: the conductivity face terms of (lambda + lam2)^T A phi along the lines, lambda the solution
+    if (phi)
+        k_thomas_t<T, true><<<nblocks(lines, 128), 128, 0, c->stream>>>(
+            U, R, c->d_zclass, f.a, f.ib, f.cu, c->nx, c->ny, c->nz, dir, c->adj->G, phi, lam2, wm, wp,
+            c->adj->rock, beta);
+    else
+        k_thomas_t<T, false><<<nblocks(lines, 128), 128, 0, c->stream>>>(
+            U, R, c->d_zclass, f.a, f.ib, f.cu, c->nx, c->ny, c->nz, dir, nullptr, nullptr, nullptr, nullptr,
+            nullptr, nullptr, 0.0);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }
@@ -757,15 +794,14 @@ int adjoint_step(gw_ctx *c, const T *un, const T *un1, StepStore<T> &S, T *B[3],
     gw_rock2_coefs(s, &mu, &nu, &kappa, &sigma, &tau);
     const double h = dt / 2;
     int rc;
-    // u^{n+1} = (I - h A_y)^{-1} t4
-    if ((rc = launch_thomas_t<T>(c, B[1], B[0], GW_DIR_Y)) || (rc = launch_param<T>(c, B[1], un1, h, GW_DIR_Y)))
-        return rc;
+    // u^{n+1} = (I - h A_y)^{-1} t4  (face terms of t4bar^T A_y u^{n+1} in the same sweep)
+    if ((rc = launch_thomas_t<T>(c, B[1], B[0], GW_DIR_Y, un1, (const T *)nullptr, h))) return rc;
     // t4 = advection(tC)
     if ((rc = advection_t<T>(c, B[1], S.pC, h, ob_scale, ob_add))) return rc;
-    // tC = (I + h A_x) u1 ; u1 = (I - h A_x)^{-1} t2
+    // tC = (I + h A_x) u1 ; u1 = (I - h A_x)^{-1} t2: both with A_x applied to u1,
+    // so one sweep sums the face terms of (t2bar + tCbar)^T A_x u1
     if ((rc = launch_explicit_t<T>(c, B[2], B[1], h, GW_DIR_X)) ||
-        (rc = launch_param<T>(c, B[1], S.u1, h, GW_DIR_X)) || (rc = launch_thomas_t<T>(c, B[0], B[2], GW_DIR_X)) ||
-        (rc = launch_param<T>(c, B[0], S.u1, h, GW_DIR_X)))
+        (rc = launch_thomas_t<T>(c, B[0], B[2], GW_DIR_X, S.u1, B[1], h)))
         return rc;
     // t2 = advection(tA)
     if ((rc = advection_t<T>(c, B[0], S.pA, h, 0.0, 0.0))) return rc;
