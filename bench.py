@@ -278,7 +278,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32+f64acc", "data": "synthetic",
+        "dtype": "f64" if args.precision == "fp64" else "f32 (f64 outlet and energy balance)", "data": "synthetic",
         "config": {"workload": w["name"], "cells": ncell, "dt_s": dt, "rock2_stages": s.value,
                    "precision": args.precision, "l2": "inputs larger than L2 (field %.0f MB)"
                    % (ncell * 8 / 1e6), "parallelism": "replicas" if world > 1 else "single"},
@@ -415,7 +415,7 @@ def run_ensemble(args):
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_tuned / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if prec == "fp64" else "f32+f64acc", "data": "synthetic",
+            "dtype": "f64" if prec == "fp64" else "f32 (f64 outlet and energy balance)", "data": "synthetic",
             "config": {"workload": "ensemble_64_designs_3x3_arrays", "designs": len(designs),
                        "cells": cells, "dt_s": dt, "setup_s": setup_s,
                        "grid_range": [min(len(d["gridx"]) for d in designs),
@@ -552,7 +552,7 @@ def run_adjoint(args):
                    "peak_device_gb": r64.peak_bytes / 1e9}
     line = {"metric": "adjoint cost (multiple of one forward solve)", "value": adj_ms / fwd_ms,
             "unit": "x", "n_gpus": 1, "steps": nsteps, "higher_is_better": False,
-            "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32+f64acc", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32 (f64 outlet and energy balance)", "data": "synthetic",
             "config": {"workload": w["name"], "cells": cells, "dt_s": dt, "checkpoint_every": K,
                        "checkpoints": r.checkpoints, "stages": r.stages, "precision": prec,
                        "params": "k_rock_layers[22], mdot, T_inlet"},

@@ -36,7 +36,9 @@ extern "C" {
 #define GW_ERR_UNSUPPORTED 5  /* a feature the device path does not offer */
 
 #define GW_PREC_FP64 0        /* all storage and arithmetic in double */
-#define GW_PREC_MIXED 1       /* float storage/Thomas, double ROCK2 accumulation + energy balance */
+#define GW_PREC_MIXED 1       /* float theta = T - T_ref(z) storage, ROCK2 stages (as increments,
+                                 rounded into the field once per step) and Thomas sweeps; double
+                                 outlet / annulus means, pipe interpolation offsets, energy balance */
 
 #define GW_INLET_CONSTANT 0        /* ConstantInlet, src/physics.jl:290-293 */
 #define GW_INLET_HEAT_EXCHANGER 1  /* HeatExchangerInlet, src/physics.jl:303-306 */
