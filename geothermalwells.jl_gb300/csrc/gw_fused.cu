@@ -615,6 +615,35 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                     dr += rst;
                 }
             }
+        } else if (l0 + HR <= N) {
+            // full chunk of a line through pipe columns: the same grouped rows,
+            // with the advected pipe value (times ib) in place of the explicit
+            // sweep at the pipe rows
+#pragma unroll
+            for (int r0 = 0; r0 < HR; r0 += kHG) {
+                Quad<T> q[kHG];
+                T xm[kHG], xc[kHG], xp[kHG], pv[kHG], iv[kHG];
+                int pq[kHG];
+#pragma unroll
+                for (int g = 0; g < kHG; ++g) {
+                    q[g] = qc[r0 + g];
+                    const T *rw = row + (r0 + g) * kRow;
+                    xm[g] = rw[0]; xc[g] = rw[32]; xp[g] = rw[64];
+                    pq[g] = pipe_levels ? __ldg(pline + l0 + r0 + g) : -1;
+                }
+#pragma unroll
+                for (int g = 0; g < kHG; ++g) {
+                    pv[g] = pq[g] >= 0 ? pp[(size_t)pq[g] * countz + k] : T(0);
+                    iv[g] = pq[g] >= 0 ? __ldg(fib + fb + l0 + r0 + g) : T(0);
+                }
+#pragma unroll
+                for (int g = 0; g < kHG; ++g) {
+                    const T ay = q[g].w * y;
+                    y = pq[g] >= 0 ? fma(pv[g], iv[g], -ay) : fma(q[g].x, xc[g], fma(q[g].y, xp[g], fma(q[g].z, xm[g], -ay)));
+                    if (active) *dr = y;
+                    dr += rst;
+                }
+            }
         } else {
             const int rmax = min(HR, N - l0);
             for (int r = 0; r < rmax; ++r) {
