@@ -152,8 +152,10 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
                                                    const T *__restrict__ sc, int s, int nz,
                                                    long long ncols) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *stage = reinterpret_cast<T *>(smem_raw);   // [2][spad(256 * LPT)]
-    const int nzs = spad(256 * LPT);
+    // nt = blockDim.x threads (a multiple of 32, at most 256), LPT levels each
+    const int nt = blockDim.x;
+    T *stage = reinterpret_cast<T *>(smem_raw);   // [2][spad(nt * LPT)]
+    const int nzs = spad(nt * LPT);
     // run ends of every thread, shifted by one slot so thread t reads its
     // neighbours at [t] (left, from s_hi) and [t + 1] (right, from s_lo)
     // without predicates; the outer slots hold zeros.
@@ -162,19 +164,19 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
     const int kb = t * LPT;
     const int nrec = s - 2;
     int xb = 0;
-    // The column is padded to 256 * LPT levels: pad levels start at zero and
+    // The column is padded to nt * LPT levels: pad levels start at zero and
     // have zero coefficients, so they never feed a real level (the real
     // bottom level's cp is 0) and every thread owns exactly LPT levels.
-    for (int k = nz + t; k < 256 * LPT; k += 256) { stage[spad(k)] = T(0); stage[nzs + spad(k)] = T(0); }
-    if (t < 2) { s_hi[t][0] = T(0); s_lo[t][256] = T(0); }
-    // thread t copies levels t + 256 i, whose padded slots are spad(t) + 264 i
-    const int st0 = spad(t);
+    for (int k = nz + t; k < nt * LPT; k += nt) { stage[spad(k)] = T(0); stage[nzs + spad(k)] = T(0); }
+    if (t < 2) { s_hi[t][0] = T(0); s_lo[t][nt] = T(0); }
+    // thread t copies levels t + nt i, whose padded slots are spad(t) + nts i
+    const int st0 = spad(t), nts = nt + nt / 32;
     auto fetch = [&](long long col, int buf) {
         T *d = stage + (size_t)buf * nzs + st0;
         const T *g = u + col * nz + t;
 #pragma unroll
         for (int i = 0; i < LPT; ++i)
-            if (t + 256 * i < nz) cp_async<sizeof(T)>(d + 264 * i, g + 256 * i, true);
+            if (t + nt * i < nz) cp_async<sizeof(T)>(d + nts * i, g + nt * i, true);
         cp_async_commit();
     };
     auto exchange = [&](const T (&v)[LPT], T &left, T &right) {
@@ -285,7 +287,7 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
         T *uc = u + col * nz + t;
 #pragma unroll
         for (int i = 0; i < LPT; ++i)
-            if (t + 256 * i < nz) uc[256 * i] = st[st0 + 264 * i];
+            if (t + nt * i < nz) uc[nt * i] = st[st0 + nts * i];
         __syncthreads();   // this buffer is refilled by the next iteration's fetch
     }
 }
@@ -869,7 +871,7 @@ size_t rock2_smem(int nz) {
 }
 
 template <typename T>
-size_t reg_smem(int lpt) { return 2 * (size_t)(256 * lpt + 8 * lpt) * sizeof(T); }
+size_t reg_smem(int lpt, int nt = 256) { return 2 * (size_t)(nt * lpt + nt * lpt / 32) * sizeof(T); }
 
 // levels per thread of the register-resident ROCK2 kernel (0: use the
 // shared-memory kernel)
@@ -897,10 +899,10 @@ int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *
     const int lpt = rock2_lpt(c->nz);
     unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid ? ncols : c->rock2_grid);
     switch (lpt) {
-        case 2: k_rock2_reg<T, INC, 2><<<grid, 256, reg_smem<T>(2), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 4: k_rock2_reg<T, INC, 4><<<grid, 256, reg_smem<T>(4), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 8: k_rock2_reg<T, INC, 8><<<grid, 256, reg_smem<T>(8), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 16: k_rock2_reg<T, INC, 16><<<grid, 256, reg_smem<T>(16), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 2: k_rock2_reg<T, INC, 2><<<grid, c->rock2_nt, reg_smem<T>(2, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 4: k_rock2_reg<T, INC, 4><<<grid, c->rock2_nt, reg_smem<T>(4, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 8: k_rock2_reg<T, INC, 8><<<grid, c->rock2_nt, reg_smem<T>(8, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 16: k_rock2_reg<T, INC, 16><<<grid, c->rock2_nt, reg_smem<T>(16, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
         default:
             k_rock2_col<T, INC><<<grid, 256, rock2_smem<T>(c->nz), c->stream>>>(u, c->d_colprof, czm, czp, fref,
                                                                             c->d_stage, s, c->nz, ncols);
@@ -1077,11 +1079,15 @@ int gw_fused_supported(const gw_ctx *c) {
     return need <= 200 * 1024;
 }
 
+// The shared-memory limit is an attribute of the kernel, shared by every
+// context: set it to the largest block (256 threads) of that LPT, and size
+// the occupancy query by this context's block.
 template <typename K>
-static cudaError_t occupancy(int *n, K kernel, size_t smem) {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+static cudaError_t occupancy(int *n, K kernel, size_t smem, int nt = 256, size_t smem_max = 0) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)std::max(smem, smem_max));
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, kernel, 256, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, kernel, nt, smem);
 }
 
 int gw_fused_prepare(gw_ctx *c) {
@@ -1099,11 +1105,16 @@ int gw_fused_prepare(gw_ctx *c) {
     // the column kernels loop over columns: one resident wave of blocks
     int per_sm = 0;
     const bool mix = c->precision == GW_PREC_MIXED;
-    switch (rock2_lpt(c->nz)) {
-        case 2: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 2>, reg_smem<float>(2)) : occupancy(&per_sm, k_rock2_reg<double, false, 2>, reg_smem<double>(2)); break;
-        case 4: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 4>, reg_smem<float>(4)) : occupancy(&per_sm, k_rock2_reg<double, false, 4>, reg_smem<double>(4)); break;
-        case 8: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 8>, reg_smem<float>(8)) : occupancy(&per_sm, k_rock2_reg<double, false, 8>, reg_smem<double>(8)); break;
-        case 16: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 16>, reg_smem<float>(16)) : occupancy(&per_sm, k_rock2_reg<double, false, 16>, reg_smem<double>(16)); break;
+    // threads per column block: the fewest multiples of 32 that cover nz at
+    // LPT levels each (at most 256)
+    const int lpt = rock2_lpt(c->nz);
+    c->rock2_nt = lpt > 0 ? std::min(256, ((c->nz + lpt - 1) / lpt + 31) / 32 * 32) : 256;
+    const int nt = c->rock2_nt;
+    switch (lpt) {
+        case 2: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 2>, reg_smem<float>(2, nt), nt, reg_smem<float>(2)) : occupancy(&per_sm, k_rock2_reg<double, false, 2>, reg_smem<double>(2, nt), nt, reg_smem<double>(2)); break;
+        case 4: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 4>, reg_smem<float>(4, nt), nt, reg_smem<float>(4)) : occupancy(&per_sm, k_rock2_reg<double, false, 4>, reg_smem<double>(4, nt), nt, reg_smem<double>(4)); break;
+        case 8: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 8>, reg_smem<float>(8, nt), nt, reg_smem<float>(8)) : occupancy(&per_sm, k_rock2_reg<double, false, 8>, reg_smem<double>(8, nt), nt, reg_smem<double>(8)); break;
+        case 16: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 16>, reg_smem<float>(16, nt), nt, reg_smem<float>(16)) : occupancy(&per_sm, k_rock2_reg<double, false, 16>, reg_smem<double>(16, nt), nt, reg_smem<double>(16)); break;
         default:
             e = mix ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rock2_col<float, true>, 256,
                                                                     rock2_smem<float>(c->nz))

@@ -118,6 +118,7 @@ struct gw_ctx {
     double *d_tp = nullptr;           // double path: [ncol][nz] swept pipe columns
     double *d_pp = nullptr;           // double path: [ncol][countz] advected pipe values
     int rock2_grid = 0;
+    int rock2_nt = 256;               // threads per block of the ROCK2 column kernel
     int half_cfg = 0;                 // half-step tiling (gw_fused.cu kTileHW/kTileHR)
     bool fused = false;
     // mixed path state (GW_PREC_MIXED): theta = T - T_ref(z) in float
