@@ -19,7 +19,9 @@ struct gw_batch {
     cudaStream_t stream = nullptr;
     cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> join;
-    cudaGraphExec_t graph = nullptr;
+    // graph = kSteps steps of every design between one fork and one join
+    // (designs do not wait for each other every step); graph1 = one step
+    cudaGraphExec_t graph = nullptr, graph1 = nullptr;
     double graph_dt = -1.0;
     int graph_steps_cap = -1;
     std::vector<int> graph_s;
@@ -28,6 +30,36 @@ struct gw_batch {
 };
 
 namespace {
+constexpr int kSteps = 4;   // steps per design between the ensemble's fork and join
+
+// Capture `steps` steps of every design, each design on its own stream,
+// between one fork and one join on the batch stream.
+int capture(gw_batch *b, double dt, const std::vector<int> &s, int steps, cudaGraphExec_t *out) {
+    const int n = (int)b->ctx.size();
+    cudaGraph_t g;
+    GW_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    int r = GW_OK;
+    cudaError_t e = cudaEventRecord(b->fork, b->stream);
+    for (int d = 0; d < n && e == cudaSuccess && r == GW_OK; ++d) {
+        gw_ctx *c = b->ctx[d];
+        if ((e = cudaStreamWaitEvent(c->stream, b->fork, 0)) != cudaSuccess) break;
+        for (int k = 0; k < steps && r == GW_OK; ++k) r = gw_fused_step(c, dt, s[d]);
+        if (r != GW_OK) break;
+        if ((e = cudaEventRecord(b->join[d], c->stream)) != cudaSuccess) break;
+        e = cudaStreamWaitEvent(b->stream, b->join[d], 0);
+    }
+    cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
+    if (r != GW_OK || e != cudaSuccess || ee != cudaSuccess) {
+        if (ee == cudaSuccess) cudaGraphDestroy(g);
+        if (r != GW_OK) return r;
+        return gw_cuda_fail(e != cudaSuccess ? e : ee, "ensemble step capture");
+    }
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return gw_cuda_fail(e, "cudaGraphInstantiate");
+    return GW_OK;
+}
+
 int prepare(gw_ctx *c, double dt, int max_stages, int nsteps, int *s_out) {
     int s, covered, rc;
     if ((rc = gw_rock2_choose(dt, c->eigen_estimate, max_stages, &s, &covered))) return rc;
@@ -73,6 +105,7 @@ int gw_batch_destroy(gw_batch *b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->graph1) cudaGraphExecDestroy(b->graph1);
     for (cudaEvent_t ev : b->join) if (ev) cudaEventDestroy(ev);
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->ev0) cudaEventDestroy(b->ev0);
@@ -183,26 +216,8 @@ int gw_batch_step(gw_batch *b, double dt, int nsteps, int max_stages) {
     if (!b->graph || b->graph_dt != dt || b->graph_s != s || b->graph_gen != gen ||
         b->graph_steps_cap < nsteps) {
         if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
-        cudaGraph_t g;
-        GW_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        int r = GW_OK;
-        cudaError_t e = cudaEventRecord(b->fork, b->stream);
-        for (int d = 0; d < n && e == cudaSuccess && r == GW_OK; ++d) {
-            gw_ctx *c = b->ctx[d];
-            if ((e = cudaStreamWaitEvent(c->stream, b->fork, 0)) != cudaSuccess) break;
-            if ((r = gw_fused_step(c, dt, s[d]))) break;
-            if ((e = cudaEventRecord(b->join[d], c->stream)) != cudaSuccess) break;
-            e = cudaStreamWaitEvent(b->stream, b->join[d], 0);
-        }
-        cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
-        if (r != GW_OK || e != cudaSuccess || ee != cudaSuccess) {
-            if (ee == cudaSuccess) cudaGraphDestroy(g);
-            if (r != GW_OK) return r;
-            return gw_cuda_fail(e != cudaSuccess ? e : ee, "ensemble step capture");
-        }
-        e = cudaGraphInstantiate(&b->graph, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return gw_cuda_fail(e, "cudaGraphInstantiate");
+        if (b->graph1) { cudaGraphExecDestroy(b->graph1); b->graph1 = nullptr; }
+        if ((rc = capture(b, dt, s, kSteps, &b->graph)) || (rc = capture(b, dt, s, 1, &b->graph1))) return rc;
         b->graph_dt = dt;
         b->graph_s = s;
         b->graph_gen = gen;
@@ -210,7 +225,8 @@ int gw_batch_step(gw_batch *b, double dt, int nsteps, int max_stages) {
     }
     for (gw_ctx *c : b->ctx) GW_CUDA(cudaStreamSynchronize(c->stream));
     GW_CUDA(cudaEventRecord(b->ev0, b->stream));
-    for (int k = 0; k < nsteps; ++k) GW_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    for (int k = 0; k + kSteps <= nsteps; k += kSteps) GW_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    for (int k = 0; k < nsteps % kSteps; ++k) GW_CUDA(cudaGraphLaunch(b->graph1, b->stream));
     GW_CUDA(cudaEventRecord(b->ev1, b->stream));
     GW_CUDA(cudaStreamSynchronize(b->stream));
     float ms = 0.f;
