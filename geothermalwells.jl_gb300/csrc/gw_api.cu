@@ -452,6 +452,16 @@ int gw_init_thermal_gradient(gw_ctx *c, double T_surface, double gradient) {
     return gw_set_field(c, T.data());
 }
 
+int gw_lincomb(gw_ctx *c, double *dst, int n, const double *coeffs, const double *const *srcs) {
+    if (!c || !dst || (n > 0 && (!coeffs || !srcs))) return gw_fail(GW_ERR_ARG, "NULL argument");
+    if (n < 0 || n > 8) return gw_fail(GW_ERR_ARG, "gw_lincomb takes 0 to 8 sources");
+    for (int q = 0; q < n; ++q)
+        if (!srcs[q]) return gw_fail(GW_ERR_ARG, "source field pointer is NULL");
+    int rc = set_device(c);
+    if (rc || (rc = gw_launch_lincomb(c, dst, n, coeffs, srcs))) return rc;
+    return sync(c);
+}
+
 int gw_rhs_diffusion_z(gw_ctx *c, double *dphi, const double *phi) {
     if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
     int rc = check_field_ptrs(dphi, phi);

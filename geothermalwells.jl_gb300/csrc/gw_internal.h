@@ -181,6 +181,7 @@ int gw_launch_thomas(gw_ctx *c, double *U, const double *RHS, int dir);
 int gw_launch_advection(gw_ctx *c, double *phi, double dt);
 int gw_launch_record(gw_ctx *c, double dt);
 int gw_launch_check_finite(gw_ctx *c, const double *u, size_t n);
+int gw_launch_lincomb(gw_ctx *c, double *dst, int n, const double *w, const double *const *src);
 int gw_ensure_factors(gw_ctx *c, double h);
 int gw_prepare_step(gw_ctx *c, double dt, int s, int nsteps);
 

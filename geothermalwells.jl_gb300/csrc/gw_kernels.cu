@@ -285,6 +285,24 @@ __global__ void k_record(double *__restrict__ series, double *__restrict__ energ
     if (b == 0) *counter = n + 1;
 }
 
+// dst = sum_i w_i src_i (up to 8 sources), grid-stride over the cells.
+struct LinComb {
+    const double *src[8];
+    double w[8];
+    int n;
+};
+
+__global__ void __launch_bounds__(256) k_lincomb(double *dst, LinComb lc, size_t ncell) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < ncell; i += stride) {
+        double v = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (q < lc.n) v = fma(lc.w[q], lc.src[q][i], v);
+        dst[i] = v;
+    }
+}
+
 __global__ void k_check_finite(const double *__restrict__ u, size_t n, int *__restrict__ flag) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t s = (size_t)gridDim.x * blockDim.x;
@@ -350,6 +368,16 @@ int gw_launch_record(gw_ctx *c, double dt) {
     k_record<<<1, threads, 0, c->stream>>>(c->d_series, c->d_energy, c->d_step_counter, c->d_outlet,
                                            c->d_bh, c->nbh, c->series_cap, dt,
                                            c->rho_c_water / 998.2, c->inlet_kind, c->inlet_param);
+    GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}
+
+int gw_launch_lincomb(gw_ctx *c, double *dst, int n, const double *w, const double *const *src) {
+    LinComb lc{};
+    for (int q = 0; q < n; ++q) { lc.src[q] = src[q]; lc.w[q] = w[q]; }
+    lc.n = n;
+    const size_t N = (size_t)c->nx * c->ny * c->nz;
+    k_lincomb<<<152 * 8, 256, 0, c->stream>>>(dst, lc, N);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }

@@ -70,6 +70,7 @@ SIGNATURES = {
     "gw_get_field": (_i, [_vp, _dp]),
     "gw_init_thermal_gradient": (_i, [_vp, _d, _d]),
     "gw_rhs_diffusion_z": (_i, [_vp, _vp, _vp]),
+    "gw_lincomb": (_i, [_vp, _vp, _i, _dp, ctypes.POINTER(_vp)]),
     "gw_diffusion_1d": (_i, [_vp, _vp, _vp, _d, _i, _i]),
     "gw_thomas": (_i, [_vp, _vp, _vp, _d, _i]),
     "gw_advection": (_i, [_vp, _vp, _d, _d]),

@@ -56,6 +56,18 @@ def advection(phi, dt, t, cache):
     _lib.check(_lib.load().gw_advection(cache.ctx, _devptr(phi, cache), float(dt), float(t)))
 
 
+def lincomb(dst, coeffs, srcs, cache):
+    """dst = sum_i coeffs[i] * srcs[i] on device fields (up to 8; dst may be
+    one of the sources): the vector updates of an integrator's stages."""
+    import ctypes
+    n = len(srcs)
+    if n != len(coeffs):
+        raise ValueError("one coefficient per source field")
+    w = np.ascontiguousarray(coeffs, dtype=np.float64)
+    ptrs = (ctypes.c_void_p * max(n, 1))(*[_devptr(x, cache) for x in srcs])
+    _lib.check(_lib.load().gw_lincomb(cache.ctx, _devptr(dst, cache), n, _lib.dptr(w), ptrs))
+
+
 def ADI_and_ADV_callback(u, temp, t, dt, cache):
     """``ADI_and_ADV_callback!``, ``src/solver.jl:432-464``, with the
     integrator's ``u``, ``uprev`` (as scratch), ``t`` and ``t - tprev``."""

@@ -119,6 +119,14 @@ int gw_advection(gw_ctx *ctx, double *phi_dev, double dt, double t);
  * temp = integrator.uprev (clobbered), t = integrator.t, dt = t - tprev. */
 int gw_adi_adv(gw_ctx *ctx, double *u_dev, double *temp_dev, double t, double dt);
 
+/* dst = sum_i coeffs[i] * srcs[i] over the context's N = nx*ny*nz cells, n <= 8
+ * device fields (dst may be one of them).  The vector updates an ODE
+ * integrator's stages make (the `@..` broadcasts of ROCK2's perform_step!)
+ * for callers that hold the state on the device and use no other GPU
+ * library. */
+int gw_lincomb(gw_ctx *ctx, double *dst_dev, int n, const double *coeffs,
+               const double *const *srcs_dev);
+
 /* ---- fused step on the context's own state ---- */
 /* Advance u by nsteps fixed steps of size dt from time t0: per step one
  * ROCK2 step of rhs_diffusion_z! (stage count from the eigenvalue estimate,

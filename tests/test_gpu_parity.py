@@ -260,3 +260,21 @@ def test_overlapped_step_is_bitwise_the_in_line_step(case, precision, gwlib):
         cache.close()
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_lincomb(gwlib, torch_cuda):
+    """gw_lincomb: dst = sum of weighted fields, dst aliasing a source."""
+    from geothermalwells_gb300.solver import lincomb
+    torch = torch_cuda
+    w = W.small_case()
+    cache, _ = make(w)
+    rng = np.random.default_rng(9)
+    fields = [rng.uniform(-5, 5, cache.N) for _ in range(5)]
+    dev = [torch.from_numpy(f.copy()).cuda() for f in fields]
+    coeffs = [0.5, -1.25, 3.0, 1e-3, -2.0]
+    out = torch.zeros(cache.N, dtype=torch.float64, device="cuda")
+    lincomb(out, coeffs, dev, cache)
+    ref = sum(c * f for c, f in zip(coeffs, fields))
+    assert np.max(np.abs(out.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
+    lincomb(dev[0], [2.0, 1.0], [dev[0], dev[1]], cache)   # in place
+    assert np.max(np.abs(dev[0].cpu().numpy() - (2 * fields[0] + fields[1]))) <= 1e-13 * 20
