@@ -863,6 +863,8 @@ int finish_grad(gw_ctx *c, double dt, int nsteps, double wE, double *grad) {
 
 int check_common(gw_ctx *c, double dt, int max_stages, int *s) {
     if (!(dt > 0) || !std::isfinite(dt)) return gw_fail(GW_ERR_ARG, "dt must be positive and finite");
+    if (c->inlet_kind == GW_INLET_SCHEDULE)
+        return gw_fail(GW_ERR_UNSUPPORTED, "the adjoint takes constant or heat-exchanger inlets");
     int covered, rc;
     GW_CUDA(cudaSetDevice(c->device));
     if ((rc = gw_rock2_choose(dt, c->eigen_estimate, max_stages, s, &covered))) return rc;

@@ -91,13 +91,15 @@ int rock2_step(gw_ctx *c, double *u, double *g1, double *spare, double dt, int s
 
 // ADI_and_ADV_callback! (src/solver.jl:432-464) with the modular kernels.
 // The Thomas factors for h = dt/2 must be current (gw_ensure_factors).
-int adi_adv(gw_ctx *c, double *u, double *temp, double dt) {
+// t is the callback's time (the step's end): the advections see t and
+// t + dt/2 (src/solver.jl:447,458).
+int adi_adv(gw_ctx *c, double *u, double *temp, double dt, double t = 0.0) {
     int rc;
     if ((rc = gw_launch_explicit(c, temp, u, dt / 2, GW_DIR_Y))) return rc;
-    if ((rc = gw_launch_advection(c, temp, dt / 2))) return rc;
+    if ((rc = gw_launch_advection(c, temp, dt / 2, t))) return rc;
     if ((rc = gw_launch_thomas(c, u, temp, GW_DIR_X))) return rc;
     if ((rc = gw_launch_explicit(c, temp, u, dt / 2, GW_DIR_X))) return rc;
-    if ((rc = gw_launch_advection(c, temp, dt / 2))) return rc;
+    if ((rc = gw_launch_advection(c, temp, dt / 2, t + dt / 2))) return rc;
     return gw_launch_thomas(c, u, temp, GW_DIR_Y);
 }
 
@@ -158,6 +160,29 @@ int gw_cuda_fail(cudaError_t e, const char *what) {
 
 // Recompute the Thomas factors of (I - h A_x) and (I - h A_y) when h changes
 // (in double; the mixed path gets them rounded to float).
+// Start time and step size of the steps about to run, read on the device by
+// the schedule inlet (with the step counter).
+int gw_set_step_time(gw_ctx *c, double t0, double dt) {
+    const double v[2] = {t0, dt};
+    GW_CUDA(cudaMemcpyAsync(c->d_time, v, sizeof(v), cudaMemcpyHostToDevice, c->stream));
+    return GW_OK;
+}
+
+double gw_schedule_at(const gw_ctx *c, double t) {
+    const std::vector<double> &ts = c->sched_t, &vs = c->sched_T;
+    const int n = (int)ts.size();
+    if (n == 0) return 0.0;
+    if (t <= ts[0]) return vs[0];
+    if (t >= ts[n - 1]) return vs[n - 1];
+    int lo = 0, hi = n - 1;   // ts[lo] <= t < ts[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (ts[mid] <= t) lo = mid; else hi = mid;
+    }
+    const double a = (t - ts[lo]) / (ts[hi] - ts[lo]);
+    return std::fma(a, vs[hi] - vs[lo], vs[lo]);
+}
+
 int gw_ensure_factors(gw_ctx *c, double h) {
     if (h == c->factors_h) return GW_OK;
     std::vector<double> cxm, cxp, cym, cyp, czm, czp;
@@ -341,7 +366,8 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         (rc = dalloc(c, &c->d_advtab, (size_t)c->nbh * c->countz * 2)) ||
         (rc = dalloc(c, &c->d_outlet, c->nbh)) || (rc = dalloc(c, &c->d_energy, c->nbh)) ||
         (rc = dalloc(c, &c->d_stage, GW_STAGE_TABLE)) || (rc = dalloc(c, &c->f_stage, GW_STAGE_TABLE)) ||
-        (rc = dalloc(c, &c->d_step_counter, 1)) || (rc = dalloc(c, &c->d_flag, 1)))
+        (rc = dalloc(c, &c->d_step_counter, 1)) || (rc = dalloc(c, &c->d_flag, 1)) ||
+        (rc = dalloc(c, &c->d_time, 2)) || (rc = dalloc(c, &c->d_inlet, c->nbh)))
         return fail(rc);
     if (mixed(c)) {
         // f_temp and f_g1 are one block, so together they can stage a double field
@@ -452,6 +478,31 @@ int gw_init_thermal_gradient(gw_ctx *c, double T_surface, double gradient) {
     return gw_set_field(c, T.data());
 }
 
+int gw_set_inlet_schedule(gw_ctx *c, int n, const double *times, const double *values) {
+    if (!c || !times || !values) return gw_fail(GW_ERR_ARG, "NULL argument");
+    if (c->inlet_kind != GW_INLET_SCHEDULE)
+        return gw_fail(GW_ERR_ARG, "the context's inlet kind is not GW_INLET_SCHEDULE");
+    if (n < 1) return gw_fail(GW_ERR_ARG, "a schedule needs at least one point");
+    for (int q = 0; q < n; ++q) {
+        if (!std::isfinite(times[q]) || !std::isfinite(values[q]))
+            return gw_fail(GW_ERR_ARG, "schedule values must be finite");
+        if (q > 0 && !(times[q] > times[q - 1]))
+            return gw_fail(GW_ERR_ARG, "schedule times must be strictly increasing");
+    }
+    int rc = set_device(c);
+    if (rc) return rc;
+    c->sched_t.assign(times, times + n);
+    c->sched_T.assign(values, values + n);
+    if (n > c->n_sched) {
+        GW_CUDA(cudaStreamSynchronize(c->stream));
+        if ((rc = dalloc(c, &c->d_sched, 2 * (size_t)n))) return rc;   // the old one is freed at gw_destroy
+    }
+    c->n_sched = n;
+    std::vector<double> tv(times, times + n);
+    tv.insert(tv.end(), values, values + n);
+    return copy_to(c->d_sched, tv);
+}
+
 int gw_lincomb(gw_ctx *c, double *dst, int n, const double *coeffs, const double *const *srcs) {
     if (!c || !dst || (n > 0 && (!coeffs || !srcs))) return gw_fail(GW_ERR_ARG, "NULL argument");
     if (n < 0 || n > 8) return gw_fail(GW_ERR_ARG, "gw_lincomb takes 0 to 8 sources");
@@ -501,21 +552,19 @@ int gw_thomas(gw_ctx *c, double *U, const double *RHS, double dt, int dir) {
 }
 
 int gw_advection(gw_ctx *c, double *phi, double dt, double t) {
-    (void)t;
     if (!c || !phi) return gw_fail(GW_ERR_ARG, "NULL argument");
     int rc = set_device(c);
-    if (rc || (rc = gw_launch_advection(c, phi, dt))) return rc;
+    if (rc || (rc = gw_launch_advection(c, phi, dt, t))) return rc;
     return sync(c);
 }
 
 int gw_adi_adv(gw_ctx *c, double *u, double *temp, double t, double dt) {
-    (void)t;
     if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
     int rc = check_field_ptrs(u, temp);
     if (rc || (rc = set_device(c))) return rc;
     if (u == temp) return gw_fail(GW_ERR_ARG, "temp must not alias u");
     if ((rc = gw_ensure_factors(c, dt / 2))) return rc;
-    if ((rc = adi_adv(c, u, temp, dt))) return rc;
+    if ((rc = adi_adv(c, u, temp, dt, t))) return rc;
     return sync(c);
 }
 
@@ -525,7 +574,6 @@ int gw_rock2_stages(gw_ctx *c, double dt, int max_stages, int *stages, int *cove
 }
 
 int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
-    (void)t0;
     if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
     if (nsteps < 0) return gw_fail(GW_ERR_ARG, "nsteps must be >= 0");
     if (!(dt > 0) || !std::isfinite(dt)) return gw_fail(GW_ERR_ARG, "dt must be positive and finite");
@@ -533,7 +581,13 @@ int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
     if (rc) return rc;
     int s, covered;
     if ((rc = gw_rock2_choose(dt, c->eigen_estimate, max_stages, &s, &covered))) return rc;
+    if (c->inlet_kind == GW_INLET_SCHEDULE && (!c->fused || c->n_sched == 0))
+        return gw_fail(c->fused ? GW_ERR_ARG : GW_ERR_UNSUPPORTED,
+                       c->fused ? "no inlet schedule set (gw_set_inlet_schedule)"
+                                : "a schedule inlet needs the fused step");
     if ((rc = gw_prepare_step(c, dt, s, nsteps))) return rc;
+    if ((rc = gw_set_step_time(c, t0, dt))) return rc;
+    c->t_now = t0 + nsteps * dt;
     if (nsteps == 0) return sync(c);
     if (!c->graph || c->graph_dt != dt || c->graph_s != s || c->graph_gen != c->series_gen) {
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }

@@ -134,8 +134,10 @@ int gw_batch_autotune(gw_batch *b, double dt, int reps, int *tiling_out) {
     int rc;
     GW_CUDA(cudaSetDevice(b->device));
     const int n = (int)b->ctx.size();
-    // save the states (u into the g1 scratch) and the outlet / energy values
+    // save the states (u into the g1 scratch), the outlet / energy values and the clocks
     std::vector<std::vector<double>> outl(n), energy(n);
+    std::vector<double> clock(n);
+    for (int d = 0; d < n; ++d) clock[d] = b->ctx[d]->t_now;
     for (int d = 0; d < n; ++d) {
         gw_ctx *c = b->ctx[d];
         const size_t N = (size_t)c->nx * c->ny * c->nz;
@@ -196,6 +198,7 @@ int gw_batch_autotune(gw_batch *b, double dt, int reps, int *tiling_out) {
         GW_CUDA(cudaMemcpyAsync(c->d_outlet, outl[d].data(), c->nbh * sizeof(double), cudaMemcpyHostToDevice, c->stream));
         GW_CUDA(cudaMemcpyAsync(c->d_energy, energy[d].data(), c->nbh * sizeof(double), cudaMemcpyHostToDevice, c->stream));
         GW_CUDA(cudaStreamSynchronize(c->stream));
+        c->t_now = clock[d];
     }
     b->graph_dt = -1.0;
     return GW_OK;
@@ -208,8 +211,13 @@ int gw_batch_step(gw_batch *b, double dt, int nsteps, int max_stages) {
     const int n = (int)b->ctx.size();
     std::vector<int> s(n);
     int rc;
-    for (int d = 0; d < n; ++d)
-        if ((rc = prepare(b->ctx[d], dt, max_stages, nsteps, &s[d]))) return rc;
+    for (int d = 0; d < n; ++d) {
+        gw_ctx *c = b->ctx[d];
+        if (c->inlet_kind == GW_INLET_SCHEDULE && c->n_sched == 0)
+            return gw_fail(GW_ERR_ARG, "a design has no inlet schedule set (gw_set_inlet_schedule)");
+        if ((rc = prepare(c, dt, max_stages, nsteps, &s[d])) || (rc = gw_set_step_time(c, c->t_now, dt)))
+            return rc;
+    }
     if (nsteps == 0) return GW_OK;
     std::vector<int> gen(n);
     for (int d = 0; d < n; ++d) gen[d] = b->ctx[d]->series_gen;
@@ -232,7 +240,7 @@ int gw_batch_step(gw_batch *b, double dt, int nsteps, int max_stages) {
     float ms = 0.f;
     GW_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     b->last_ms = ms;
-    for (gw_ctx *c : b->ctx) c->last_nsteps = nsteps;
+    for (gw_ctx *c : b->ctx) { c->last_nsteps = nsteps; c->t_now += nsteps * dt; }
     return GW_OK;
 }
 

@@ -450,6 +450,28 @@ __global__ void k_adv_table(GwAdvRec *__restrict__ tab, const double *__restrict
     tab[e] = r;
 }
 
+// Schedule inlet: T_in at t = t0 + (n + 1 + off) dt for the step n the
+// counter holds (off 0: first advection, 1/2: second), for every borehole.
+__global__ void k_inlet_eval(double *__restrict__ inlet_v, const double *__restrict__ sched, int ns,
+                             const double *__restrict__ time, const int *__restrict__ counter, double off,
+                             int nbh) {
+    const double t = __fma_rn((double)(*counter) + 1.0 + off, time[1], time[0]);
+    const double *ts = sched, *vs = sched + ns;
+    double v;
+    if (t <= ts[0]) v = vs[0];
+    else if (t >= ts[ns - 1]) v = vs[ns - 1];
+    else {
+        int lo = 0, hi = ns - 1;   // ts[lo] <= t < ts[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (ts[mid] <= t) lo = mid; else hi = mid;
+        }
+        const double a = __ddiv_rn(__dsub_rn(t, ts[lo]), __dsub_rn(ts[hi], ts[lo]));
+        v = __fma_rn(a, __dsub_rn(vs[hi], vs[lo]), vs[lo]);
+    }
+    for (int b = threadIdx.x; b < nbh; b += blockDim.x) inlet_v[b] = v;
+}
+
 // kernel_advection! on the compact buffer with the departure table; the
 // result (minus T_ref in the mixed path) goes to pp[q][k], k < countz.
 template <typename T>
@@ -460,7 +482,7 @@ __global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *_
                                                   const double *__restrict__ outlet,
                                                   const double *__restrict__ Tref, int n_inner,
                                                   int ncol, int nz, int countz, int inlet_kind,
-                                                  double inlet_param) {
+                                                  double inlet_param, const double *__restrict__ inlet_v) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)ncol * countz) return;
     const int k = (int)(e % countz);
@@ -472,7 +494,8 @@ __global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *_
     if (r.type == kAdvKeep) {
         v = absT(col[k], Tref, k);
     } else if (r.type == kAdvInlet) {
-        v = inlet_kind == GW_INLET_CONSTANT ? inlet_param : outlet[b] - inlet_param;
+        v = inlet_kind == GW_INLET_CONSTANT ? inlet_param
+          : inlet_kind == GW_INLET_SCHEDULE ? inlet_v[b] : outlet[b] - inlet_param;
     } else if (r.type == kAdvTurn) {
         const double *m = ann_mean + (size_t)b * nz;
         v = __fma_rn(r.alpha, m[r.ir], __dmul_rn(__dsub_rn(1.0, r.alpha), m[r.il]));
@@ -940,11 +963,17 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h, cudaStream_t st = n
     k_pipe_reduce<<<gr, 128, 0, st>>>(c->d_outlet, c->d_annmean, c->d_pipepart, c->d_bchunk,
                                              c->d_gz, c->d_bh, c->nz, h);
     GW_CUDA(cudaGetLastError());
+    if (c->inlet_kind == GW_INLET_SCHEDULE) {
+        // first advection of the step at its end time, the second half a step later
+        k_inlet_eval<<<1, 32, 0, st>>>(c->d_inlet, c->d_sched, c->n_sched, c->d_time, c->d_step_counter,
+                                       edir == GW_DIR_Y ? 0.0 : 0.5, c->nbh);
+        GW_CUDA(cudaGetLastError());
+    }
     long long na = (long long)ncol * c->countz;
     if (na > 0) {
         k_advect_c<T><<<grid_for(na, 256), 256, 0, st>>>(
             B.pp, B.tp, c->d_advtab, c->d_pipe_b, c->d_annmean, c->d_outlet, B.Tref, c->n_inner,
-            ncol, c->nz, c->countz, c->inlet_kind, c->inlet_param);
+            ncol, c->nz, c->countz, c->inlet_kind, c->inlet_param, c->d_inlet);
         GW_CUDA(cudaGetLastError());
     }
     return GW_OK;

@@ -63,6 +63,13 @@ struct gw_ctx {
     double k_backfill, rho_c_backfill;
     int inlet_kind = 0;
     double inlet_param = 0.0;
+    // GW_INLET_SCHEDULE: T_in(t) piecewise linear; d_sched = times then values
+    std::vector<double> sched_t, sched_T;
+    double *d_sched = nullptr;
+    int n_sched = 0;
+    double *d_time = nullptr;         // [2]: start time of the current gw_step call, dt
+    double *d_inlet = nullptr;        // [nbh]: inlet value of the last pipe pass
+    double t_now = 0.0;               // end time of the last step taken
     double eigen_estimate = 0.0;
 
     // host-side material model
@@ -178,11 +185,14 @@ int gw_launch_zstage(gw_ctx *c, double *out, const double *x, const double *y, d
                      double kap, int rhs_only);
 int gw_launch_explicit(gw_ctx *c, double *dst, const double *src, double h, int dir);
 int gw_launch_thomas(gw_ctx *c, double *U, const double *RHS, int dir);
-int gw_launch_advection(gw_ctx *c, double *phi, double dt);
+int gw_launch_advection(gw_ctx *c, double *phi, double dt, double t = 0.0);
+// T_in(t) of the context's schedule (host); the same formula as the device.
+double gw_schedule_at(const gw_ctx *c, double t);
 int gw_launch_record(gw_ctx *c, double dt);
 int gw_launch_check_finite(gw_ctx *c, const double *u, size_t n);
 int gw_launch_lincomb(gw_ctx *c, double *dst, int n, const double *w, const double *const *src);
 int gw_ensure_factors(gw_ctx *c, double h);
+int gw_set_step_time(gw_ctx *c, double t0, double dt);
 int gw_prepare_step(gw_ctx *c, double dt, int s, int nsteps);
 
 #define GW_STAGE_TABLE 208   // doubles: 2 per recurrence stage (<= 98) + 3

@@ -271,13 +271,15 @@ __global__ void __launch_bounds__(256) k_scatter(double *__restrict__ phi,
 __global__ void k_record(double *__restrict__ series, double *__restrict__ energy,
                          int *__restrict__ counter, const double *__restrict__ outlet,
                          const GwBhDev *__restrict__ bh, int nbh, int cap, double dt,
-                         double c_w, int inlet_kind, double inlet_param) {
+                         double c_w, int inlet_kind, double inlet_param,
+                         const double *__restrict__ inlet_v) {
     const int b = threadIdx.x;
     const int n = *counter;
     __syncthreads();
     if (b < nbh) {
         double to = outlet[b];
-        double ti = inlet_kind == GW_INLET_CONSTANT ? inlet_param : to - inlet_param;
+        double ti = inlet_kind == GW_INLET_CONSTANT ? inlet_param
+                  : inlet_kind == GW_INLET_SCHEDULE ? inlet_v[b] : to - inlet_param;
         if (n < cap) series[(size_t)n * nbh + b] = to;
         energy[b] += bh[b].mdot * c_w * (to - ti) * dt;
     }
@@ -342,7 +344,11 @@ int gw_launch_thomas(gw_ctx *c, double *U, const double *R, int dir) {
     return GW_OK;
 }
 
-int gw_launch_advection(gw_ctx *c, double *phi, double dt) {
+int gw_launch_advection(gw_ctx *c, double *phi, double dt, double t) {
+    // a schedule inlet is a known value at the call's time t
+    const bool sched = c->inlet_kind == GW_INLET_SCHEDULE;
+    const int ikind = sched ? GW_INLET_CONSTANT : c->inlet_kind;
+    const double iparam = sched ? gw_schedule_at(c, t) : c->inlet_param;
     const int ncol = c->n_inner + c->n_outer;
     k_outlet<<<c->nbh, 256, 0, c->stream>>>(c->d_outlet, phi, c->d_gz, c->d_pipe_i, c->d_pipe_j,
                                             c->d_bh, c->ny, c->nz, dt);
@@ -355,7 +361,7 @@ int gw_launch_advection(gw_ctx *c, double *phi, double dt) {
     long long n = (long long)ncol * c->countz;
     k_advect<<<grid_for(n, 256), 256, 0, c->stream>>>(
         c->d_utmp, phi, c->d_gz, c->d_pipe_i, c->d_pipe_j, c->d_pipe_b, c->d_bh, c->d_annmean,
-        c->d_outlet, c->n_inner, ncol, c->ny, c->nz, c->countz, dt, c->inlet_kind, c->inlet_param);
+        c->d_outlet, c->n_inner, ncol, c->ny, c->nz, c->countz, dt, ikind, iparam);
     GW_CUDA(cudaGetLastError());
     k_scatter<<<grid_for(n, 256), 256, 0, c->stream>>>(phi, c->d_utmp, c->d_pipe_i, c->d_pipe_j,
                                                         ncol, c->ny, c->nz, c->countz);
@@ -367,7 +373,7 @@ int gw_launch_record(gw_ctx *c, double dt) {
     int threads = ((c->nbh + 31) / 32) * 32;
     k_record<<<1, threads, 0, c->stream>>>(c->d_series, c->d_energy, c->d_step_counter, c->d_outlet,
                                            c->d_bh, c->nbh, c->series_cap, dt,
-                                           c->rho_c_water / 998.2, c->inlet_kind, c->inlet_param);
+                                           c->rho_c_water / 998.2, c->inlet_kind, c->inlet_param, c->d_inlet);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }

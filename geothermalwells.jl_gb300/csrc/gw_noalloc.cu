@@ -203,7 +203,8 @@ extern "C" int gw_advection_noalloc(gw_ctx *c, double *phi, double dt, double t,
         if ((e = cudaGetLastError()) != cudaSuccess) return gw_cuda_fail(e, "na_annulus_mean");
         na_advect_column<<<ncol, 256, (size_t)c->countz * sizeof(double), c->stream>>>(
             phi, c->d_gz, c->d_pipe_i, c->d_pipe_j, c->d_pipe_b, c->d_bh, ann, outlet, c->n_inner,
-            c->ny, c->nz, c->countz, dt, c->inlet_kind, c->inlet_param);
+            c->ny, c->nz, c->countz, dt, c->inlet_kind == GW_INLET_SCHEDULE ? GW_INLET_CONSTANT : c->inlet_kind,
+            c->inlet_kind == GW_INLET_SCHEDULE ? gw_schedule_at(c, t) : c->inlet_param);
         if ((e = cudaGetLastError()) != cudaSuccess) return gw_cuda_fail(e, "na_advect_column");
     }
     e = cudaMemcpyAsync(T_outlet_dev, outlet, c->nbh * sizeof(double), cudaMemcpyDeviceToDevice,

@@ -85,9 +85,10 @@ int gw_setup_host(gw_ctx *c, const gw_desc *d) {
     if (d->materials.n_layers < 1 || !d->materials.k_rock_layers || !d->materials.rho_c_rock_layers ||
         !d->materials.layer_depths)
         return gw_fail(GW_ERR_ARG, "materials need at least one rock layer");
-    if (d->inlet_kind != GW_INLET_CONSTANT && d->inlet_kind != GW_INLET_HEAT_EXCHANGER)
-        return gw_fail(GW_ERR_UNSUPPORTED, "inlet kind must be GW_INLET_CONSTANT or GW_INLET_HEAT_EXCHANGER "
-                                            "(CustomInlet closures cannot cross the C ABI)");
+    if (d->inlet_kind != GW_INLET_CONSTANT && d->inlet_kind != GW_INLET_HEAT_EXCHANGER &&
+        d->inlet_kind != GW_INLET_SCHEDULE)
+        return gw_fail(GW_ERR_UNSUPPORTED, "inlet kind must be GW_INLET_CONSTANT, GW_INLET_HEAT_EXCHANGER or "
+                                            "GW_INLET_SCHEDULE (CustomInlet closures cannot cross the C ABI)");
     if (d->precision != GW_PREC_FP64 && d->precision != GW_PREC_MIXED)
         return gw_fail(GW_ERR_ARG, "precision must be GW_PREC_FP64 or GW_PREC_MIXED");
 

@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(PKG_ROOT, "lib", "libgw_gb300.so")
 
 GW_OK, GW_ERR_ARG, GW_ERR_CUDA, GW_ERR_NONFINITE, GW_ERR_TIMEOUT, GW_ERR_UNSUPPORTED = range(6)
 GW_PREC_FP64, GW_PREC_MIXED = 0, 1
-GW_INLET_CONSTANT, GW_INLET_HEAT_EXCHANGER = 0, 1
+GW_INLET_CONSTANT, GW_INLET_HEAT_EXCHANGER, GW_INLET_SCHEDULE = 0, 1, 2
 DIRS = {"x": 0, "y": 1, "z": 2}
 
 # Every symbol include/gw_gb300.h declares, with (restype, argtypes).
@@ -71,6 +71,7 @@ SIGNATURES = {
     "gw_init_thermal_gradient": (_i, [_vp, _d, _d]),
     "gw_rhs_diffusion_z": (_i, [_vp, _vp, _vp]),
     "gw_lincomb": (_i, [_vp, _vp, _i, _dp, ctypes.POINTER(_vp)]),
+    "gw_set_inlet_schedule": (_i, [_vp, _i, _dp, _dp]),
     "gw_diffusion_1d": (_i, [_vp, _vp, _vp, _d, _i, _i]),
     "gw_thomas": (_i, [_vp, _vp, _vp, _d, _i]),
     "gw_advection": (_i, [_vp, _vp, _d, _d]),

@@ -207,6 +207,29 @@ class HeatExchangerInlet:
         return T_outlet_values[bh_idx] - self.dT
 
 
+class ScheduleInlet:
+    """A ``CustomInlet`` (``src/physics.jl:315-318``) whose closure is a
+    piecewise-linear schedule ``(bh, T_outlet, t) -> T_in(t)``: linear between
+    the points, held constant before the first and after the last.  The form
+    of custom inlet that crosses the C ABI (``GW_INLET_SCHEDULE``)."""
+    kind = 2
+
+    def __init__(self, times, values):
+        self.times = tuple(float(v) for v in times)
+        self.values = tuple(float(v) for v in values)
+        if len(self.times) < 1 or len(self.times) != len(self.values):
+            raise ValueError("one value per schedule time, at least one point")
+        if any(b <= a for a, b in zip(self.times, self.times[1:])):
+            raise ValueError("schedule times must be strictly increasing")
+
+    @property
+    def param(self):
+        return 0.0
+
+    def __call__(self, bh_idx, T_outlet_values, t):
+        return float(np.interp(t, self.times, self.values))
+
+
 class CustomInlet:
     """``src/physics.jl:315-318``: an arbitrary host function.  The GB300
     backend evaluates the inlet on the device, so a Python callable cannot

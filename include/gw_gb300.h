@@ -42,6 +42,9 @@ extern "C" {
 
 #define GW_INLET_CONSTANT 0        /* ConstantInlet, src/physics.jl:290-293 */
 #define GW_INLET_HEAT_EXCHANGER 1  /* HeatExchangerInlet, src/physics.jl:303-306 */
+#define GW_INLET_SCHEDULE 2        /* a CustomInlet (src/physics.jl:315-318) of the form
+                                      (bh, T_outlet, t) -> T_in(t): a piecewise-linear
+                                      schedule, set with gw_set_inlet_schedule */
 
 #define GW_DIR_X 0
 #define GW_DIR_Y 1
@@ -118,6 +121,13 @@ int gw_advection(gw_ctx *ctx, double *phi_dev, double dt, double t);
 /* ADI_and_ADV_callback!(integrator), src/solver.jl:432-464: u = integrator.u,
  * temp = integrator.uprev (clobbered), t = integrator.t, dt = t - tprev. */
 int gw_adi_adv(gw_ctx *ctx, double *u_dev, double *temp_dev, double t, double dt);
+
+/* Inlet temperature schedule of a GW_INLET_SCHEDULE context: T_in(t) linear
+ * between the n points (times strictly increasing), held constant before the
+ * first and after the last.  Evaluated where the reference calls
+ * inlet_model(bh, T_outlet, t) (src/solver.jl:349-350): at the step's end time
+ * in the first advection and half a step later in the second. */
+int gw_set_inlet_schedule(gw_ctx *ctx, int n, const double *times, const double *values);
 
 /* dst = sum_i coeffs[i] * srcs[i] over the context's N = nx*ny*nz cells, n <= 8
  * device fields (dst may be one of them).  The vector updates an ODE

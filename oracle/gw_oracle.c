@@ -38,8 +38,10 @@ typedef struct {
     double *k_layers, *rhoc_layers, *depths;
     double k_water, rho_c_water, k_steel, rho_c_steel;
     double k_insulating, rho_c_insulating, k_backfill, rho_c_backfill;
-    int inlet_kind;      /* 0 = ConstantInlet, 1 = HeatExchangerInlet */
+    int inlet_kind;      /* 0 = ConstantInlet, 1 = HeatExchangerInlet, 2 = schedule T_in(t) */
     double inlet_param;  /* T_const or DeltaT */
+    int sched_n;         /* kind 2: piecewise-linear T_in(t), constant outside the points */
+    double *sched_t, *sched_T;
     /* advection index lists, cache.jl:9-44 (0-based i, j, bh) */
     int n_inner, n_outer, countz;
     int *idx;            /* 3 * (n_inner + n_outer): inner list then outer list */
@@ -109,6 +111,7 @@ void ogw_destroy(void *h) {
     free(c->gx); free(c->gy); free(c->gz); free(c->bh);
     free(c->k_layers); free(c->rhoc_layers); free(c->depths);
     free(c->idx); free(c->u_tmp); free(c->T_outlet); free(c->T_outlet_counter);
+    free(c->sched_t); free(c->sched_T);
     free(c);
 }
 
@@ -350,16 +353,41 @@ static void interp_helper(const double *grid, int n, double dep, int *il, int *i
     *alpha = (dep - grid[l]) / (grid[r] - grid[l]);
 }
 
-/* physics.jl:290-306 inlet models */
-static double inlet_value(const octx_t *c, int bh) {
+/* physics.jl:290-306 inlet models; kind 2 is a CustomInlet (physics.jl:315-318)
+ * whose closure is the piecewise-linear schedule T_in(t) */
+static double schedule_at(const octx_t *c, double t) {
+    const int n = c->sched_n;
+    if (n == 0) return 0.0;
+    if (t <= c->sched_t[0]) return c->sched_T[0];
+    if (t >= c->sched_t[n - 1]) return c->sched_T[n - 1];
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) / 2;
+        if (c->sched_t[mid] <= t) lo = mid; else hi = mid;
+    }
+    double a = (t - c->sched_t[lo]) / (c->sched_t[hi] - c->sched_t[lo]);
+    return fma(a, c->sched_T[hi] - c->sched_T[lo], c->sched_T[lo]);
+}
+
+static double inlet_value(const octx_t *c, int bh, double t) {
+    if (c->inlet_kind == 2) return schedule_at(c, t);
     return c->inlet_kind == 0 ? c->inlet_param : c->T_outlet[bh] - c->inlet_param;
+}
+
+void ogw_set_schedule(void *h, int n, const double *t, const double *T) {
+    octx_t *c = (octx_t *)h;
+    free(c->sched_t); free(c->sched_T);
+    c->sched_n = n;
+    c->sched_t = (double *)malloc(sizeof(double) * (n > 0 ? n : 1));
+    c->sched_T = (double *)malloc(sizeof(double) * (n > 0 ? n : 1));
+    memcpy(c->sched_t, t, sizeof(double) * n);
+    memcpy(c->sched_T, T, sizeof(double) * n);
 }
 
 /* solver.jl:250-396 advection! with kernel_accumulate_outlet!, kernel_advection!,
  * kernel_copy_advection! */
 void ogw_advection(void *h, double *phi, double dt, double t) {
     octx_t *c = (octx_t *)h;
-    (void)t;
     const int ni = c->n_inner, no = c->n_outer, ncol = ni + no, cz = c->countz;
     /* solver.jl:253-257 */
     for (int b = 0; b < c->nbh; ++b) { c->T_outlet[b] = 0; c->T_outlet_counter[b] = 0; }
@@ -405,7 +433,7 @@ void ogw_advection(void *h, double *phi, double dt, double t) {
             } else {
                 double zd = fma(-bh->v_outer, dt, z);
                 if (zd <= 0.0) {
-                    *out = inlet_value(c, b);
+                    *out = inlet_value(c, b, t);
                 } else {
                     int kl, kr; double a;
                     interp_helper(c->gz, c->nz, zd, &kl, &kr, &a);

@@ -53,6 +53,7 @@ def lib():
         L.ogw_initial_condition.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double]
         _lp = ctypes.POINTER(ctypes.c_longlong)
         L.ogw_tridiag_batch.argtypes = [ctypes.c_int, _lp, _ip, _dp, _dp, _dp, _dp, _dp]
+        L.ogw_set_schedule.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
         L.ogw_set_threads.restype = ctypes.c_int
         L.ogw_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -82,13 +83,17 @@ class Oracle:
         bh = np.array([b.args() for b in boreholes], dtype=np.float64).ravel()
         kl, rl, dl = (np.array(v, dtype=np.float64) for v in materials.layers())
         m8 = np.array(materials.fixed(), dtype=np.float64)
-        if inlet_model.kind not in (0, 1):
-            raise ValueError("oracle supports ConstantInlet and HeatExchangerInlet")
+        if inlet_model.kind not in (0, 1, 2):
+            raise ValueError("oracle supports ConstantInlet, HeatExchangerInlet and ScheduleInlet")
         self.nbh = len(boreholes)
         self._keep = (bh, kl, rl, dl, m8)
         self.h = L.ogw_create(self.nx, self.ny, self.nz, _p(self.gx), _p(self.gy), _p(self.gz),
                               self.nbh, _p(bh), len(kl), _p(kl), _p(rl), _p(dl), _p(m8),
                               inlet_model.kind, inlet_model.param)
+        if inlet_model.kind == 2:
+            st = np.ascontiguousarray(inlet_model.times, dtype=np.float64)
+            sv = np.ascontiguousarray(inlet_model.values, dtype=np.float64)
+            L.ogw_set_schedule(self.h, len(st), _p(st), _p(sv))
         self.temp = np.zeros(self.shape, order="F")
         self._work = None
 
