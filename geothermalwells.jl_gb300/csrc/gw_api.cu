@@ -34,7 +34,12 @@ int upload(gw_ctx *c, T **p, const std::vector<T> &v) {
 
 template <typename T>
 int copy_to(T *dst, const std::vector<T> &v) {
-    if (!v.empty()) GW_CUDA(cudaMemcpy(dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    if (!v.empty()) {
+        GW_CUDA(cudaMemcpy(dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        // a pageable copy may return before its DMA lands; the context's
+        // stream is non-blocking, so wait for it here
+        GW_CUDA(cudaStreamSynchronize(0));
+    }
     return GW_OK;
 }
 
@@ -470,12 +475,24 @@ int gw_get_field(gw_ctx *c, double *T) {
 
 int gw_init_thermal_gradient(gw_ctx *c, double T_surface, double gradient) {
     if (!c) return gw_fail(GW_ERR_ARG, "NULL argument");
-    std::vector<double> T(ncell(c));
-    for (int i = 0; i < c->nx; ++i)
-        for (int j = 0; j < c->ny; ++j)
-            for (int k = 0; k < c->nz; ++k)
-                T[k + (size_t)c->nz * (j + (size_t)c->ny * i)] = T_surface + gradient * c->gz[k];
-    return gw_set_field(c, T.data());
+    if (!std::isfinite(T_surface) || !std::isfinite(gradient))
+        return gw_fail(GW_ERR_ARG, "T_surface and gradient must be finite");
+    int rc = set_device(c);
+    if (rc) return rc;
+    // one column on the host, T_surface + gradient * z_k, as gw_set_field would
+    // receive it; the field is then filled on the device (no N-cell host array)
+    std::vector<double> col(c->nz);
+    for (int k = 0; k < c->nz; ++k) col[k] = T_surface + gradient * c->gz[k];
+    if (mixed(c)) {
+        // T_ref is the first column, so theta = T - T_ref is exactly 0 everywhere
+        if ((rc = set_reference_profile(c, col.data()))) return rc;
+        c->tables_dt = -1.0;
+        GW_CUDA(cudaMemsetAsync(c->f_u, 0, ncell(c) * sizeof(float), c->stream));
+        return sync(c);
+    }
+    GW_CUDA(cudaMemcpyAsync(c->d_temp, col.data(), c->nz * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if ((rc = gw_launch_broadcast_column(c, c->d_u, c->d_temp))) return rc;
+    return sync(c);
 }
 
 int gw_set_inlet_schedule(gw_ctx *c, int n, const double *times, const double *values) {

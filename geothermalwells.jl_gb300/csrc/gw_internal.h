@@ -191,6 +191,8 @@ double gw_schedule_at(const gw_ctx *c, double t);
 int gw_launch_record(gw_ctx *c, double dt);
 int gw_launch_check_finite(gw_ctx *c, const double *u, size_t n);
 int gw_launch_lincomb(gw_ctx *c, double *dst, int n, const double *w, const double *const *src);
+// u = col[k] in every column (col: nz device doubles)
+int gw_launch_broadcast_column(gw_ctx *c, double *u, const double *col);
 int gw_ensure_factors(gw_ctx *c, double h);
 int gw_set_step_time(gw_ctx *c, double t0, double dt);
 int gw_prepare_step(gw_ctx *c, double dt, int s, int nsteps);

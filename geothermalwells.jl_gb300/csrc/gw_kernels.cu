@@ -305,6 +305,14 @@ __global__ void __launch_bounds__(256) k_lincomb(double *dst, LinComb lc, size_t
     }
 }
 
+// u[k, j, i] = col[k]: one z profile copied into every column (z fastest).
+__global__ void __launch_bounds__(256) k_broadcast_column(double *__restrict__ u, const double *__restrict__ col,
+                                                          size_t ncell, int nz) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < ncell; i += stride)
+        u[i] = col[i % (size_t)nz];
+}
+
 __global__ void k_check_finite(const double *__restrict__ u, size_t n, int *__restrict__ flag) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t s = (size_t)gridDim.x * blockDim.x;
@@ -384,6 +392,13 @@ int gw_launch_lincomb(gw_ctx *c, double *dst, int n, const double *w, const doub
     lc.n = n;
     const size_t N = (size_t)c->nx * c->ny * c->nz;
     k_lincomb<<<152 * 8, 256, 0, c->stream>>>(dst, lc, N);
+    GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}
+
+int gw_launch_broadcast_column(gw_ctx *c, double *u, const double *col) {
+    const size_t N = (size_t)c->nx * c->ny * c->nz;
+    k_broadcast_column<<<152 * 8, 256, 0, c->stream>>>(u, col, N, c->nz);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }

@@ -99,6 +99,12 @@ class Cache:
         buf = np.ascontiguousarray(T.reshape(self.shape, order="F").ravel(order="F"))
         _lib.check(_lib.load().gw_set_field(self.ctx, _lib.dptr(buf)))
 
+    def init_thermal_gradient(self, T_surface, gradient):
+        """u = T_surface + gradient * z filled on the device
+        (``initial_condition_thermal_gradient``, ``src/physics.jl:333-348``,
+        without an N-cell host array)."""
+        _lib.check(_lib.load().gw_init_thermal_gradient(self.ctx, float(T_surface), float(gradient)))
+
     def get_field(self, dtype=np.float64):
         buf = np.zeros(self.N)
         _lib.check(_lib.load().gw_get_field(self.ctx, _lib.dptr(buf)))

@@ -18,18 +18,24 @@ TILINGS = ((4, 16), (8, 16), (8, 8), (4, 32), (2, 16), (8, 32), (2, "seg8x32"))
 
 
 class Ensemble:
-    def __init__(self, designs, precision="mixed", device=0, initial_field=None):
+    def __init__(self, designs, precision="mixed", device=0, initial_field=None,
+                 initial_gradient=None):
         """designs: dicts with gridx, gridy, gridz, boreholes, materials,
-        inlet_model; initial_field(design) -> (Nz, Ny, Nx) array (default: the
-        design's "T0")."""
+        inlet_model.  The initial field is, in this order of preference:
+        initial_gradient(design) -> (T_surface, gradient), filled on the
+        device; initial_field(design) -> (Nz, Ny, Nx) host array; the
+        design's "T0"."""
         L = _lib.load()
         self.caches = []
         for d in designs:
             c = create_cache(backend=GB300(device=device, precision=precision), gridx=d["gridx"],
                              gridy=d["gridy"], gridz=d["gridz"], materials=d["materials"],
                              boreholes=d["boreholes"], inlet_model=d["inlet_model"])
-            c.set_field(initial_field(d) if initial_field else d["T0"])
             self.caches.append(c)
+            if initial_gradient is not None:
+                c.init_thermal_gradient(*initial_gradient(d))
+            else:
+                c.set_field(initial_field(d) if initial_field else d["T0"])
         arr = (ctypes.c_void_p * len(self.caches))(*[c.ctx for c in self.caches])
         h = ctypes.c_void_p()
         _lib.check(L.gw_batch_create(arr, len(self.caches), ctypes.byref(h)))

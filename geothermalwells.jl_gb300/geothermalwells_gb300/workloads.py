@@ -229,6 +229,11 @@ def initial_field(d):
                                               T_surface=d["T_surface"], gradient=d["gradient"])
 
 
+def initial_gradient(d):
+    """(T_surface, gradient) of one design, for the device-side initial field."""
+    return d["T_surface"], d["gradient"]
+
+
 def adjoint_small(inlet="constant", nbh=1, n_layers=3, backfill_quirk=False, dt=200.0, nsteps=12):
     """A few-thousand-cell well for checking gradients against central
     differences of the oracle: the small_case geometry at low flow (0.6 kg/s,

@@ -60,3 +60,27 @@ def test_autotune_returns_valid_choices(gwlib):
     assert len(choice) == 3 and all(0 <= t < len(TILINGS) for t in choice)
     ens.step(40.0, 2)
     ens.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_device_initial_field_equals_host_field(precision, gwlib):
+    """gw_init_thermal_gradient fills the field on the device: the same field
+    as the host-built initial_condition_thermal_gradient, and the same run."""
+    from geothermalwells_gb300 import initial_condition_thermal_gradient
+    ds = designs()
+    ic = [(4.0 + q, 0.03 + 0.01 * q) for q in range(len(ds))]
+    host = [dict(d, T0=initial_condition_thermal_gradient(None, np.float64, d["gridx"], d["gridy"],
+                                                          d["gridz"], T_surface=ts, gradient=g))
+            for d, (ts, g) in zip(ds, ic)]
+    a = Ensemble(host, precision=precision)
+    by_id = {id(d): v for d, v in zip(ds, ic)}
+    b = Ensemble(ds, precision=precision, initial_gradient=lambda d: by_id[id(d)])
+    for ca, cb, h in zip(a.caches, b.caches, host):
+        assert np.array_equal(cb.get_field(), ca.get_field())
+        assert np.array_equal(cb.get_field(), h["T0"])
+    a.step(40.0, 3)
+    b.step(40.0, 3)
+    for d, (ca, cb) in enumerate(zip(a.caches, b.caches)):
+        assert np.array_equal(ca.get_field(), cb.get_field())
+        assert np.array_equal(a.outlet_series(d, 3), b.outlet_series(d, 3))
+    a.close(); b.close()
