@@ -302,12 +302,13 @@ __device__ __forceinline__ double absT(T v, const double *Tref, int k) {
 }
 
 // Pipe pass in two launches before the advection: k_pipe_sweep applies the
-// explicit sweep to the pipe columns of one chunk (a run of at most kPipeChunk
+// explicit sweep to the pipe columns of one chunk (a run of at most 32
 // columns of one borehole's inner pipe or annulus) for 128 levels, stores the
 // swept values and the chunk's column sum per level; k_pipe_reduce turns the
 // sums into the outlet mean (src/solver.jl:267-282, 257) and the per-level
-// annulus means (src/solver.jl:322-335).  Fixed summation order: the results
-// do not depend on scheduling.
+// annulus means (src/solver.jl:322-335).  Every sum runs in a fixed order
+// (per warp, then across warps in warp order): the results do not depend on
+// scheduling.
 
 template <typename T>
 __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *__restrict__ part,
@@ -353,28 +354,38 @@ __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *
     part[(size_t)ch * nz + k] = acc;
 }
 
-// grid (ceil(nz / 128), nbh): annulus means per level; the first block of a
+constexpr int kReduceWarps = 8;   // warps of k_pipe_reduce, splitting a borehole's chunks
+
+// grid (ceil(nz / 32), nbh), block 32 * kReduceWarps: annulus means per
+// level (lane = level, warps split the chunks); the first block of a
 // borehole also reduces its inner-pipe chunks over the outlet window.
-__global__ void __launch_bounds__(128) k_pipe_reduce(double *__restrict__ outlet,
+__global__ void __launch_bounds__(32 * kReduceWarps) k_pipe_reduce(double *__restrict__ outlet,
                                                      double *__restrict__ mean,
                                                      const double *__restrict__ part,
                                                      const int *__restrict__ bchunk,
                                                      const double *__restrict__ gz,
                                                      const GwBhDev *__restrict__ bh, int nz,
                                                      double dt) {
+    __shared__ double s_red[32 * kReduceWarps];
+    __shared__ int s_nlev;
     const int b = blockIdx.y;
     const GwBhDev B = bh[b];
     // chunks of b: inner [bchunk[4b], bchunk[4b+1]), outer [bchunk[4b+2], bchunk[4b+3])
     const int i0 = bchunk[4 * b], i1 = bchunk[4 * b + 1], o0 = bchunk[4 * b + 2], o1 = bchunk[4 * b + 3];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < nz) {
-        double sacc = 0.0;
-        for (int ch = o0; ch < o1; ++ch) sacc += part[(size_t)ch * nz + k];
-        mean[(size_t)b * nz + k] = sacc / (double)B.outer_count;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int k = blockIdx.x * 32 + lane;
+    double sacc = 0.0;
+    if (k < nz)
+        for (int ch = o0 + w; ch < o1; ch += kReduceWarps) sacc += part[(size_t)ch * nz + k];
+    s_red[threadIdx.x] = sacc;
+    __syncthreads();
+    if (w == 0 && k < nz) {
+        double m = s_red[lane];
+#pragma unroll
+        for (int q = 1; q < kReduceWarps; ++q) m += s_red[32 * q + lane];
+        mean[(size_t)b * nz + k] = m / (double)B.outer_count;
     }
-    if (blockIdx.x != 0) return;
-    __shared__ double s_red[128];
-    __shared__ int s_nlev;
+    if (blockIdx.x != 0) return;   // the whole block: the outlet is block 0's
     if (threadIdx.x == 0) {
         int lo = 0, hi = nz;   // gz sorted: the levels with gz <= v_inner dt are a prefix
         const double zmax = B.v_inner * dt;
@@ -384,15 +395,16 @@ __global__ void __launch_bounds__(128) k_pipe_reduce(double *__restrict__ outlet
         }
         s_nlev = lo;
     }
-    __syncthreads();
+    __syncthreads();   // s_nlev set; every read of s_red above is done
     const int nlev = s_nlev;
+    const int total = nlev * (i1 - i0);
     double acc = 0.0;
-    for (int kk = threadIdx.x; kk < nlev; kk += blockDim.x)
-        for (int ch = i0; ch < i1; ++ch) acc += part[(size_t)ch * nz + kk];
+    for (int e = threadIdx.x; e < total; e += blockDim.x)   // level fastest: coalesced
+        acc += part[(size_t)(i0 + e / nlev) * nz + e % nlev];
     s_red[threadIdx.x] = acc;
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) s_red[threadIdx.x] += s_red[threadIdx.x + w];
+    for (int r = blockDim.x / 2; r > 0; r >>= 1) {
+        if (threadIdx.x < r) s_red[threadIdx.x] += s_red[threadIdx.x + r];
         __syncthreads();
     }
     if (threadIdx.x == 0) outlet[b] = s_red[0] / (double)((long long)B.inner_count * nlev);
@@ -475,7 +487,7 @@ __global__ void k_inlet_eval(double *__restrict__ inlet_v, const double *__restr
 // kernel_advection! on the compact buffer with the departure table; the
 // result (minus T_ref in the mixed path) goes to pp[q][k], k < countz.
 template <typename T>
-__global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *__restrict__ tp,
+__global__ void __launch_bounds__(128) k_advect_c(T *__restrict__ pp, const T *__restrict__ tp,
                                                   const GwAdvRec *__restrict__ tab,
                                                   const int *__restrict__ pb,
                                                   const double *__restrict__ ann_mean,
@@ -483,33 +495,35 @@ __global__ void __launch_bounds__(256) k_advect_c(T *__restrict__ pp, const T *_
                                                   const double *__restrict__ Tref, int n_inner,
                                                   int ncol, int nz, int countz, int inlet_kind,
                                                   double inlet_param, const double *__restrict__ inlet_v) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= (long long)ncol * countz) return;
-    const int k = (int)(e % countz);
-    const int q = (int)(e / countz);
-    const int b = pb[q];
-    const GwAdvRec r = tab[((size_t)b * countz + k) * 2 + (q < n_inner ? 0 : 1)];
-    const T *col = tp + (size_t)q * nz;
-    double v;
-    if (r.type == kAdvKeep) {
-        v = absT(col[k], Tref, k);
-    } else if (r.type == kAdvInlet) {
-        v = inlet_kind == GW_INLET_CONSTANT ? inlet_param
-          : inlet_kind == GW_INLET_SCHEDULE ? inlet_v[b] : outlet[b] - inlet_param;
-    } else if (r.type == kAdvTurn) {
-        const double *m = ann_mean + (size_t)b * nz;
-        v = __fma_rn(r.alpha, m[r.ir], __dmul_rn(__dsub_rn(1.0, r.alpha), m[r.il]));
-    } else if (sizeof(T) == 4) {
-        // mixed path: interpolate theta in float, the T_ref part is the
-        // tabulated double offset
-        const float a = (float)r.alpha;
-        pp[e] = (T)(fmaf(a, (float)col[r.ir], (1.0f - a) * (float)col[r.il]) + (float)r.dref);
-        return;
-    } else {
-        v = __fma_rn(r.alpha, absT(col[r.ir], Tref, r.ir),
-                     __dmul_rn(__dsub_rn(1.0, r.alpha), absT(col[r.il], Tref, r.il)));
+    // grid (ceil(countz / blockDim.x), min(ncol, 65535)): level fastest, columns strided
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= countz) return;
+    for (int q = blockIdx.y; q < ncol; q += gridDim.y) {
+        const size_t e = (size_t)q * countz + k;
+        const int b = pb[q];
+        const GwAdvRec r = tab[((size_t)b * countz + k) * 2 + (q < n_inner ? 0 : 1)];
+        const T *col = tp + (size_t)q * nz;
+        double v;
+        if (r.type == kAdvKeep) {
+            v = absT(col[k], Tref, k);
+        } else if (r.type == kAdvInlet) {
+            v = inlet_kind == GW_INLET_CONSTANT ? inlet_param
+              : inlet_kind == GW_INLET_SCHEDULE ? inlet_v[b] : outlet[b] - inlet_param;
+        } else if (r.type == kAdvTurn) {
+            const double *m = ann_mean + (size_t)b * nz;
+            v = __fma_rn(r.alpha, m[r.ir], __dmul_rn(__dsub_rn(1.0, r.alpha), m[r.il]));
+        } else if (sizeof(T) == 4) {
+            // mixed path: interpolate theta in float, the T_ref part is the
+            // tabulated double offset
+            const float a = (float)r.alpha;
+            pp[e] = (T)(fmaf(a, (float)col[r.ir], (1.0f - a) * (float)col[r.il]) + (float)r.dref);
+            continue;
+        } else {
+            v = __fma_rn(r.alpha, absT(col[r.ir], Tref, r.ir),
+                         __dmul_rn(__dsub_rn(1.0, r.alpha), absT(col[r.il], Tref, r.il)));
+        }
+        pp[e] = (T)(Tref ? v - Tref[k] : v);
     }
-    pp[e] = (T)(Tref ? v - Tref[k] : v);
 }
 
 // ---------------------------------------------------------------------------
@@ -959,8 +973,8 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h, cudaStream_t st = n
                                                   B.Tref, c->nx, c->ny, c->nz, h, edir);
         GW_CUDA(cudaGetLastError());
     }
-    dim3 gr(grid_for(c->nz, 128), c->nbh);
-    k_pipe_reduce<<<gr, 128, 0, st>>>(c->d_outlet, c->d_annmean, c->d_pipepart, c->d_bchunk,
+    dim3 gr((c->nz + 31) / 32, c->nbh);
+    k_pipe_reduce<<<gr, 32 * kReduceWarps, 0, st>>>(c->d_outlet, c->d_annmean, c->d_pipepart, c->d_bchunk,
                                              c->d_gz, c->d_bh, c->nz, h);
     GW_CUDA(cudaGetLastError());
     if (c->inlet_kind == GW_INLET_SCHEDULE) {
@@ -971,7 +985,8 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h, cudaStream_t st = n
     }
     long long na = (long long)ncol * c->countz;
     if (na > 0) {
-        k_advect_c<T><<<grid_for(na, 256), 256, 0, st>>>(
+        dim3 ga((c->countz + 127) / 128, std::min(ncol, 65535));
+        k_advect_c<T><<<ga, 128, 0, st>>>(
             B.pp, B.tp, c->d_advtab, c->d_pipe_b, c->d_annmean, c->d_outlet, B.Tref, c->n_inner,
             ncol, c->nz, c->countz, c->inlet_kind, c->inlet_param, c->d_inlet);
         GW_CUDA(cudaGetLastError());
