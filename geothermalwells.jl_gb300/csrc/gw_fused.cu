@@ -486,43 +486,61 @@ __global__ void k_inlet_eval(double *__restrict__ inlet_v, const double *__restr
 
 // kernel_advection! on the compact buffer with the departure table; the
 // result (minus T_ref in the mixed path) goes to pp[q][k], k < countz.
+// grid (ceil(countz / 128), chunks): a thread takes one level of every
+// column of one pipe chunk (the columns of one borehole's inner pipe or
+// annulus share the departure record of that level), so the record is read
+// once per chunk; turnaround and inlet values do not depend on the column
+// and are computed once.
 template <typename T>
 __global__ void __launch_bounds__(128) k_advect_c(T *__restrict__ pp, const T *__restrict__ tp,
                                                   const GwAdvRec *__restrict__ tab,
-                                                  const int *__restrict__ pb,
+                                                  const int4 *__restrict__ chunks,
                                                   const double *__restrict__ ann_mean,
                                                   const double *__restrict__ outlet,
-                                                  const double *__restrict__ Tref, int n_inner,
-                                                  int ncol, int nz, int countz, int inlet_kind,
-                                                  double inlet_param, const double *__restrict__ inlet_v) {
-    // grid (ceil(countz / blockDim.x), min(ncol, 65535)): level fastest, columns strided
+                                                  const double *__restrict__ Tref, int nz, int countz,
+                                                  int inlet_kind, double inlet_param,
+                                                  const double *__restrict__ inlet_v) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= countz) return;
-    for (int q = blockIdx.y; q < ncol; q += gridDim.y) {
-        const size_t e = (size_t)q * countz + k;
-        const int b = pb[q];
-        const GwAdvRec r = tab[((size_t)b * countz + k) * 2 + (q < n_inner ? 0 : 1)];
-        const T *col = tp + (size_t)q * nz;
+    const int4 C = chunks[blockIdx.y];   // (borehole, first column, end column, annulus?)
+    const int b = C.x;
+    const GwAdvRec r = tab[((size_t)b * countz + k) * 2 + C.w];
+    T *out = pp + k;
+    if (r.type == kAdvInlet || r.type == kAdvTurn) {
         double v;
-        if (r.type == kAdvKeep) {
-            v = absT(col[k], Tref, k);
-        } else if (r.type == kAdvInlet) {
+        if (r.type == kAdvInlet) {
             v = inlet_kind == GW_INLET_CONSTANT ? inlet_param
               : inlet_kind == GW_INLET_SCHEDULE ? inlet_v[b] : outlet[b] - inlet_param;
-        } else if (r.type == kAdvTurn) {
+        } else {
             const double *m = ann_mean + (size_t)b * nz;
             v = __fma_rn(r.alpha, m[r.ir], __dmul_rn(__dsub_rn(1.0, r.alpha), m[r.il]));
-        } else if (sizeof(T) == 4) {
-            // mixed path: interpolate theta in float, the T_ref part is the
-            // tabulated double offset
-            const float a = (float)r.alpha;
-            pp[e] = (T)(fmaf(a, (float)col[r.ir], (1.0f - a) * (float)col[r.il]) + (float)r.dref);
-            continue;
-        } else {
-            v = __fma_rn(r.alpha, absT(col[r.ir], Tref, r.ir),
-                         __dmul_rn(__dsub_rn(1.0, r.alpha), absT(col[r.il], Tref, r.il)));
         }
-        pp[e] = (T)(Tref ? v - Tref[k] : v);
+        const T o = (T)(Tref ? v - Tref[k] : v);
+        for (int q = C.y; q < C.z; ++q) out[(size_t)q * countz] = o;
+        return;
+    }
+    if (r.type == kAdvKeep) {
+        for (int q = C.y; q < C.z; ++q) {
+            const double v = absT(tp[(size_t)q * nz + k], Tref, k);
+            out[(size_t)q * countz] = (T)(Tref ? v - Tref[k] : v);
+        }
+        return;
+    }
+    if (sizeof(T) == 4) {
+        // mixed path: interpolate theta in float, the T_ref part is the
+        // tabulated double offset
+        const float a = (float)r.alpha, a1 = 1.0f - a, dref = (float)r.dref;
+        for (int q = C.y; q < C.z; ++q) {
+            const T *col = tp + (size_t)q * nz;
+            out[(size_t)q * countz] = (T)(fmaf(a, (float)col[r.ir], a1 * (float)col[r.il]) + dref);
+        }
+        return;
+    }
+    const double a1 = __dsub_rn(1.0, r.alpha);
+    for (int q = C.y; q < C.z; ++q) {
+        const T *col = tp + (size_t)q * nz;
+        const double v = __fma_rn(r.alpha, absT(col[r.ir], Tref, r.ir), __dmul_rn(a1, absT(col[r.il], Tref, r.il)));
+        out[(size_t)q * countz] = (T)(Tref ? v - Tref[k] : v);
     }
 }
 
@@ -968,7 +986,6 @@ template <typename T>
 int launch_pipe(gw_ctx *c, const T *src, int edir, double h, cudaStream_t st = nullptr) {
     Bufs<T> B = bufs<T>(c);
     if (!st) st = c->stream;
-    const int ncol = c->n_inner + c->n_outer;
     const T *cm = edir == GW_DIR_X ? B.ct->cxm : B.ct->cym;
     const T *cp = edir == GW_DIR_X ? B.ct->cxp : B.ct->cyp;
     if (c->n_pipe_chunks > 0) {
@@ -988,12 +1005,11 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h, cudaStream_t st = n
                                        edir == GW_DIR_Y ? 0.0 : 0.5, c->nbh);
         GW_CUDA(cudaGetLastError());
     }
-    long long na = (long long)ncol * c->countz;
-    if (na > 0) {
-        dim3 ga((c->countz + 127) / 128, std::min(ncol, 65535));
-        k_advect_c<T><<<ga, 128, 0, st>>>(
-            B.pp, B.tp, c->d_advtab, c->d_pipe_b, c->d_annmean, c->d_outlet, B.Tref, c->n_inner,
-            ncol, c->nz, c->countz, c->inlet_kind, c->inlet_param, c->d_inlet);
+    if (c->n_pipe_chunks > 0 && c->countz > 0) {
+        dim3 ga((c->countz + 127) / 128, c->n_pipe_chunks);
+        k_advect_c<T><<<ga, 128, 0, st>>>(B.pp, B.tp, c->d_advtab, c->d_pipe_chunks, c->d_annmean,
+                                          c->d_outlet, B.Tref, c->nz, c->countz, c->inlet_kind,
+                                          c->inlet_param, c->d_inlet);
         GW_CUDA(cudaGetLastError());
     }
     return GW_OK;
