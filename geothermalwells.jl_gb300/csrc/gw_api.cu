@@ -369,6 +369,7 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         (rc = dalloc(c, &c->d_annpart, (size_t)c->nbh * 32 * c->nz)) ||
         (rc = dalloc(c, &c->d_outpart, (size_t)c->nbh * 64)) ||
         (rc = dalloc(c, &c->d_advtab, (size_t)c->nbh * c->countz * 2)) ||
+        (rc = dalloc(c, &c->d_nlev, c->nbh)) ||
         (rc = dalloc(c, &c->d_outlet, c->nbh)) || (rc = dalloc(c, &c->d_energy, c->nbh)) ||
         (rc = dalloc(c, &c->d_stage, GW_STAGE_TABLE)) || (rc = dalloc(c, &c->f_stage, GW_STAGE_TABLE)) ||
         (rc = dalloc(c, &c->d_step_counter, 1)) || (rc = dalloc(c, &c->d_flag, 1)) ||

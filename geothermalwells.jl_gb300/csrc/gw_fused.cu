@@ -327,8 +327,7 @@ __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *
     const int4 C = chunks[ch];   // (borehole, first column, end column, outer?)
     const int zc = zclass[k];
     const T hh = (T)h;
-    double acc = 0.0;
-    for (int q = C.y; q < C.z; ++q) {
+    auto sweep = [&](int q) {
         const int i = pi[q], j = pj[q];
         const long long c = k + (long long)nz * (j + (long long)ny * i);
         const T xc = src[c];
@@ -345,7 +344,24 @@ __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *
             t = ((size_t)zc * nx + i) * ny + j;
         }
         const T a = __ldg(cpt + t) * (xp - xc) - __ldg(cmt + t) * (xc - xm);
-        const T v = fma(hh, a, xc);
+        return fma(hh, a, xc);
+    };
+    // four columns per round: their loads are independent and overlap; the
+    // sum still runs over the columns in order
+    double acc = 0.0;
+    int q = C.y;
+    for (; q + 4 <= C.z; q += 4) {
+        T v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = sweep(q + u);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            tp[(size_t)(q + u) * nz + k] = v[u];
+            acc += (double)v[u];
+        }
+    }
+    for (; q < C.z; ++q) {
+        const T v = sweep(q);
         tp[(size_t)q * nz + k] = v;
         acc += (double)v;
     }
@@ -363,11 +379,9 @@ __global__ void __launch_bounds__(32 * kReduceWarps) k_pipe_reduce(double *__res
                                                      double *__restrict__ mean,
                                                      const double *__restrict__ part,
                                                      const int *__restrict__ bchunk,
-                                                     const double *__restrict__ gz,
-                                                     const GwBhDev *__restrict__ bh, int nz,
-                                                     double dt) {
+                                                     const int *__restrict__ nlev_b,
+                                                     const GwBhDev *__restrict__ bh, int nz) {
     __shared__ double s_red[32 * kReduceWarps];
-    __shared__ int s_nlev;
     const int b = blockIdx.y;
     const GwBhDev B = bh[b];
     // chunks of b: inner [bchunk[4b], bchunk[4b+1]), outer [bchunk[4b+2], bchunk[4b+3])
@@ -386,17 +400,8 @@ __global__ void __launch_bounds__(32 * kReduceWarps) k_pipe_reduce(double *__res
         mean[(size_t)b * nz + k] = m / (double)B.outer_count;
     }
     if (blockIdx.x != 0) return;   // the whole block: the outlet is block 0's
-    if (threadIdx.x == 0) {
-        int lo = 0, hi = nz;   // gz sorted: the levels with gz <= v_inner dt are a prefix
-        const double zmax = B.v_inner * dt;
-        while (lo < hi) {
-            int mid = (lo + hi) >> 1;
-            if (gz[mid] <= zmax) lo = mid + 1; else hi = mid;
-        }
-        s_nlev = lo;
-    }
-    __syncthreads();   // s_nlev set; every read of s_red above is done
-    const int nlev = s_nlev;
+    __syncthreads();   // every read of s_red above is done
+    const int nlev = nlev_b[b];
     const int total = nlev * (i1 - i0);
     double acc = 0.0;
     for (int e = threadIdx.x; e < total; e += blockDim.x)   // level fastest: coalesced
@@ -408,6 +413,22 @@ __global__ void __launch_bounds__(32 * kReduceWarps) k_pipe_reduce(double *__res
         __syncthreads();
     }
     if (threadIdx.x == 0) outlet[b] = s_red[0] / (double)((long long)B.inner_count * nlev);
+}
+
+// Outlet window of kernel_accumulate_outlet! (src/solver.jl:273-281) for a
+// step size: the number of levels with z <= v_inner dt (gz is sorted, so
+// they are a prefix), per borehole.
+__global__ void k_outlet_levels(int *__restrict__ nlev, const double *__restrict__ gz,
+                                const GwBhDev *__restrict__ bh, int nbh, int nz, double dt) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbh) return;
+    const double zmax = bh[b].v_inner * dt;
+    int lo = 0, hi = nz;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (gz[mid] <= zmax) lo = mid + 1; else hi = mid;
+    }
+    nlev[b] = lo;
 }
 
 // Departure table of kernel_advection! (src/solver.jl:285-360): for every
@@ -997,7 +1018,7 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h, cudaStream_t st = n
     }
     dim3 gr((c->nz + 31) / 32, c->nbh);
     k_pipe_reduce<<<gr, 32 * kReduceWarps, 0, st>>>(c->d_outlet, c->d_annmean, c->d_pipepart, c->d_bchunk,
-                                             c->d_gz, c->d_bh, c->nz, h);
+                                                    c->d_nlev, c->d_bh, c->nz);
     GW_CUDA(cudaGetLastError());
     if (c->inlet_kind == GW_INLET_SCHEDULE) {
         // first advection of the step at its end time, the second half a step later
@@ -1200,6 +1221,10 @@ int gw_fused_set_dt(gw_ctx *c, double dt) {
         k_adv_table<<<grid_for(n, 128), 128, 0, c->stream>>>(
             c->d_advtab, c->d_gz, c->d_bh, c->precision == GW_PREC_MIXED ? c->d_Tref : nullptr, c->nbh,
             c->nz, c->countz, dt / 2);
+        GW_CUDA(cudaGetLastError());
+    }
+    if (c->nbh > 0) {
+        k_outlet_levels<<<grid_for(c->nbh, 64), 64, 0, c->stream>>>(c->d_nlev, c->d_gz, c->d_bh, c->nbh, c->nz, dt / 2);
         GW_CUDA(cudaGetLastError());
     }
     GW_CUDA(cudaStreamSynchronize(c->stream));

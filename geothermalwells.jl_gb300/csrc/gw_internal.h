@@ -120,6 +120,7 @@ struct gw_ctx {
     double *d_pipepart = nullptr;     // [chunk][nz] column sums of the swept pipe values
     int n_pipe_chunks = 0;
     GwAdvRec *d_advtab = nullptr;     // [nbh][countz][2] departure table for dt/2
+    int *d_nlev = nullptr;            // [nbh] outlet window of that step size: levels with z <= v_inner dt/2
     double *d_stage = nullptr;        // ROCK2 stage coefficients of the captured step
     float *f_stage = nullptr;         // the same, rounded to float (mixed path)
     double *d_tp = nullptr;           // double path: [ncol][nz] swept pipe columns
