@@ -332,7 +332,11 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         slot = q;
     }
     for (auto &B : bhd) { if (B.inner_begin < 0) B.inner_begin = 0; if (B.outer_begin < 0) B.outer_begin = 0; }
-    // chunks of at most 32 pipe columns, never spanning two boreholes or pipes
+    // chunks of at most kPipeChunk pipe columns, never spanning two boreholes
+    // or pipes (16: the sweep's per-thread column loop is short enough to
+    // fill the GPU on a single well; 2 mm well step 0.280 -> 0.270 ms
+    // against 32, and 8 is slower again)
+    constexpr int kPipeChunk = 16;
     std::vector<int4> chunks;
     std::vector<int> bchunk(4 * (size_t)c->nbh, 0);
     for (int b = 0; b < c->nbh; ++b)
@@ -340,7 +344,7 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
             const int q0 = outer ? bhd[b].outer_begin : bhd[b].inner_begin;
             const int n = outer ? bhd[b].outer_count : bhd[b].inner_count;
             bchunk[4 * b + 2 * outer] = (int)chunks.size();
-            for (int q = q0; q < q0 + n; q += 32) chunks.push_back(make_int4(b, q, std::min(q + 32, q0 + n), outer));
+            for (int q = q0; q < q0 + n; q += kPipeChunk) chunks.push_back(make_int4(b, q, std::min(q + kPipeChunk, q0 + n), outer));
             bchunk[4 * b + 2 * outer + 1] = (int)chunks.size();
         }
     c->n_pipe_chunks = (int)chunks.size();
@@ -366,8 +370,6 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
     const size_t N = ncell(c);
     if ((rc = dalloc(c, &c->d_utmp, (size_t)ncol * c->countz)) ||
         (rc = dalloc(c, &c->d_annmean, (size_t)c->nbh * c->nz)) ||
-        (rc = dalloc(c, &c->d_annpart, (size_t)c->nbh * 32 * c->nz)) ||
-        (rc = dalloc(c, &c->d_outpart, (size_t)c->nbh * 64)) ||
         (rc = dalloc(c, &c->d_advtab, (size_t)c->nbh * c->countz * 2)) ||
         (rc = dalloc(c, &c->d_nlev, c->nbh)) ||
         (rc = dalloc(c, &c->d_outlet, c->nbh)) || (rc = dalloc(c, &c->d_energy, c->nbh)) ||

@@ -302,7 +302,7 @@ __device__ __forceinline__ double absT(T v, const double *Tref, int k) {
 }
 
 // Pipe pass in two launches before the advection: k_pipe_sweep applies the
-// explicit sweep to the pipe columns of one chunk (a run of at most 32
+// explicit sweep to the pipe columns of one chunk (a run of at most 16
 // columns of one borehole's inner pipe or annulus) for 128 levels, stores the
 // swept values and the chunk's column sum per level; k_pipe_reduce turns the
 // sums into the outlet mean (src/solver.jl:267-282, 257) and the per-level

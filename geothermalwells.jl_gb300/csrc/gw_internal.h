@@ -113,8 +113,6 @@ struct gw_ctx {
     int *d_pipe_of = nullptr;         // [nx*ny] pipe-column index or -1
     int *d_pipe_lx = nullptr;         // [ny][nx] pipe index along x-lines (j, i), then [ny] line flags
     int *d_pipe_ly = nullptr;         // [nx][ny] pipe index along y-lines (i, j), then [nx] line flags
-    double *d_annpart = nullptr;      // [nbh][32][nz] partial annulus sums
-    double *d_outpart = nullptr;      // [nbh][64] partial outlet sums
     int4 *d_pipe_chunks = nullptr;    // pipe-column chunks: (borehole, q0, q1, outer)
     int *d_bchunk = nullptr;          // [nbh][4]: chunk ranges (inner, outer) per borehole
     double *d_pipepart = nullptr;     // [chunk][nz] column sums of the swept pipe values
