@@ -950,13 +950,22 @@ template <typename T>
 size_t reg_smem(int lpt, int nt = 256) { return 2 * (size_t)(nt * lpt + nt * lpt / 32) * sizeof(T); }
 
 // levels per thread of the register-resident ROCK2 kernel (0: use the
-// shared-memory kernel).  Float columns of up to 2048 levels take 8 per
-// thread: fewer threads per column leave more columns, each an independent
+// shared-memory kernel).  Float columns of up to 2048 levels take 4 to 8 per
+// thread: few threads per column leave more columns, each an independent
 // chain of stages and barriers, in flight per SM (nz = 402: 0.329 -> 0.308 ms
-// per step against 2 per thread).  Double columns keep 2 / 4 / 8, which the
-// FP64 pipe prefers.
+// per step with 8 against 2 per thread), and among 4..8 the count that pads
+// the column least (nt LPT levels, nt a multiple of 32) does the least
+// work: nz = 402 takes 7 (448 levels, not 512), nz = 301 takes 5 (320, not
+// 512).  Double columns keep 2 / 4 / 8, which the FP64 pipe prefers.
 inline int rock2_lpt(int nz, bool f32) {
-    if (f32 && nz <= 2048) return 8;
+    if (f32 && nz <= 2048) {
+        int best = 8, pad = ((nz + 7) / 8 + 31) / 32 * 32 * 8;
+        for (int L = 7; L >= 4; --L) {
+            const int nt = ((nz + L - 1) / L + 31) / 32 * 32;
+            if (nt <= 256 && nt * L < pad) { best = L; pad = nt * L; }
+        }
+        return best;
+    }
     if (nz <= 512) return 2;
     if (nz <= 1024) return 4;
     if (nz <= 2048) return 8;
@@ -982,6 +991,9 @@ int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *
     switch (lpt) {
         case 2: k_rock2_reg<T, INC, 2><<<grid, c->rock2_nt, reg_smem<T>(2, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
         case 4: k_rock2_reg<T, INC, 4><<<grid, c->rock2_nt, reg_smem<T>(4, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 5: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 5><<<grid, c->rock2_nt, reg_smem<T>(5, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 6: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 6><<<grid, c->rock2_nt, reg_smem<T>(6, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 7: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 7><<<grid, c->rock2_nt, reg_smem<T>(7, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
         case 8: k_rock2_reg<T, INC, 8><<<grid, c->rock2_nt, reg_smem<T>(8, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
         case 16: k_rock2_reg<T, INC, 16><<<grid, c->rock2_nt, reg_smem<T>(16, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
         default:
@@ -1199,6 +1211,9 @@ int gw_fused_prepare(gw_ctx *c) {
     switch (lpt) {
         case 2: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 2>, reg_smem<float>(2, nt), nt, reg_smem<float>(2)) : occupancy(&per_sm, k_rock2_reg<double, false, 2>, reg_smem<double>(2, nt), nt, reg_smem<double>(2)); break;
         case 4: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 4>, reg_smem<float>(4, nt), nt, reg_smem<float>(4)) : occupancy(&per_sm, k_rock2_reg<double, false, 4>, reg_smem<double>(4, nt), nt, reg_smem<double>(4)); break;
+        case 5: e = occupancy(&per_sm, k_rock2_reg<float, true, 5>, reg_smem<float>(5, nt), nt, reg_smem<float>(5)); break;   // float only
+        case 6: e = occupancy(&per_sm, k_rock2_reg<float, true, 6>, reg_smem<float>(6, nt), nt, reg_smem<float>(6)); break;
+        case 7: e = occupancy(&per_sm, k_rock2_reg<float, true, 7>, reg_smem<float>(7, nt), nt, reg_smem<float>(7)); break;
         case 8: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 8>, reg_smem<float>(8, nt), nt, reg_smem<float>(8)) : occupancy(&per_sm, k_rock2_reg<double, false, 8>, reg_smem<double>(8, nt), nt, reg_smem<double>(8)); break;
         case 16: e = mix ? occupancy(&per_sm, k_rock2_reg<float, true, 16>, reg_smem<float>(16, nt), nt, reg_smem<float>(16)) : occupancy(&per_sm, k_rock2_reg<double, false, 16>, reg_smem<double>(16, nt), nt, reg_smem<double>(16)); break;
         default:
