@@ -235,10 +235,11 @@ def run_ours(args):
     try:
         import torch
         pin = torch.empty(ncell, dtype=torch.float64, pin_memory=True).numpy()
+        out_pin = torch.empty(ncell, dtype=torch.float64, pin_memory=True).numpy()
     except Exception:
-        pin = np.empty(ncell)
+        pin, out_pin = np.empty(ncell), np.empty(ncell)
     pin[:] = np.asfortranarray(w["T0"]).ravel(order="F")
-    out_pin = np.empty_like(pin)
+    out_pin[:] = 0.0   # pages resident before the timed region
     series = np.zeros(args.steps * cache.N_bh)
     t0 = time.perf_counter()
     _lib.check(L.gw_set_field(cache.ctx, _lib.dptr(pin)))
