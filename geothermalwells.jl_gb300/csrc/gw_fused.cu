@@ -198,17 +198,24 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
     int pcur = -1;
     long long it = blockIdx.x;
     int buf = 0;
-    if (it < ncols) fetch(order[it], 0);
+    // column indices and profiles run one column ahead of their use, so their
+    // loads are not on the per-column chain
+    long long col = it < ncols ? order[it] : 0;
+    long long col_n = it + gridDim.x < ncols ? order[it + gridDim.x] : 0;
+    int p_cur = it < ncols ? colprof[col] : 0;
+    if (it < ncols) fetch(col, 0);
     for (; it < ncols; it += gridDim.x, buf ^= 1) {
-        const long long col = order[it];
         const long long nxt = it + gridDim.x;
+        const int p = p_cur;
+        long long col_nn = 0;
         if (nxt < ncols) {
-            fetch(order[nxt], buf ^ 1);
+            fetch(col_n, buf ^ 1);
+            if (nxt + gridDim.x < ncols) col_nn = order[nxt + gridDim.x];
+            p_cur = colprof[col_n];
             cp_async_wait<1>();
         } else {
             cp_async_wait<0>();
         }
-        const int p = colprof[col];
         if (p != pcur) {   // block-uniform
             pcur = p;
 #pragma unroll
@@ -289,6 +296,8 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
         for (int i = 0; i < LPT; ++i)
             if (t + nt * i < nz) uc[nt * i] = st[st0 + nts * i];
         __syncthreads();   // this buffer is refilled by the next iteration's fetch
+        col = col_n;
+        col_n = col_nn;
     }
 }
 
