@@ -62,3 +62,27 @@ def test_mixed_field_roundtrip(gwlib):
     cache.set_field(T)
     back = cache.get_field()
     assert np.max(np.abs(back - T)) < 1e-5
+
+
+# The float ROCK2 column kernel takes 4..8 levels per thread, whichever pads
+# the column least (gw_fused.cu, rock2_lpt); these z resolutions of the small
+# well select each of them: nz = 14, 129, 161, 193, 225.
+LPT_NZ_CELLS = {4: 12, 5: 127, 6: 159, 7: 191, 8: 223}
+
+
+def float_levels_per_thread(nz):
+    best, pad = 8, ((nz + 7) // 8 + 31) // 32 * 32 * 8
+    for L in range(7, 3, -1):
+        nt = ((nz + L - 1) // L + 31) // 32 * 32
+        if nt <= 256 and nt * L < pad:
+            best, pad = L, nt * L
+    return best
+
+
+@pytest.mark.parametrize("lpt", sorted(LPT_NZ_CELLS))
+def test_mixed_rock2_levels_per_thread(lpt, gwlib):
+    w = W.small_case(nz_cells=LPT_NZ_CELLS[lpt], n_layers=2)
+    assert float_levels_per_thread(len(w["gridz"])) == lpt
+    cache, sol, u, out = run_both(w, 4)
+    assert np.max(np.abs(sol.T_outlet - out)) < 1e-4
+    assert np.max(np.abs(sol.u[-1] - u)) < 1e-3
