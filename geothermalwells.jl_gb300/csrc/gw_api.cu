@@ -409,11 +409,13 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
     }
     GW_CUDA(cudaMemset(c->d_outlet, 0, c->nbh * sizeof(double)));
     GW_CUDA(cudaMemset(c->d_energy, 0, c->nbh * sizeof(double)));
-    c->fused = unique_cols && gw_fused_supported(c);
+    // the fused pipe kernels put one chunk per grid row (at most 65535)
+    c->fused = unique_cols && c->n_pipe_chunks <= 65535 && gw_fused_supported(c);
     if (c->fused && (rc = gw_fused_prepare(c))) return fail(rc);
     if (mixed(c) && !c->fused)
-        return fail(gw_fail(GW_ERR_UNSUPPORTED, "GW_PREC_MIXED needs the fused step: nz too large or "
-                                                "a pipe column shared by two boreholes"));
+        return fail(gw_fail(GW_ERR_UNSUPPORTED, "GW_PREC_MIXED needs the fused step: nz too large, "
+                                                "a pipe column shared by two boreholes, or more than "
+                                                "65535 chunks of 16 pipe columns"));
     *out = c;
     return GW_OK;
 }
