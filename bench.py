@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--no-compare", action="store_true",
                    help="skip timing the other precision beside the main one")
     p.add_argument("--cpu-sample-steps", type=int, default=1)
+    p.add_argument("--cpu-threads", type=int, default=0,
+                   help="reference arm: host threads for the oracle (default: all cores)")
     p.add_argument("--accuracy", type=int, default=0, metavar="NSTEPS",
                    help="run FP64 and mixed for NSTEPS steps and report their differences")
     p.add_argument("--dt", type=float, default=0.0, help="override the workload's step size [s]")
@@ -141,13 +143,14 @@ def reduce_replicas(dist, t_ms, units, device="cuda"):
     return float(t.item()), float(u.item())
 
 
-def cpu_baseline(w, sample_steps):
-    """The oracle (CPU FP64 restatement of the reference) on all host cores,
-    timed on a bounded sample: sample_steps full time steps of the workload."""
+def cpu_baseline(w, sample_steps, threads=0):
+    """The oracle (CPU FP64 restatement of the reference) on all host cores
+    (or `threads` of them), timed on a bounded sample: sample_steps full time
+    steps of the workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from geothermalwells_gb300 import rock2
-    cores = O.set_threads(os.cpu_count() or 1)
+    cores = O.set_threads(threads if threads > 0 else (os.cpu_count() or 1))
     orc = O.Oracle(w["gridx"], w["gridy"], w["gridz"], w["boreholes"], w["materials"],
                    w["inlet_model"])
     s, _ = rock2.choose_stages(w["dt"], orc.eigen_estimate())
@@ -169,7 +172,7 @@ def run_reference(args):
         return
     w = workload(args.workload, args.dt)
     steps = max(1, min(args.steps, 2))
-    cb = cpu_baseline(w, steps)
+    cb = cpu_baseline(w, steps, args.cpu_threads)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": METRIC,
             "n_gpus": args.gpus, "steps": steps, "warmup": 0, "ms_per_step": cb["seconds"] * 1e3 / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
