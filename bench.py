@@ -55,6 +55,9 @@ def parse():
     p.add_argument("--accuracy", type=int, default=0, metavar="NSTEPS",
                    help="run FP64 and mixed for NSTEPS steps and report their differences")
     p.add_argument("--dt", type=float, default=0.0, help="override the workload's step size [s]")
+    p.add_argument("--accuracy-suite", action="store_true",
+                   help="errors of every GPU path on every configuration (oracle / FP64 reference)")
+    p.add_argument("--suite", default="", help="with --accuracy-suite: subset, e.g. cfg1,cfg2")
     return p.parse_args()
 
 
@@ -335,6 +338,125 @@ def run_accuracy(args):
     print(json.dumps(line), flush=True)
 
 
+def _gpu_solve(w, precision, nsteps, flags=0, T0=None):
+    """Final field, outlet series, extracted heat and wall time of a fused
+    GPU solve of nsteps steps (flags: GW_MIXED_* options of a mixed run)."""
+    from geothermalwells_gb300 import (GB300, ODEProblem, ROCK2, _lib, create_cache, eigen_estimator,
+                                       rhs_diffusion_z, solve)
+    cache = create_cache(backend=GB300(precision=precision), gridx=w["gridx"], gridy=w["gridy"],
+                         gridz=w["gridz"], materials=w["materials"], boreholes=w["boreholes"],
+                         inlet_model=w["inlet_model"])
+    if flags:
+        _lib.check(_lib.load().gw_set_mixed_options(cache.ctx, flags))
+    u0 = w["T0"] if T0 is None else T0
+    t0 = time.perf_counter()
+    sol = solve(ODEProblem(rhs_diffusion_z, u0, (0.0, nsteps * w["dt"]), cache),
+                ROCK2(max_stages=100, eigen_est=eigen_estimator), dt=w["dt"], adaptive=False)
+    wall = time.perf_counter() - t0
+    cache.close()
+    return sol.u[-1], sol.T_outlet, sol.energy, wall
+
+
+def _oracle_solve(w, nsteps, T0=None):
+    """The oracle's final field and outlet series (all host threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from geothermalwells_gb300 import rock2
+    O.set_threads(os.cpu_count() or 1)
+    orc = O.Oracle(w["gridx"], w["gridy"], w["gridz"], w["boreholes"], w["materials"], w["inlet_model"])
+    s, _ = rock2.choose_stages(w["dt"], orc.eigen_estimate())
+    u = (w["T0"] if T0 is None else T0).copy(order="F")
+    t0 = time.perf_counter()
+    out = orc.simulate(u, 0.0, w["dt"], nsteps, s, rock2.coefficients(s))
+    wall = time.perf_counter() - t0
+    orc.close()
+    return u, out, wall
+
+
+def _energy_from_outlet(w, out):
+    """sum over steps of mdot c_w (T_out - T_in) dt per borehole, the balance
+    gw_get_energy keeps, from an outlet series (constant or heat-exchanger inlet)."""
+    from geothermalwells_gb300.physics import RHO_WATER
+    c_w = w["materials"].rho_c_water / RHO_WATER
+    im = w["inlet_model"]
+    mdot = np.array([b.mdot for b in w["boreholes"]])
+    t_in = (im.param if im.kind == 0 else out - im.param)
+    return np.sum(mdot * c_w * (out - t_in) * w["dt"], axis=0)
+
+
+def _errors(u, out, energy, u_ref, out_ref, energy_ref):
+    return {"field_max_abs_dT_K": float(np.max(np.abs(u - u_ref))),
+            "field_max_rel": float(np.max(np.abs(u - u_ref)) / np.max(np.abs(u_ref))),
+            "outlet_max_abs_err_K": float(np.max(np.abs(out - out_ref))),
+            "heat_rel_err": float(np.max(np.abs(energy - energy_ref) / np.abs(energy_ref)))}
+
+
+def run_accuracy_suite(args):
+    """Errors of the GPU paths on every configuration, against the FP64 oracle
+    (the reference's algorithm in C) where it runs in seconds, else against
+    the FP64 GPU path (itself pinned to the oracle at 1e-10):
+
+      cfg1 2 mm well, 1 simulated hour (60 steps of 60 s), oracle in full;
+      cfg2 large well, 24-step window of the 300 s steps against the oracle,
+           and 30 days (12,960 steps of 200 s) mixed against FP64;
+      cfg4 four ensemble designs, a 12-step window against the oracle and
+           5 days (720 steps of 600 s) mixed against FP64;
+      cfg5 the adjoint workload's forward solve (22 layers, 3024 steps of
+           200 s), mixed against FP64.
+
+    Each mixed run is repeated with the two FP64 options of the mixed step
+    (GW_MIXED_ROCK2_F64, GW_MIXED_REFINE) and their wall times."""
+    from geothermalwells_gb300 import _lib
+    from geothermalwells_gb300 import workloads as W
+    variants = {"mixed": 0, "mixed+rock2_f64": _lib.GW_MIXED_ROCK2_F64,
+                "mixed+refine": _lib.GW_MIXED_REFINE,
+                "mixed+both": _lib.GW_MIXED_ROCK2_F64 | _lib.GW_MIXED_REFINE}
+    res = {}
+    only = set(args.suite.split(",")) if args.suite else None
+
+    def against_oracle(name, w, nsteps, T0=None):
+        u_r, o_r, wall_r = _oracle_solve(w, nsteps, T0)
+        e_r = _energy_from_outlet(w, o_r)
+        entry = {"workload": w["name"], "cells": int(np.prod(u_r.shape)), "steps": nsteps, "dt_s": w["dt"],
+                 "reference": "FP64 oracle", "oracle_wall_s": wall_r}
+        u, o, e, wall = _gpu_solve(w, "fp64", nsteps, T0=T0)
+        entry["fp64"] = dict(_errors(u, o, e, u_r, o_r, e_r), wall_s=wall)
+        for v, f in variants.items():
+            u, o, e, wall = _gpu_solve(w, "mixed", nsteps, f, T0=T0)
+            entry[v] = dict(_errors(u, o, e, u_r, o_r, e_r), wall_s=wall)
+        res[name] = entry
+        print(json.dumps({name: entry}), flush=True)
+
+    def against_fp64(name, w, nsteps, T0=None, vlist=None):
+        u_r, o_r, e_r, wall_r = _gpu_solve(w, "fp64", nsteps, T0=T0)
+        entry = {"workload": w["name"], "cells": int(np.prod(u_r.shape)), "steps": nsteps, "dt_s": w["dt"],
+                 "simulated_days": nsteps * w["dt"] / 86400.0, "reference": "FP64 GPU path",
+                 "fp64_wall_s": wall_r}
+        for v in (vlist or variants):
+            u, o, e, wall = _gpu_solve(w, "mixed", nsteps, variants[v], T0=T0)
+            entry[v] = dict(_errors(u, o, e, u_r, o_r, e_r), wall_s=wall)
+        res[name] = entry
+        print(json.dumps({name: entry}), flush=True)
+
+    if not only or "cfg1" in only:
+        against_oracle("cfg1_2mm_1h", W.single_well_2mm(), 60)
+    if not only or "cfg2" in only:
+        w = W.single_well_large()
+        against_oracle("cfg2_large_24steps", w, 24)
+        against_fp64("cfg2_large_30days", dict(w, dt=200.0), 12960)
+    if not only or "cfg4" in only:
+        designs = W.ensemble()
+        for q in (0, 1, 2, 3):
+            d = dict(designs[q], dt=600.0, name="ensemble_design_%d" % q)
+            T0 = W.initial_field(d)
+            against_oracle("cfg4_design%d_12steps" % q, dict(d, T0=T0), 12)
+            against_fp64("cfg4_design%d_5days" % q, dict(d, T0=T0), 720, vlist=["mixed", "mixed+both"])
+    if not only or "cfg5" in only:
+        w = W.adjoint_well()
+        against_fp64("cfg5_adjoint_forward_7days", w, w["nsteps"])
+    print(json.dumps({"accuracy_suite": res}), flush=True)
+
+
 def run_thomas(args):
     """Batched tridiagonal microbenchmark: 262,144 seeded systems, lengths
     U[32, 1024]; algorithmic traffic 5 words per unknown (a, b, c, d in, x
@@ -595,6 +717,9 @@ def main():
         return
     if args.workload == "thomas":
         run_thomas(args)
+        return
+    if args.accuracy_suite:
+        run_accuracy_suite(args)
         return
     if args.accuracy:
         run_accuracy(args)

@@ -863,8 +863,10 @@ int finish_grad(gw_ctx *c, double dt, int nsteps, double wE, double *grad) {
 
 int check_common(gw_ctx *c, double dt, int max_stages, int *s) {
     if (!(dt > 0) || !std::isfinite(dt)) return gw_fail(GW_ERR_ARG, "dt must be positive and finite");
-    if (c->inlet_kind == GW_INLET_SCHEDULE)
+    if (c->inlet_kind == GW_INLET_SCHEDULE || c->inlet_kind == GW_INLET_EXPRESSION)
         return gw_fail(GW_ERR_UNSUPPORTED, "the adjoint takes constant or heat-exchanger inlets");
+    if (c->modular_reason & GW_MODULAR_SHARED_COLUMN)
+        return gw_fail(GW_ERR_UNSUPPORTED, "the adjoint needs every pipe column in one borehole");
     int covered, rc;
     GW_CUDA(cudaSetDevice(c->device));
     if ((rc = gw_rock2_choose(dt, c->eigen_estimate, max_stages, s, &covered))) return rc;
@@ -1049,6 +1051,9 @@ extern "C" int gw_adjoint(gw_ctx *c, double dt, int nsteps, int max_stages, int 
     if (checkpoint_every < 1) return gw_fail(GW_ERR_ARG, "checkpoint_every must be >= 1");
     int s, rc;
     if ((rc = check_common(c, dt, max_stages, &s))) return rc;
+    if (c->mixed_flags)
+        return gw_fail(GW_ERR_UNSUPPORTED, "the adjoint transposes the default mixed step: "
+                                           "gw_set_mixed_options(ctx, 0) first");
     if (c->precision == GW_PREC_MIXED)
         return adjoint_run<float>(c, dt, nsteps, max_stages, s, checkpoint_every, w_energy, w_outlet, grad,
                                   grad_T0, info);

@@ -148,7 +148,7 @@ int set_reference_profile(gw_ctx *c, const double *T) {
             f[q] = c->h_czp[q] * (tp - tc) - c->h_czm[q] * (tc - tm);
         }
     int rc;
-    if ((rc = copy_to(c->d_Tref, c->Tref))) return rc;
+    if ((rc = copy_to(c->d_Tref, c->Tref)) || (rc = copy_to(c->d_fref64, f))) return rc;
     return copy_to(c->f_fref, to_float(f));
 }
 }  // namespace
@@ -383,6 +383,7 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
             (rc = dalloc(c, &c->f_tp, (size_t)ncol * c->nz)) ||
             (rc = dalloc(c, &c->f_pp, (size_t)ncol * c->countz)) ||
             (rc = dalloc(c, &c->f_fref, (size_t)c->n_profiles * c->nz)) ||
+            (rc = dalloc(c, &c->d_fref64, (size_t)c->n_profiles * c->nz)) ||
             (rc = dalloc(c, &c->d_Tref, c->nz)))
             return fail(rc);
         if ((rc = upload(c, &c->c32.cxm, to_float(cxm))) || (rc = upload(c, &c->c32.cxp, to_float(cxp))) ||
@@ -409,13 +410,15 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
     }
     GW_CUDA(cudaMemset(c->d_outlet, 0, c->nbh * sizeof(double)));
     GW_CUDA(cudaMemset(c->d_energy, 0, c->nbh * sizeof(double)));
-    // the fused pipe kernels put one chunk per grid row (at most 65535)
-    c->fused = unique_cols && c->n_pipe_chunks <= 65535 && gw_fused_supported(c);
+    c->modular_reason = (gw_fused_supported(c) ? 0 : GW_MODULAR_NZ) |
+                        (unique_cols ? 0 : GW_MODULAR_SHARED_COLUMN);
+    c->fused = c->modular_reason == 0;
     if (c->fused && (rc = gw_fused_prepare(c))) return fail(rc);
     if (mixed(c) && !c->fused)
-        return fail(gw_fail(GW_ERR_UNSUPPORTED, "GW_PREC_MIXED needs the fused step: nz too large, "
-                                                "a pipe column shared by two boreholes, or more than "
-                                                "65535 chunks of 16 pipe columns"));
+        return fail(gw_fail(GW_ERR_UNSUPPORTED, (c->modular_reason & GW_MODULAR_NZ)
+                                                    ? "GW_PREC_MIXED needs the fused step: nz too large"
+                                                    : "GW_PREC_MIXED needs the fused step: a pipe column "
+                                                      "shared by two boreholes"));
     *out = c;
     return GW_OK;
 }
@@ -445,6 +448,31 @@ int gw_get_info(gw_ctx *c, gw_info_t *o) {
     o->eigen_estimate = c->eigen_estimate;
     o->device_bytes = c->device_bytes;
     o->overlap = c->overlap ? 1 : 0;
+    o->fused = c->fused ? 1 : 0;
+    o->modular_reason = c->modular_reason;
+    o->tiling = c->half_cfg;
+    o->mixed_options = c->mixed_flags;
+    return GW_OK;
+}
+
+int gw_set_tiling(gw_ctx *c, int tiling) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
+    if (tiling < 0 || tiling >= GW_TILINGS) return gw_fail(GW_ERR_ARG, "tiling out of range");
+    c->half_cfg = tiling;
+    c->graph_dt = -1.0;   // recapture the step graph
+    return GW_OK;
+}
+
+int gw_set_mixed_options(gw_ctx *c, int flags) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
+    if (flags & ~(GW_MIXED_ROCK2_F64 | GW_MIXED_REFINE)) return gw_fail(GW_ERR_ARG, "unknown GW_MIXED_* flag");
+    if (!mixed(c)) return flags ? gw_fail(GW_ERR_ARG, "GW_MIXED_* options need a GW_PREC_MIXED context") : GW_OK;
+    int rc = set_device(c);
+    if (rc) return rc;
+    if ((flags & GW_MIXED_ROCK2_F64) && (rc = gw_fused_prepare_rock2_f64(c))) return rc;
+    if ((flags & GW_MIXED_REFINE) && (rc = gw_fused_prepare_refine(c))) return rc;
+    c->mixed_flags = flags;
+    c->graph_dt = -1.0;   // recapture the step graph
     return GW_OK;
 }
 
@@ -500,10 +528,50 @@ int gw_init_thermal_gradient(gw_ctx *c, double T_surface, double gradient) {
     return sync(c);
 }
 
+int gw_set_inlet_program(gw_ctx *c, int n, const int *ops, const double *args) {
+    if (!c || !ops || !args) return gw_fail(GW_ERR_ARG, "NULL argument");
+    if (c->inlet_kind != GW_INLET_EXPRESSION)
+        return gw_fail(GW_ERR_ARG, "the context's inlet kind is not GW_INLET_EXPRESSION");
+    if (n < 1 || n > GW_PROGRAM_MAX) return gw_fail(GW_ERR_ARG, "an inlet program has 1 to 64 operations");
+    // the stack never underflows or grows beyond 16, and one value is left
+    int depth = 0;
+    bool uses_sched = false;
+    for (int i = 0; i < n; ++i) {
+        const int o = ops[i];
+        if (o < GW_OP_CONST || o > GW_OP_MAX) return gw_fail(GW_ERR_ARG, "unknown GW_OP_* in the inlet program");
+        if (o == GW_OP_CONST && !std::isfinite(args[i]))
+            return gw_fail(GW_ERR_ARG, "inlet program constants must be finite");
+        if (o <= GW_OP_BH) ++depth;                      // pushes
+        else if (o == GW_OP_SCHED || o == GW_OP_NEG) {   // unary
+            if (depth < 1) return gw_fail(GW_ERR_ARG, "inlet program: operand missing");
+            uses_sched |= o == GW_OP_SCHED;
+        } else {                                         // binary
+            if (depth < 2) return gw_fail(GW_ERR_ARG, "inlet program: operand missing");
+            --depth;
+        }
+        if (depth > 16) return gw_fail(GW_ERR_ARG, "inlet program: stack deeper than 16");
+    }
+    if (depth != 1) return gw_fail(GW_ERR_ARG, "inlet program must leave exactly one value");
+    int rc = set_device(c);
+    if (rc) return rc;
+    if (!c->d_prog_op) {
+        if ((rc = dalloc(c, &c->d_prog_op, GW_PROGRAM_MAX)) || (rc = dalloc(c, &c->d_prog_arg, GW_PROGRAM_MAX)))
+            return rc;
+    }
+    c->prog_op.assign(ops, ops + n);
+    c->prog_arg.assign(args, args + n);
+    c->prog_sched = uses_sched;
+    GW_CUDA(cudaStreamSynchronize(c->stream));
+    if ((rc = copy_to(c->d_prog_op, c->prog_op)) || (rc = copy_to(c->d_prog_arg, c->prog_arg))) return rc;
+    c->n_prog = n;
+    c->graph_dt = -1.0;   // the captured step reads the program's length
+    return GW_OK;
+}
+
 int gw_set_inlet_schedule(gw_ctx *c, int n, const double *times, const double *values) {
     if (!c || !times || !values) return gw_fail(GW_ERR_ARG, "NULL argument");
-    if (c->inlet_kind != GW_INLET_SCHEDULE)
-        return gw_fail(GW_ERR_ARG, "the context's inlet kind is not GW_INLET_SCHEDULE");
+    if (c->inlet_kind != GW_INLET_SCHEDULE && c->inlet_kind != GW_INLET_EXPRESSION)
+        return gw_fail(GW_ERR_ARG, "the context's inlet kind is not GW_INLET_SCHEDULE or GW_INLET_EXPRESSION");
     if (n < 1) return gw_fail(GW_ERR_ARG, "a schedule needs at least one point");
     for (int q = 0; q < n; ++q) {
         if (!std::isfinite(times[q]) || !std::isfinite(values[q]))
@@ -523,6 +591,41 @@ int gw_set_inlet_schedule(gw_ctx *c, int n, const double *times, const double *v
     std::vector<double> tv(times, times + n);
     tv.insert(tv.end(), values, values + n);
     return copy_to(c->d_sched, tv);
+}
+
+int gw_field_alloc(gw_ctx *c, double **out) {
+    if (!c || !out) return gw_fail(GW_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    int rc = set_device(c);
+    if (rc) return rc;
+    double *p = nullptr;
+    GW_CUDA(cudaMalloc((void **)&p, ncell(c) * sizeof(double)));
+    cudaError_t e = cudaMemsetAsync(p, 0, ncell(c) * sizeof(double), c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        cudaFree(p);
+        return gw_cuda_fail(e, "cudaMemsetAsync(field)");
+    }
+    *out = p;
+    return GW_OK;
+}
+
+int gw_field_free(gw_ctx *c, double *p) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
+    if (!p) return GW_OK;
+    int rc = set_device(c);
+    if (rc || (rc = sync(c))) return rc;
+    GW_CUDA(cudaFree(p));
+    return GW_OK;
+}
+
+int gw_field_copy(gw_ctx *c, double *dst, const double *src) {
+    if (!c || !dst || !src) return gw_fail(GW_ERR_ARG, "NULL argument");
+    int rc = set_device(c);
+    if (rc) return rc;
+    if (dst == src) return GW_OK;
+    GW_CUDA(cudaMemcpyAsync(dst, src, ncell(c) * sizeof(double), cudaMemcpyDefault, c->stream));
+    return sync(c);
 }
 
 int gw_lincomb(gw_ctx *c, double *dst, int n, const double *coeffs, const double *const *srcs) {
@@ -573,16 +676,29 @@ int gw_thomas(gw_ctx *c, double *U, const double *RHS, double dt, int dir) {
     return sync(c);
 }
 
+// An expression inlet needs its program (and the schedule it reads).
+static int inlet_ready(const gw_ctx *c) {
+    if (c->inlet_kind != GW_INLET_EXPRESSION) return GW_OK;
+    if (c->n_prog == 0) return gw_fail(GW_ERR_ARG, "no inlet program set (gw_set_inlet_program)");
+    if (c->prog_sched && c->n_sched == 0)
+        return gw_fail(GW_ERR_ARG, "the inlet program reads a schedule: gw_set_inlet_schedule first");
+    return GW_OK;
+}
+
 int gw_advection(gw_ctx *c, double *phi, double dt, double t) {
     if (!c || !phi) return gw_fail(GW_ERR_ARG, "NULL argument");
-    int rc = set_device(c);
+    int rc = inlet_ready(c);
+    if (rc) return rc;
+    rc = set_device(c);
     if (rc || (rc = gw_launch_advection(c, phi, dt, t))) return rc;
     return sync(c);
 }
 
 int gw_adi_adv(gw_ctx *c, double *u, double *temp, double t, double dt) {
     if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
-    int rc = check_field_ptrs(u, temp);
+    int rc = inlet_ready(c);
+    if (rc) return rc;
+    rc = check_field_ptrs(u, temp);
     if (rc || (rc = set_device(c))) return rc;
     if (u == temp) return gw_fail(GW_ERR_ARG, "temp must not alias u");
     if ((rc = gw_ensure_factors(c, dt / 2))) return rc;
@@ -607,6 +723,12 @@ int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
         return gw_fail(c->fused ? GW_ERR_ARG : GW_ERR_UNSUPPORTED,
                        c->fused ? "no inlet schedule set (gw_set_inlet_schedule)"
                                 : "a schedule inlet needs the fused step");
+    if (c->inlet_kind == GW_INLET_EXPRESSION) {
+        if (!c->fused) return gw_fail(GW_ERR_UNSUPPORTED, "an inlet program needs the fused step");
+        if (c->n_prog == 0) return gw_fail(GW_ERR_ARG, "no inlet program set (gw_set_inlet_program)");
+        if (c->prog_sched && c->n_sched == 0)
+            return gw_fail(GW_ERR_ARG, "the inlet program reads a schedule: gw_set_inlet_schedule first");
+    }
     if ((rc = gw_prepare_step(c, dt, s, nsteps))) return rc;
     if ((rc = gw_set_step_time(c, t0, dt))) return rc;
     c->t_now = t0 + nsteps * dt;

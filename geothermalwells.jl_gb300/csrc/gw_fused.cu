@@ -26,6 +26,7 @@
 
 #include "gw_internal.h"
 #include "gw_fused.h"
+#include "gw_inlet.cuh"
 
 namespace {
 
@@ -143,13 +144,16 @@ __global__ void __launch_bounds__(256) k_rock2_col(T *__restrict__ u, const int 
 // free of shared-memory bank conflicts.
 __device__ __forceinline__ int spad(int k) { return k + (k >> 5); }
 
-template <typename T, bool INC, int LPT>
-__global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) k_rock2_reg(T *__restrict__ u, const int *__restrict__ order,
+// C is the arithmetic type of the stages (the storage type T by default;
+// double over float storage for the mixed path's FP64 stage accumulation,
+// where the column is rounded to float once, when it is stored).
+template <typename T, bool INC, int LPT, typename C = T>
+__global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) k_rock2_reg(T *__restrict__ u, const int *__restrict__ order,
                                                    const int *__restrict__ colprof,
-                                                   const T *__restrict__ czm,
-                                                   const T *__restrict__ czp,
-                                                   const T *__restrict__ fref,
-                                                   const T *__restrict__ sc, int s, int nz,
+                                                   const C *__restrict__ czm,
+                                                   const C *__restrict__ czp,
+                                                   const C *__restrict__ fref,
+                                                   const C *__restrict__ sc, int s, int nz,
                                                    long long ncols) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // nt = blockDim.x threads (a multiple of 32, at most 256), LPT levels each
@@ -159,7 +163,7 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
     // run ends of every thread, shifted by one slot so thread t reads its
     // neighbours at [t] (left, from s_hi) and [t + 1] (right, from s_lo)
     // without predicates; the outer slots hold zeros.
-    __shared__ T s_lo[2][257], s_hi[2][257];
+    __shared__ C s_lo[2][257], s_hi[2][257];
     const int t = threadIdx.x;
     const int kb = t * LPT;
     const int nrec = s - 2;
@@ -168,7 +172,7 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
     // have zero coefficients, so they never feed a real level (the real
     // bottom level's cp is 0) and every thread owns exactly LPT levels.
     for (int k = nz + t; k < nt * LPT; k += nt) { stage[spad(k)] = T(0); stage[nzs + spad(k)] = T(0); }
-    if (t < 2) { s_hi[t][0] = T(0); s_lo[t][nt] = T(0); }
+    if (t < 2) { s_hi[t][0] = C(0); s_lo[t][nt] = C(0); }
     // thread t copies levels t + nt i, whose padded slots are spad(t) + nts i
     const int st0 = spad(t), nts = nt + nt / 32;
     auto fetch = [&](long long col, int buf) {
@@ -179,7 +183,7 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
             if (t + nt * i < nz) cp_async<sizeof(T)>(d + nts * i, g + nt * i, true);
         cp_async_commit();
     };
-    auto exchange = [&](const T (&v)[LPT], T &left, T &right) {
+    auto exchange = [&](const C (&v)[LPT], C &left, C &right) {
         s_lo[xb][t] = v[0];
         s_hi[xb][t + 1] = v[LPT - 1];
         __syncthreads();
@@ -187,14 +191,14 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
         right = s_lo[xb][t + 1];
         xb ^= 1;
     };
-    auto apply = [&](const T (&v)[LPT], const T (&cm)[LPT], const T (&cp)[LPT], int i, T left,
-                     T right) {
-        const T gc = v[i];
-        const T gm = i == 0 ? left : v[i > 0 ? i - 1 : 0];
-        const T gp = i + 1 < LPT ? v[i + 1 < LPT ? i + 1 : i] : right;
+    auto apply = [&](const C (&v)[LPT], const C (&cm)[LPT], const C (&cp)[LPT], int i, C left,
+                     C right) {
+        const C gc = v[i];
+        const C gm = i == 0 ? left : v[i > 0 ? i - 1 : 0];
+        const C gp = i + 1 < LPT ? v[i + 1 < LPT ? i + 1 : i] : right;
         return cp[i] * (gp - gc) - cm[i] * (gc - gm);
     };
-    T cm[LPT], cp[LPT], fr[LPT];
+    C cm[LPT], cp[LPT], fr[LPT];
     int pcur = -1;
     long long it = blockIdx.x;
     int buf = 0;
@@ -222,43 +226,43 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
             for (int i = 0; i < LPT; ++i) {
                 const bool ok = kb + i < nz;
                 const size_t q = (size_t)p * nz + kb + i;
-                cm[i] = ok ? __ldg(czm + q) : T(0);
-                cp[i] = ok ? __ldg(czp + q) : T(0);
-                fr[i] = (INC && fref && ok) ? __ldg(fref + q) : T(0);
+                cm[i] = ok ? __ldg(czm + q) : C(0);
+                cp[i] = ok ? __ldg(czp + q) : C(0);
+                fr[i] = (INC && fref && ok) ? __ldg(fref + q) : C(0);
             }
         }
         __syncthreads();
         T *st = stage + (size_t)buf * nzs;
-        T base[LPT], F0[LPT], prev[LPT], cur[LPT];
+        C base[LPT], F0[LPT], prev[LPT], cur[LPT];
 #pragma unroll
-        for (int i = 0; i < LPT; ++i) base[i] = st[spad(kb + i)];
-        T left, right;
+        for (int i = 0; i < LPT; ++i) base[i] = (C)st[spad(kb + i)];
+        C left, right;
         exchange(base, left, right);
         if (INC) {
 #pragma unroll
             for (int i = 0; i < LPT; ++i) {
                 F0[i] = fr[i] + apply(base, cm, cp, i, left, right);
-                prev[i] = T(0);
-                cur[i] = T(0);
+                prev[i] = C(0);
+                cur[i] = C(0);
             }
         } else {
 #pragma unroll
-            for (int i = 0; i < LPT; ++i) { F0[i] = T(0); prev[i] = base[i]; cur[i] = base[i]; }
+            for (int i = 0; i < LPT; ++i) { F0[i] = C(0); prev[i] = base[i]; cur[i] = base[i]; }
         }
         // recurrence g_j = g_{j-1} + h mu_j A g_{j-1} + kappa_j (g_{j-1} - g_{j-2});
         // in the increment form g = base + delta and A g = F0 + A delta
         for (int j = 0; j < nrec; ++j) {
-            const T hmu = (T)sc[2 * j], kap = (T)sc[2 * j + 1];
+            const C hmu = sc[2 * j], kap = sc[2 * j + 1];
             if (INC && j == 0) {
 #pragma unroll
                 for (int i = 0; i < LPT; ++i) { prev[i] = cur[i]; cur[i] = hmu * F0[i]; }
                 continue;
             }
             exchange(cur, left, right);
-            T out[LPT];
+            C out[LPT];
 #pragma unroll
             for (int i = 0; i < LPT; ++i) {
-                T a = apply(cur, cm, cp, i, left, right);
+                C a = apply(cur, cm, cp, i, left, right);
                 if (INC) a += F0[i];
                 out[i] = cur[i] + hmu * a + kap * (cur[i] - prev[i]);
             }
@@ -267,8 +271,8 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
         }
         // finishing procedure: gq = gp + h sigma A gp;
         // y = gq + (h tau / sigma) A gq + (1 - tau / sigma^2) (gq - gp)
-        const T hs = (T)sc[2 * nrec], hts = (T)sc[2 * nrec + 1], c3 = (T)sc[2 * nrec + 2];
-        T q[LPT];
+        const C hs = sc[2 * nrec], hts = sc[2 * nrec + 1], c3 = sc[2 * nrec + 2];
+        C q[LPT];
         if (INC && nrec == 0) {
 #pragma unroll
             for (int i = 0; i < LPT; ++i) q[i] = hs * F0[i];
@@ -276,7 +280,7 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
             exchange(cur, left, right);
 #pragma unroll
             for (int i = 0; i < LPT; ++i) {
-                T a = apply(cur, cm, cp, i, left, right);
+                C a = apply(cur, cm, cp, i, left, right);
                 if (INC) a += F0[i];
                 q[i] = cur[i] + hs * a;
             }
@@ -285,10 +289,10 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(T) == 4 ? 3 : 2) : 1) 
         // results go back through the staging buffer for a coalesced store
 #pragma unroll
         for (int i = 0; i < LPT; ++i) {
-            T a = apply(q, cm, cp, i, left, right);
+            C a = apply(q, cm, cp, i, left, right);
             if (INC) a += F0[i];
-            const T y = q[i] + hts * a + c3 * (q[i] - cur[i]);
-            st[spad(kb + i)] = INC ? base[i] + y : y;
+            const C y = q[i] + hts * a + c3 * (q[i] - cur[i]);
+            st[spad(kb + i)] = (T)(INC ? base[i] + y : y);
         }
         __syncthreads();
         T *uc = u + col * nz + t;
@@ -319,6 +323,13 @@ __device__ __forceinline__ double absT(T v, const double *Tref, int k) {
 // (per warp, then across warps in warp order): the results do not depend on
 // scheduling.
 
+// Pipe kernels put the chunks on the grid's y dimension (at most 65535),
+// continued on z for more chunks.
+constexpr int kChunkRows = 65535;
+inline dim3 chunk_grid(int kblocks, int nchunks) {
+    return dim3(kblocks, std::min(nchunks, kChunkRows), (nchunks + kChunkRows - 1) / kChunkRows);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *__restrict__ part,
                                                     const T *__restrict__ src,
@@ -329,10 +340,10 @@ __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *
                                                     const T *__restrict__ cmt,
                                                     const T *__restrict__ cpt,
                                                     const double *__restrict__ Tref, int nx, int ny,
-                                                    int nz, double h, int dir) {
+                                                    int nz, double h, int dir, int nchunks) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int ch = blockIdx.y;
-    if (k >= nz) return;
+    const int ch = blockIdx.y + kChunkRows * blockIdx.z;   // chunk rows of at most 65535
+    if (k >= nz || ch >= nchunks) return;
     const int4 C = chunks[ch];   // (borehole, first column, end column, outer?)
     const int zc = zclass[k];
     const T hh = (T)h;
@@ -492,25 +503,21 @@ __global__ void k_adv_table(GwAdvRec *__restrict__ tab, const double *__restrict
     tab[e] = r;
 }
 
-// Schedule inlet: T_in at t = t0 + (n + 1 + off) dt for the step n the
-// counter holds (off 0: first advection, 1/2: second), for every borehole.
+// Time-dependent inlets at t = t0 + (n + 1 + off) dt for the step n the
+// counter holds (off 0: first advection, 1/2: second): the schedule
+// (nprog = 0), or the inlet program of every borehole with the outlet
+// temperatures of this pipe pass (GW_INLET_EXPRESSION).
 __global__ void k_inlet_eval(double *__restrict__ inlet_v, const double *__restrict__ sched, int ns,
                              const double *__restrict__ time, const int *__restrict__ counter, double off,
-                             int nbh) {
+                             int nbh, const int *__restrict__ op, const double *__restrict__ arg, int nprog,
+                             const double *__restrict__ outlet) {
     const double t = __fma_rn((double)(*counter) + 1.0 + off, time[1], time[0]);
-    const double *ts = sched, *vs = sched + ns;
-    double v;
-    if (t <= ts[0]) v = vs[0];
-    else if (t >= ts[ns - 1]) v = vs[ns - 1];
-    else {
-        int lo = 0, hi = ns - 1;   // ts[lo] <= t < ts[hi]
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (ts[mid] <= t) lo = mid; else hi = mid;
-        }
-        const double a = __ddiv_rn(__dsub_rn(t, ts[lo]), __dsub_rn(ts[hi], ts[lo]));
-        v = __fma_rn(a, __dsub_rn(vs[hi], vs[lo]), vs[lo]);
+    if (nprog > 0) {
+        for (int b = threadIdx.x; b < nbh; b += blockDim.x)
+            inlet_v[b] = gw_program_eval(op, arg, nprog, outlet[b], t, b, sched, ns);
+        return;
     }
+    const double v = gw_sched_eval(sched, ns, t);
     for (int b = threadIdx.x; b < nbh; b += blockDim.x) inlet_v[b] = v;
 }
 
@@ -529,10 +536,11 @@ __global__ void __launch_bounds__(128) k_advect_c(T *__restrict__ pp, const T *_
                                                   const double *__restrict__ outlet,
                                                   const double *__restrict__ Tref, int nz, int countz,
                                                   int inlet_kind, double inlet_param,
-                                                  const double *__restrict__ inlet_v) {
+                                                  const double *__restrict__ inlet_v, int nchunks) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= countz) return;
-    const int4 C = chunks[blockIdx.y];   // (borehole, first column, end column, annulus?)
+    const int ch = blockIdx.y + kChunkRows * blockIdx.z;
+    if (k >= countz || ch >= nchunks) return;
+    const int4 C = chunks[ch];   // (borehole, first column, end column, annulus?)
     const int b = C.x;
     const GwAdvRec r = tab[((size_t)b * countz + k) * 2 + C.w];
     T *out = pp + k;
@@ -540,7 +548,7 @@ __global__ void __launch_bounds__(128) k_advect_c(T *__restrict__ pp, const T *_
         double v;
         if (r.type == kAdvInlet) {
             v = inlet_kind == GW_INLET_CONSTANT ? inlet_param
-              : inlet_kind == GW_INLET_SCHEDULE ? inlet_v[b] : outlet[b] - inlet_param;
+              : inlet_kind >= GW_INLET_SCHEDULE ? inlet_v[b] : outlet[b] - inlet_param;
         } else {
             const double *m = ann_mean + (size_t)b * nz;
             v = __fma_rn(r.alpha, m[r.ir], __dmul_rn(__dsub_rn(1.0, r.alpha), m[r.il]));
@@ -595,6 +603,7 @@ constexpr int kTilings = 7;   // the last one is the segmented kernel (k_half_se
 constexpr int kTileHW[kTilings] = {4, 8, 8, 4, 2, 8, 2};
 constexpr int kTileHR[kTilings] = {16, 16, 8, 32, 16, 32, 16};
 constexpr int kSegCfg = 6;
+static_assert(kTilings == GW_TILINGS, "tiling count of the C ABI");
 constexpr int kSegS = 8, kSegR = 32;   // segments per line, rows per segment (lines up to 256)
 constexpr int kHG = 4;    // rows whose coefficients are loaded together
 constexpr int kHB = 16;    // rows per backward batch
@@ -912,6 +921,75 @@ __global__ void __launch_bounds__(32 * HW * S) k_half_seg(T *__restrict__ dst, c
     }
 }
 
+// Mixed path, GW_MIXED_REFINE: one residual correction of a half step's
+// line solves.  The float solve left x in dst for (I - h A_line) x = b, b the
+// explicit sweep (I + h A_other) of src (the advected pipe value at pipe
+// rows).  Per line, in double: r = b - (I - h A_line) x with the double
+// coefficient tables, then (I - h A_line) d = r with the same LU factors the
+// float solve used, and x <- x + d, rounded to float once.  One thread per
+// line (lanes = levels, so every row access of a warp is contiguous); the
+// forward values of the correction solve go to the scratch field yb.
+// Coefficient layouts: line direction [zc][line][row] (lcm, lcp and the
+// factors), the other direction [zc][row][line] (ecm, ecp).
+template <bool XL>
+__global__ void __launch_bounds__(128) k_half_refine(float *__restrict__ x, float *__restrict__ yb,
+                                                     const float *__restrict__ src,
+                                                     const float *__restrict__ pp,
+                                                     const int *__restrict__ pipe_line,
+                                                     const int *__restrict__ zclass,
+                                                     const double *__restrict__ lcm,
+                                                     const double *__restrict__ lcp,
+                                                     const double *__restrict__ ecm,
+                                                     const double *__restrict__ ecp,
+                                                     const float *__restrict__ fa,
+                                                     const float *__restrict__ fib,
+                                                     const float *__restrict__ fcu, int nx, int ny,
+                                                     int nz, int countz, double h) {
+    const int nl = XL ? ny : nx, N = XL ? nx : ny;
+    const int k = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int m = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (k >= nz || m >= nl) return;
+    const long long mst = XL ? (long long)nz : (long long)nz * ny;
+    const long long rst = XL ? (long long)nz * ny : (long long)nz;
+    const int zc = zclass[k];
+    const size_t lb = ((size_t)zc * nl + m) * N;   // line-direction tables
+    const bool pipe_levels = k < countz && __ldg(pipe_line + (size_t)nl * N + m) != 0;
+    const int *pline = pipe_line + (size_t)m * N;
+    const long long e0 = k + m * mst;
+    auto b_at = [&](int l) -> double {   // right-hand side of row l, in double
+        const long long e = e0 + l * rst;
+        const int pq = pipe_levels ? __ldg(pline + l) : -1;
+        if (pq >= 0) return (double)pp[(size_t)pq * countz + k];
+        const double uc = src[e];
+        const double up = m + 1 < nl ? (double)src[e + mst] : uc;
+        const double um = m > 0 ? (double)src[e - mst] : uc;
+        const size_t q = ((size_t)zc * N + l) * nl + m;
+        return fma(h, __ldg(ecp + q) * (up - uc) - __ldg(ecm + q) * (uc - um), uc);
+    };
+    double xm = 0.0, xc = x[e0], y = 0.0;
+    for (int l = 0; l < N; ++l) {
+        const double xp = l + 1 < N ? (double)x[e0 + (l + 1) * rst] : 0.0;
+        const double cm = __ldg(lcm + lb + l), cp = __ldg(lcp + lb + l);
+        double ax = (1.0 + h * (cm + cp)) * xc;
+        if (l > 0) ax -= h * cm * xm;
+        if (l + 1 < N) ax -= h * cp * xp;
+        const double r = b_at(l) - ax;
+        y = (r - (double)__ldg(fa + lb + l) * y) * (double)__ldg(fib + lb + l);
+        yb[e0 + l * rst] = (float)y;
+        xm = xc;
+        xc = xp;
+    }
+    // back substitution of the correction, added to x (x_{N-1} first)
+    double d = y;
+    long long e = e0 + (long long)(N - 1) * rst;
+    x[e] = (float)((double)x[e] + d);
+    for (int l = N - 2; l >= 0; --l) {
+        e -= rst;
+        d = (double)yb[e] - (double)__ldg(fcu + lb + l) * d;
+        x[e] = (float)((double)x[e] + d);
+    }
+}
+
 // mixed path field conversion: theta = T - T_ref(z) and back
 __global__ void k_to_theta(float *__restrict__ th, const double *__restrict__ T,
                            const double *__restrict__ Tref, size_t n, int nz) {
@@ -957,6 +1035,9 @@ size_t rock2_smem(int nz) {
     const bool inc = sizeof(T) == 4;   // the float path runs the increment form
     return (size_t)nz * sizeof(T) * (inc ? 4 : 2);
 }
+
+// largest shared-memory block of the column kernel k_rock2_col
+constexpr size_t kColumnSmemMax = 200 * 1024;
 
 template <typename T>
 size_t reg_smem(int lpt, int nt = 256) { return 2 * (size_t)(nt * lpt + nt * lpt / 32) * sizeof(T); }
@@ -1016,8 +1097,29 @@ int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *
     return GW_OK;
 }
 
+// GW_MIXED_ROCK2_F64: the column kernel with double stages over the float
+// field (double tables, the double A_z T_ref source), LPT by the double rule.
+int launch_rock2_f64(gw_ctx *c, int s, const int *order, long long ncols) {
+    if (!order) order = c->d_colorder;
+    if (ncols < 0) ncols = (long long)c->nx * c->ny;
+    if (ncols == 0) return GW_OK;
+    const int lpt = rock2_lpt(c->nz, false), nt = c->rock2_nt64;
+    const unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid64 ? ncols : c->rock2_grid64);
+    const double *czm = c->c64.czm, *czp = c->c64.czp, *fr = c->d_fref64, *sc = c->d_stage;
+    switch (lpt) {
+        case 2: k_rock2_reg<float, true, 2, double><<<grid, nt, reg_smem<float>(2, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, ncols); break;
+        case 4: k_rock2_reg<float, true, 4, double><<<grid, nt, reg_smem<float>(4, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, ncols); break;
+        case 8: k_rock2_reg<float, true, 8, double><<<grid, nt, reg_smem<float>(8, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, ncols); break;
+        case 16: k_rock2_reg<float, true, 16, double><<<grid, nt, reg_smem<float>(16, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, ncols); break;
+        default: return gw_fail(GW_ERR_UNSUPPORTED, "GW_MIXED_ROCK2_F64 supports nz <= 4096");
+    }
+    GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}
+
 template <typename T>
 int launch_rock2(gw_ctx *c, int s, const int *order = nullptr, long long ncols = -1) {
+    if (sizeof(T) == 4 && (c->mixed_flags & GW_MIXED_ROCK2_F64)) return launch_rock2_f64(c, s, order, ncols);
     Bufs<T> B = bufs<T>(c);
     if (sizeof(T) == 4)
         return launch_rock2_t<float, true>(c, s, (float *)B.u, (const float *)B.ct->czm,
@@ -1034,27 +1136,29 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h, cudaStream_t st = n
     const T *cm = edir == GW_DIR_X ? B.ct->cxm : B.ct->cym;
     const T *cp = edir == GW_DIR_X ? B.ct->cxp : B.ct->cyp;
     if (c->n_pipe_chunks > 0) {
-        dim3 g(grid_for(c->nz, 128), c->n_pipe_chunks);
+        const dim3 g = chunk_grid(grid_for(c->nz, 128), c->n_pipe_chunks);
         k_pipe_sweep<T><<<g, 128, 0, st>>>(B.tp, c->d_pipepart, src, c->d_pipe_chunks,
                                                   c->d_pipe_i, c->d_pipe_j, c->d_zclass, cm, cp,
-                                                  B.Tref, c->nx, c->ny, c->nz, h, edir);
+                                                  B.Tref, c->nx, c->ny, c->nz, h, edir, c->n_pipe_chunks);
         GW_CUDA(cudaGetLastError());
     }
     dim3 gr((c->nz + 31) / 32, c->nbh);
     k_pipe_reduce<<<gr, 32 * kReduceWarps, 0, st>>>(c->d_outlet, c->d_annmean, c->d_pipepart, c->d_bchunk,
                                                     c->d_nlev, c->d_bh, c->nz);
     GW_CUDA(cudaGetLastError());
-    if (c->inlet_kind == GW_INLET_SCHEDULE) {
+    if (c->inlet_kind == GW_INLET_SCHEDULE || c->inlet_kind == GW_INLET_EXPRESSION) {
         // first advection of the step at its end time, the second half a step later
+        const bool prog = c->inlet_kind == GW_INLET_EXPRESSION;
         k_inlet_eval<<<1, 32, 0, st>>>(c->d_inlet, c->d_sched, c->n_sched, c->d_time, c->d_step_counter,
-                                       edir == GW_DIR_Y ? 0.0 : 0.5, c->nbh);
+                                       edir == GW_DIR_Y ? 0.0 : 0.5, c->nbh, c->d_prog_op, c->d_prog_arg,
+                                       prog ? c->n_prog : 0, c->d_outlet);
         GW_CUDA(cudaGetLastError());
     }
     if (c->n_pipe_chunks > 0 && c->countz > 0) {
-        dim3 ga((c->countz + 127) / 128, c->n_pipe_chunks);
+        const dim3 ga = chunk_grid((c->countz + 127) / 128, c->n_pipe_chunks);
         k_advect_c<T><<<ga, 128, 0, st>>>(B.pp, B.tp, c->d_advtab, c->d_pipe_chunks, c->d_annmean,
                                           c->d_outlet, B.Tref, c->nz, c->countz, c->inlet_kind,
-                                          c->inlet_param, c->d_inlet);
+                                          c->inlet_param, c->d_inlet, c->n_pipe_chunks);
         GW_CUDA(cudaGetLastError());
     }
     return GW_OK;
@@ -1117,6 +1221,24 @@ int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h, int mb = 
     return GW_OK;
 }
 
+// GW_MIXED_REFINE: the residual correction of the half step that left its
+// solution in x (src: the explicit sweep's input; pp: the pipe values).
+int launch_refine(gw_ctx *c, float *x, const float *src, int xlines, double h) {
+    const int nl = xlines ? c->ny : c->nx;
+    dim3 grid((c->nz + 31) / 32, (nl + 3) / 4);
+    const GwFactors<float> &f = xlines ? c->c32.fx : c->c32.fy;
+    if (xlines)
+        k_half_refine<true><<<grid, 128, 0, c->stream>>>(x, c->f_g1, src, c->f_pp, c->d_pipe_lx, c->d_zclass,
+                                                         c->c64.cxm, c->c64.cxp, c->c64.cym, c->c64.cyp, f.a,
+                                                         f.ib, f.cu, c->nx, c->ny, c->nz, c->countz, h);
+    else
+        k_half_refine<false><<<grid, 128, 0, c->stream>>>(x, c->f_g1, src, c->f_pp, c->d_pipe_ly, c->d_zclass,
+                                                          c->c64.cym, c->c64.cyp, c->c64.cxm, c->c64.cxp, f.a,
+                                                          f.ib, f.cu, c->nx, c->ny, c->nz, c->countz, h);
+    GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}
+
 template <typename T, int HW, int HR>
 cudaError_t half_attr() {
     const int sm = (int)(2 * (size_t)HR * (HW + 2) * 32 * sizeof(T));
@@ -1139,7 +1261,10 @@ template <typename T>
 int fused_step(gw_ctx *c, double dt, int s) {
     Bufs<T> B = bufs<T>(c);
     int rc;
-    if (c->overlap && rock2_lpt(c->nz, sizeof(T) == 4) > 0) {
+    // GW_MIXED_REFINE corrects each half step right after its solve, while
+    // the pipe values it used are still in pp: the in-line order
+    const bool refine = sizeof(T) == 4 && (c->mixed_flags & GW_MIXED_REFINE);
+    if (c->overlap && rock2_lpt(c->nz, sizeof(T) == 4) > 0 && !refine) {
         // The pipe passes need only the rows around the pipes: ROCK2 first
         // does the columns of rows jlo-1..jhi+1; then a second stream runs
         // the y pipe pass, the x-lines through the pipes (rows jlo..jhi) and
@@ -1166,8 +1291,10 @@ int fused_step(gw_ctx *c, double dt, int s) {
     if ((rc = launch_rock2<T>(c, s))) return rc;
     if ((rc = launch_pipe<T>(c, B.u, GW_DIR_Y, dt / 2))) return rc;
     if ((rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2))) return rc;
+    if (refine && (rc = launch_refine(c, (float *)B.temp, (const float *)B.u, 1, dt / 2))) return rc;
     if ((rc = launch_pipe<T>(c, B.temp, GW_DIR_X, dt / 2))) return rc;
     if ((rc = launch_half<T>(c, B.u, B.temp, 0, dt / 2))) return rc;
+    if (refine && (rc = launch_refine(c, (float *)B.u, (const float *)B.temp, 0, dt / 2))) return rc;
     return gw_launch_record(c, dt);
 }
 
@@ -1186,7 +1313,7 @@ int time_part(gw_ctx *c, double dt, int s, int part) {
 
 int gw_fused_supported(const gw_ctx *c) {
     const size_t need = c->precision == GW_PREC_MIXED ? rock2_smem<float>(c->nz) : rock2_smem<double>(c->nz);
-    return need <= 200 * 1024;
+    return need <= kColumnSmemMax;
 }
 
 // The shared-memory limit is an attribute of the kernel, shared by every
@@ -1201,14 +1328,18 @@ static cudaError_t occupancy(int *n, K kernel, size_t smem, int nt = 256, size_t
 }
 
 int gw_fused_prepare(gw_ctx *c) {
-    // shared-memory opt-in for the column kernel (once per context is enough)
+    // shared-memory opt-in for the column kernel.  The limit belongs to the
+    // kernel (per device), not to the context, so it is set to the largest
+    // block any context may use (kColumnSmemMax, the bound gw_fused_supported
+    // checks): a later context with fewer levels must not lower it under an
+    // earlier one.
     cudaError_t e;
     if (c->precision == GW_PREC_MIXED)
         e = cudaFuncSetAttribute(k_rock2_col<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)rock2_smem<float>(c->nz));
+                                 (int)kColumnSmemMax);
     else
         e = cudaFuncSetAttribute(k_rock2_col<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)rock2_smem<double>(c->nz));
+                                 (int)kColumnSmemMax);
     if (e != cudaSuccess) return gw_cuda_fail(e, "cudaFuncSetAttribute(k_rock2_col)");
     if ((e = (c->precision == GW_PREC_MIXED ? half_attrs<float>() : half_attrs<double>())) != cudaSuccess)
         return gw_cuda_fail(e, "cudaFuncSetAttribute(k_half_tile)");
@@ -1318,5 +1449,34 @@ int gw_fused_get_theta(gw_ctx *c, double *T_host) {
     GW_CUDA(cudaGetLastError());
     GW_CUDA(cudaMemcpyAsync(T_host, stage, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     GW_CUDA(cudaStreamSynchronize(c->stream));
+    return GW_OK;
+}
+
+int gw_fused_prepare_rock2_f64(gw_ctx *c) {
+    if (c->precision != GW_PREC_MIXED || !c->fused)
+        return gw_fail(GW_ERR_ARG, "GW_MIXED_ROCK2_F64 needs a fused GW_PREC_MIXED context");
+    const int lpt = rock2_lpt(c->nz, false);
+    if (lpt <= 0) return gw_fail(GW_ERR_UNSUPPORTED, "GW_MIXED_ROCK2_F64 supports nz <= 4096");
+    const int nt = std::min(256, ((c->nz + lpt - 1) / lpt + 31) / 32 * 32);
+    int per_sm = 0;
+    cudaError_t e;
+    switch (lpt) {
+        case 2: e = occupancy(&per_sm, k_rock2_reg<float, true, 2, double>, reg_smem<float>(2, nt), nt, reg_smem<float>(2)); break;
+        case 4: e = occupancy(&per_sm, k_rock2_reg<float, true, 4, double>, reg_smem<float>(4, nt), nt, reg_smem<float>(4)); break;
+        case 8: e = occupancy(&per_sm, k_rock2_reg<float, true, 8, double>, reg_smem<float>(8, nt), nt, reg_smem<float>(8)); break;
+        default: e = occupancy(&per_sm, k_rock2_reg<float, true, 16, double>, reg_smem<float>(16, nt), nt, reg_smem<float>(16)); break;
+    }
+    if (e != cudaSuccess) return gw_cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    int sms = 0;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device)) != cudaSuccess)
+        return gw_cuda_fail(e, "cudaDeviceGetAttribute");
+    c->rock2_nt64 = nt;
+    c->rock2_grid64 = (per_sm > 0 ? per_sm : 1) * sms;
+    return GW_OK;
+}
+
+int gw_fused_prepare_refine(gw_ctx *c) {
+    if (c->precision != GW_PREC_MIXED || !c->fused)
+        return gw_fail(GW_ERR_ARG, "GW_MIXED_REFINE needs a fused GW_PREC_MIXED context");
     return GW_OK;
 }

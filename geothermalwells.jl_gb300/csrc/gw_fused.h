@@ -6,6 +6,11 @@
 int gw_fused_supported(const gw_ctx *c);
 // Per-context kernel attributes and the column kernel's grid size.
 int gw_fused_prepare(gw_ctx *c);
+// Mixed contexts: launch shape of the ROCK2 column kernel with double stages
+// over the float field (GW_MIXED_ROCK2_F64); GW_ERR_UNSUPPORTED beyond its nz.
+int gw_fused_prepare_rock2_f64(gw_ctx *c);
+// Mixed contexts: check that GW_MIXED_REFINE can run (fused mixed step).
+int gw_fused_prepare_refine(gw_ctx *c);
 // Build the step-size dependent tables (advection departures) for dt.
 int gw_fused_set_dt(gw_ctx *c, double dt);
 // Enqueue one full step (ROCK2 columns, two half steps, record) on c->stream.

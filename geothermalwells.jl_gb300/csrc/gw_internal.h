@@ -67,6 +67,13 @@ struct gw_ctx {
     std::vector<double> sched_t, sched_T;
     double *d_sched = nullptr;
     int n_sched = 0;
+    // GW_INLET_EXPRESSION: the inlet program (gw_set_inlet_program)
+    std::vector<int> prog_op;
+    std::vector<double> prog_arg;
+    int *d_prog_op = nullptr;
+    double *d_prog_arg = nullptr;
+    int n_prog = 0;
+    bool prog_sched = false;          // the program reads the schedule
     double *d_time = nullptr;         // [2]: start time of the current gw_step call, dt
     double *d_inlet = nullptr;        // [nbh]: inlet value of the last pipe pass
     double t_now = 0.0;               // end time of the last step taken
@@ -127,9 +134,13 @@ struct gw_ctx {
     int rock2_nt = 256;               // threads per block of the ROCK2 column kernel
     int half_cfg = 0;                 // half-step tiling (gw_fused.cu kTileHW/kTileHR)
     bool fused = false;
+    int modular_reason = 0;           // GW_MODULAR_* bits when !fused
     // mixed path state (GW_PREC_MIXED): theta = T - T_ref(z) in float
     float *f_u = nullptr, *f_temp = nullptr, *f_g1 = nullptr, *f_tp = nullptr, *f_pp = nullptr;
     float *f_fref = nullptr;          // [profile][nz] A_z T_ref
+    double *d_fref64 = nullptr;       // the same in double (FP64 ROCK2 stage accumulation)
+    int mixed_flags = 0;              // GW_MIXED_* options of the mixed step
+    int rock2_nt64 = 0, rock2_grid64 = 0;   // column kernel with double stages over float storage
     double *d_Tref = nullptr;         // [nz]
     std::vector<double> Tref;         // host copy
     std::vector<double> h_czm, h_czp; // host copies of the z coefficients

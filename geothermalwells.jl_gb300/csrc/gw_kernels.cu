@@ -7,6 +7,7 @@
 // column, see gw_setup.cpp) instead of being re-evaluated per cell.
 #include <cuda_runtime.h>
 
+#include "gw_inlet.cuh"
 #include "gw_internal.h"
 
 namespace {
@@ -213,7 +214,8 @@ __global__ void __launch_bounds__(256) k_advect(double *__restrict__ utmp,
                                                 const double *__restrict__ ann_mean,
                                                 const double *__restrict__ outlet, int n_inner,
                                                 int ncol, int ny, int nz, int countz, double dt,
-                                                int inlet_kind, double inlet_param) {
+                                                int inlet_kind, double inlet_param,
+                                                const double *__restrict__ inlet_v) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)ncol * countz) return;
     const int k = (int)(e % countz);
@@ -243,7 +245,8 @@ __global__ void __launch_bounds__(256) k_advect(double *__restrict__ utmp,
     } else {
         double zd = __fma_rn(-B.v_outer, dt, z);
         if (zd <= 0.0) {
-            v = inlet_kind == GW_INLET_CONSTANT ? inlet_param : outlet[b] - inlet_param;
+            v = inlet_kind == GW_INLET_CONSTANT ? inlet_param
+              : inlet_kind == GW_INLET_EXPRESSION ? inlet_v[b] : outlet[b] - inlet_param;
         } else {
             int il, ir; double a;
             interp(gz, nz, zd, il, ir, a);
@@ -253,16 +256,31 @@ __global__ void __launch_bounds__(256) k_advect(double *__restrict__ utmp,
     utmp[(size_t)q * countz + k] = v;
 }
 
-// kernel_copy_advection! (src/solver.jl:391-396)
+// The inlet program of every borehole at time t (GW_INLET_EXPRESSION), with
+// the outlet temperatures of the advection's k_outlet.
+__global__ void k_inlet_program(double *__restrict__ inlet_v, const int *__restrict__ op,
+                                const double *__restrict__ arg, int nprog,
+                                const double *__restrict__ outlet, const double *__restrict__ sched, int ns,
+                                double t, int nbh) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbh; b += gridDim.x * blockDim.x)
+        inlet_v[b] = gw_program_eval(op, arg, nprog, outlet[b], t, b, sched, ns);
+}
+
+// kernel_copy_advection! (src/solver.jl:391-396).  A column listed for two
+// boreholes (their pipes overlap) is written by its last list entry only,
+// as a sequential run of the reference's loop leaves it (pipe_of holds the
+// last entry of every column).
 __global__ void __launch_bounds__(256) k_scatter(double *__restrict__ phi,
                                                  const double *__restrict__ utmp,
                                                  const int *__restrict__ pi,
-                                                 const int *__restrict__ pj, int ncol, int ny,
+                                                 const int *__restrict__ pj,
+                                                 const int *__restrict__ pipe_of, int ncol, int ny,
                                                  int nz, int countz) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)ncol * countz) return;
     const int k = (int)(e % countz);
     const int q = (int)(e / countz);
+    if (pipe_of[(size_t)pi[q] * ny + pj[q]] != q) return;
     phi[k + (long long)nz * (pj[q] + (long long)ny * pi[q])] = utmp[e];
 }
 
@@ -279,7 +297,7 @@ __global__ void k_record(double *__restrict__ series, double *__restrict__ energ
     if (b < nbh) {
         double to = outlet[b];
         double ti = inlet_kind == GW_INLET_CONSTANT ? inlet_param
-                  : inlet_kind == GW_INLET_SCHEDULE ? inlet_v[b] : to - inlet_param;
+                  : inlet_kind >= GW_INLET_SCHEDULE ? inlet_v[b] : to - inlet_param;
         if (n < cap) series[(size_t)n * nbh + b] = to;
         energy[b] += bh[b].mdot * c_w * (to - ti) * dt;
     }
@@ -362,6 +380,12 @@ int gw_launch_advection(gw_ctx *c, double *phi, double dt, double t) {
                                             c->d_bh, c->ny, c->nz, dt);
     GW_CUDA(cudaGetLastError());
     if (ncol == 0 || c->countz == 0) return GW_OK;
+    if (c->inlet_kind == GW_INLET_EXPRESSION) {
+        // the program reads this advection's outlet temperatures
+        k_inlet_program<<<1, 128, 0, c->stream>>>(c->d_inlet, c->d_prog_op, c->d_prog_arg, c->n_prog,
+                                                  c->d_outlet, c->d_sched, c->n_sched, t, c->nbh);
+        GW_CUDA(cudaGetLastError());
+    }
     dim3 g(grid_for(c->nz, 128), c->nbh);
     k_annulus_mean<<<g, 128, 0, c->stream>>>(c->d_annmean, phi, c->d_pipe_i, c->d_pipe_j, c->d_bh,
                                              c->ny, c->nz);
@@ -369,10 +393,10 @@ int gw_launch_advection(gw_ctx *c, double *phi, double dt, double t) {
     long long n = (long long)ncol * c->countz;
     k_advect<<<grid_for(n, 256), 256, 0, c->stream>>>(
         c->d_utmp, phi, c->d_gz, c->d_pipe_i, c->d_pipe_j, c->d_pipe_b, c->d_bh, c->d_annmean,
-        c->d_outlet, c->n_inner, ncol, c->ny, c->nz, c->countz, dt, ikind, iparam);
+        c->d_outlet, c->n_inner, ncol, c->ny, c->nz, c->countz, dt, ikind, iparam, c->d_inlet);
     GW_CUDA(cudaGetLastError());
     k_scatter<<<grid_for(n, 256), 256, 0, c->stream>>>(phi, c->d_utmp, c->d_pipe_i, c->d_pipe_j,
-                                                        ncol, c->ny, c->nz, c->countz);
+                                                        c->d_pipe_of, ncol, c->ny, c->nz, c->countz);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }

@@ -185,6 +185,10 @@ extern "C" int gw_advection_noalloc(gw_ctx *c, double *phi, double dt, double t,
     if (c->countz > GW_NOALLOC_MAX_COUNTZ)
         return gw_fail(GW_ERR_ARG, "gw_advection_noalloc: more than 12288 levels above the "
                                    "deepest borehole bottom");
+    if (c->inlet_kind == GW_INLET_EXPRESSION)
+        return gw_fail(GW_ERR_UNSUPPORTED, "gw_advection_noalloc: inlet programs run in gw_advection");
+    if (c->modular_reason & GW_MODULAR_SHARED_COLUMN)   // one block per list entry writes its column
+        return gw_fail(GW_ERR_UNSUPPORTED, "gw_advection_noalloc: a pipe column belongs to two boreholes");
     cudaError_t e = cudaSetDevice(c->device);
     if (e != cudaSuccess) return gw_cuda_fail(e, "cudaSetDevice");
     double *scratch = nullptr;

@@ -86,9 +86,10 @@ int gw_setup_host(gw_ctx *c, const gw_desc *d) {
         !d->materials.layer_depths)
         return gw_fail(GW_ERR_ARG, "materials need at least one rock layer");
     if (d->inlet_kind != GW_INLET_CONSTANT && d->inlet_kind != GW_INLET_HEAT_EXCHANGER &&
-        d->inlet_kind != GW_INLET_SCHEDULE)
-        return gw_fail(GW_ERR_UNSUPPORTED, "inlet kind must be GW_INLET_CONSTANT, GW_INLET_HEAT_EXCHANGER or "
-                                            "GW_INLET_SCHEDULE (CustomInlet closures cannot cross the C ABI)");
+        d->inlet_kind != GW_INLET_SCHEDULE && d->inlet_kind != GW_INLET_EXPRESSION)
+        return gw_fail(GW_ERR_UNSUPPORTED, "inlet kind must be GW_INLET_CONSTANT, GW_INLET_HEAT_EXCHANGER, "
+                                           "GW_INLET_SCHEDULE or GW_INLET_EXPRESSION (CustomInlet closures "
+                                           "cannot cross the C ABI)");
     if (d->precision != GW_PREC_FP64 && d->precision != GW_PREC_MIXED)
         return gw_fail(GW_ERR_ARG, "precision must be GW_PREC_FP64 or GW_PREC_MIXED");
 

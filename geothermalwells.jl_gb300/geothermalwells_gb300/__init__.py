@@ -13,7 +13,7 @@ that a simulation script uses, with ``GB300()`` as the backend value:
 All computation runs in ``lib/libgw_gb300.so`` (C ABI, ``include/gw_gb300.h``).
 """
 from .physics import (Borehole, HomogenousMaterialProperties, StratifiedMaterialProperties,
-                      ConstantInlet, HeatExchangerInlet, ScheduleInlet, CustomInlet,
+                      ConstantInlet, HeatExchangerInlet, ScheduleInlet, ExpressionInlet, CustomInlet,
                       initial_condition_thermal_gradient, get_thermal_conductivity,
                       get_volumetric_heat_capacity)
 from .grids import (compute_domain, create_uniform_gridz_with_borehole_depths,
@@ -25,7 +25,7 @@ from . import rock2
 
 __all__ = [
     "Borehole", "HomogenousMaterialProperties", "StratifiedMaterialProperties", "ConstantInlet",
-    "HeatExchangerInlet", "ScheduleInlet", "CustomInlet", "initial_condition_thermal_gradient",
+    "HeatExchangerInlet", "ScheduleInlet", "ExpressionInlet", "CustomInlet", "initial_condition_thermal_gradient",
     "get_thermal_conductivity", "get_volumetric_heat_capacity", "compute_domain",
     "create_uniform_gridz_with_borehole_depths", "create_adaptive_grid_1d", "julia_range",
     "julia_colon", "GB300", "Cache", "create_cache", "get_simulation_callback", "SavedValues",

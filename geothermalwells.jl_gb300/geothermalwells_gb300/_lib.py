@@ -13,7 +13,9 @@ LIB_PATH = os.path.join(PKG_ROOT, "lib", "libgw_gb300.so")
 
 GW_OK, GW_ERR_ARG, GW_ERR_CUDA, GW_ERR_NONFINITE, GW_ERR_TIMEOUT, GW_ERR_UNSUPPORTED = range(6)
 GW_PREC_FP64, GW_PREC_MIXED = 0, 1
-GW_INLET_CONSTANT, GW_INLET_HEAT_EXCHANGER, GW_INLET_SCHEDULE = 0, 1, 2
+GW_INLET_CONSTANT, GW_INLET_HEAT_EXCHANGER, GW_INLET_SCHEDULE, GW_INLET_EXPRESSION = 0, 1, 2, 3
+GW_MODULAR_NZ, GW_MODULAR_SHARED_COLUMN = 1, 2
+GW_MIXED_ROCK2_F64, GW_MIXED_REFINE = 1, 2
 DIRS = {"x": 0, "y": 1, "z": 2}
 
 # Every symbol include/gw_gb300.h declares, with (restype, argtypes).
@@ -57,7 +59,8 @@ class Info(ctypes.Structure):
                 ("nx", "ny", "nz", "n_boreholes", "countxy_inner", "countxy_outer", "countz",
                  "n_zclass", "n_profiles")] + \
                [("eigen_estimate", ctypes.c_double), ("device_bytes", ctypes.c_longlong),
-                ("overlap", ctypes.c_int)]
+                ("overlap", ctypes.c_int), ("fused", ctypes.c_int), ("modular_reason", ctypes.c_int),
+                ("tiling", ctypes.c_int), ("mixed_options", ctypes.c_int)]
 
 
 SIGNATURES = {
@@ -71,13 +74,19 @@ SIGNATURES = {
     "gw_init_thermal_gradient": (_i, [_vp, _d, _d]),
     "gw_rhs_diffusion_z": (_i, [_vp, _vp, _vp]),
     "gw_lincomb": (_i, [_vp, _vp, _i, _dp, ctypes.POINTER(_vp)]),
+    "gw_field_alloc": (_i, [_vp, ctypes.POINTER(_vp)]),
+    "gw_field_free": (_i, [_vp, _vp]),
+    "gw_field_copy": (_i, [_vp, _vp, _vp]),
     "gw_set_inlet_schedule": (_i, [_vp, _i, _dp, _dp]),
+    "gw_set_inlet_program": (_i, [_vp, _i, _ip, _dp]),
     "gw_diffusion_1d": (_i, [_vp, _vp, _vp, _d, _i, _i]),
     "gw_thomas": (_i, [_vp, _vp, _vp, _d, _i]),
     "gw_advection": (_i, [_vp, _vp, _d, _d]),
     "gw_adi_adv": (_i, [_vp, _vp, _vp, _d, _d]),
     "gw_step": (_i, [_vp, _d, _d, _i, _i]),
     "gw_set_overlap": (_i, [_vp, _i]),
+    "gw_set_tiling": (_i, [_vp, _i]),
+    "gw_set_mixed_options": (_i, [_vp, _i]),
     "gw_rock2_stages": (_i, [_vp, _d, _i, _ip, _ip]),
     "gw_get_outlet": (_i, [_vp, _dp]),
     "gw_get_outlet_series": (_i, [_vp, _dp, _i]),

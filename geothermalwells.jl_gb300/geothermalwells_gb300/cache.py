@@ -41,9 +41,9 @@ class Cache:
     def __init__(self, backend, gridx, gridy, gridz, materials, boreholes, inlet_model):
         if not isinstance(backend, GB300):
             raise TypeError("this package provides the GB300 backend only; got %r" % (backend,))
-        if isinstance(inlet_model, CustomInlet) or getattr(inlet_model, "kind", -1) not in (0, 1, 2):
+        if isinstance(inlet_model, CustomInlet) or getattr(inlet_model, "kind", -1) not in (0, 1, 2, 3):
             raise ValueError("CustomInlet closures cannot cross the C ABI: use ConstantInlet, "
-                             "HeatExchangerInlet or ScheduleInlet")
+                             "HeatExchangerInlet, ScheduleInlet or ExpressionInlet")
         L = _lib.load()
         self.backend = backend
         self.gridx = np.ascontiguousarray(gridx, dtype=np.float64)
@@ -64,10 +64,16 @@ class Cache:
         h = ctypes.c_void_p()
         _lib.check(L.gw_create(ctypes.byref(desc), ctypes.byref(h)))
         self.ctx = h
-        if inlet_model.kind == 2:
-            st = np.ascontiguousarray(inlet_model.times, dtype=np.float64)
-            sv = np.ascontiguousarray(inlet_model.values, dtype=np.float64)
+        sched = inlet_model if inlet_model.kind == 2 else getattr(inlet_model, "schedule", None)
+        if sched is not None:
+            st = np.ascontiguousarray(sched.times, dtype=np.float64)
+            sv = np.ascontiguousarray(sched.values, dtype=np.float64)
             _lib.check(L.gw_set_inlet_schedule(self.ctx, len(st), _lib.dptr(st), _lib.dptr(sv)))
+        if inlet_model.kind == 3:
+            ops = np.ascontiguousarray(inlet_model.ops, dtype=np.int32)
+            args = np.ascontiguousarray(inlet_model.args, dtype=np.float64)
+            _lib.check(L.gw_set_inlet_program(self.ctx, len(ops), ops.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                              _lib.dptr(args)))
         info = _lib.Info()
         _lib.check(L.gw_get_info(self.ctx, ctypes.byref(info)))
         self.countxy_inner = info.countxy_inner

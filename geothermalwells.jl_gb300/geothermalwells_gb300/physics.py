@@ -230,6 +230,112 @@ class ScheduleInlet:
         return float(np.interp(t, self.times, self.values))
 
 
+# GW_OP_* codes of include/gw_gb300.h (the inlet program of GW_INLET_EXPRESSION)
+OP_CONST, OP_TOUT, OP_TIME, OP_BH, OP_SCHED, OP_NEG = 0, 1, 2, 3, 4, 5
+OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_MIN, OP_MAX = 6, 7, 8, 9, 10, 11
+
+
+class ExpressionInlet:
+    """A ``CustomInlet`` (``src/physics.jl:315-318``) whose closure
+    ``(bh, T_outlet, t) -> T_in`` is arithmetic, written as an expression
+    string over ``T_out`` (the borehole's outlet temperature,
+    ``T_outlet[bh]``), ``t``, ``bh`` (0-based), numbers, ``+ - * /``,
+    unary ``-``, ``min(a, b)``, ``max(a, b)`` and ``sched(x)`` (the optional
+    piecewise-linear ``schedule=(times, values)`` at ``x``).  For example a
+    heat pump that takes ``dT(t)`` out of the outlet but never cools the inlet
+    below 5 degrees: ``ExpressionInlet("max(5.0, T_out - sched(t))",
+    schedule=([0, 3600], [3.0, 6.0]))``.
+
+    It is compiled to the postfix program of ``GW_INLET_EXPRESSION``, which the
+    GPU evaluates per borehole where the reference calls the inlet model
+    (``src/solver.jl:349-350``), each operation one correctly rounded double
+    operation; calling the object evaluates the same program on the host."""
+    kind = 3
+
+    def __init__(self, expr, schedule=None):
+        import ast
+        self.expr = str(expr)
+        self.schedule = None
+        if schedule is not None:
+            self.schedule = ScheduleInlet(*schedule)
+        ops, args = [], []
+
+        def emit(op, a=0.0):
+            ops.append(op)
+            args.append(float(a))
+
+        bin_ops = {ast.Add: OP_ADD, ast.Sub: OP_SUB, ast.Mult: OP_MUL, ast.Div: OP_DIV}
+        names = {"T_out": OP_TOUT, "t": OP_TIME, "bh": OP_BH}
+
+        def walk(n):
+            if isinstance(n, ast.Expression):
+                return walk(n.body)
+            if isinstance(n, ast.Constant) and isinstance(n.value, (int, float)) and not isinstance(n.value, bool):
+                return emit(OP_CONST, n.value)
+            if isinstance(n, ast.Name) and n.id in names:
+                return emit(names[n.id])
+            if isinstance(n, ast.UnaryOp) and isinstance(n.op, (ast.USub, ast.UAdd)):
+                walk(n.operand)
+                if isinstance(n.op, ast.USub):
+                    emit(OP_NEG)
+                return None
+            if isinstance(n, ast.BinOp) and type(n.op) in bin_ops:
+                walk(n.left)
+                walk(n.right)
+                return emit(bin_ops[type(n.op)])
+            if isinstance(n, ast.Call) and isinstance(n.func, ast.Name) and not n.keywords:
+                f, a = n.func.id, n.args
+                if f in ("min", "max") and len(a) >= 2:
+                    walk(a[0])
+                    for x in a[1:]:
+                        walk(x)
+                        emit(OP_MIN if f == "min" else OP_MAX)
+                    return None
+                if f == "sched" and len(a) == 1:
+                    if self.schedule is None:
+                        raise ValueError("sched(...) needs ExpressionInlet(..., schedule=(times, values))")
+                    walk(a[0])
+                    return emit(OP_SCHED)
+            raise ValueError("unsupported element in the inlet expression %r: %s"
+                             % (self.expr, ast.dump(n)))
+
+        walk(ast.parse(self.expr, mode="eval"))
+        depth, top = 0, 0
+        for o in ops:
+            depth += 1 if o <= OP_BH else (0 if o <= OP_NEG else -1)
+            top = max(top, depth)
+        if len(ops) > 64 or top > 16:
+            raise ValueError("inlet expression too long (at most 64 operations, stack depth 16)")
+        self.ops = tuple(ops)
+        self.args = tuple(args)
+
+    @property
+    def param(self):
+        return 0.0
+
+    def __call__(self, bh_idx, T_outlet_values, t):
+        st = []
+        for o, a in zip(self.ops, self.args):
+            if o == OP_CONST:
+                st.append(a)
+            elif o == OP_TOUT:
+                st.append(float(T_outlet_values[bh_idx]))
+            elif o == OP_TIME:
+                st.append(float(t))
+            elif o == OP_BH:
+                st.append(float(bh_idx))
+            elif o == OP_SCHED:
+                st[-1] = self.schedule(bh_idx, T_outlet_values, st[-1])
+            elif o == OP_NEG:
+                st[-1] = -st[-1]
+            else:
+                b = st.pop()
+                x = st[-1]
+                st[-1] = {OP_ADD: x + b, OP_SUB: x - b, OP_MUL: x * b, OP_DIV: x / b if b else np.inf,
+                          OP_MIN: min(x, b), OP_MAX: max(x, b)}[o]
+        return st[0]
+
+
 class CustomInlet:
     """``src/physics.jl:315-318``: an arbitrary host function.  The GB300
     backend evaluates the inlet on the device, so a Python callable cannot

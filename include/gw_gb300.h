@@ -45,6 +45,10 @@ extern "C" {
 #define GW_INLET_SCHEDULE 2        /* a CustomInlet (src/physics.jl:315-318) of the form
                                       (bh, T_outlet, t) -> T_in(t): a piecewise-linear
                                       schedule, set with gw_set_inlet_schedule */
+#define GW_INLET_EXPRESSION 3      /* a CustomInlet whose closure is arithmetic in the
+                                      borehole's outlet temperature, t, the borehole index
+                                      and the schedule: a program set with
+                                      gw_set_inlet_program */
 
 #define GW_DIR_X 0
 #define GW_DIR_Y 1
@@ -89,7 +93,18 @@ typedef struct gw_info_t {
     double eigen_estimate;           /* src/solver.jl:474-488 */
     long long device_bytes;          /* device memory held by the context */
     int overlap;                     /* pipe passes on a second stream (gw_set_overlap) */
+    int fused;                       /* 1: gw_step runs the fused graph-captured step;
+                                        0: the modular reference-shaped kernels (several
+                                        times slower; GW_PREC_FP64 only) */
+    int modular_reason;              /* why fused == 0: GW_MODULAR_* bits, 0 when fused */
+    int tiling;                      /* half-step kernel (gw_set_tiling) */
+    int mixed_options;               /* GW_MIXED_* flags (gw_set_mixed_options) */
 } gw_info_t;
+
+/* gw_info_t.modular_reason bits */
+#define GW_MODULAR_NZ 1               /* nz beyond the fused ROCK2 column kernels' shared memory */
+#define GW_MODULAR_SHARED_COLUMN 2    /* a pipe column belongs to two boreholes (the later one
+                                         overrides, src/physics.jl:204-229) */
 
 typedef struct gw_ctx gw_ctx;
 
@@ -108,6 +123,21 @@ int gw_get_field(gw_ctx *ctx, double *T);
 /* initial_condition_thermal_gradient (src/physics.jl:333-348) into u. */
 int gw_init_thermal_gradient(gw_ctx *ctx, double T_surface, double gradient);
 
+/* ---- device fields for hosts without a CUDA binding ----
+ * No single counterpart in the reference, where KernelAbstractions'
+ * `allocate(backend, ...)` / `adapt(backend, ...)` make the device arrays
+ * (src/cache.jl:41, src/physics.jl:333-348).  A host language that binds only
+ * this library (e.g. Julia through ccall, without CUDA.jl) allocates the
+ * fields of the fine-grained entry points here.  Each field holds the
+ * context's N = nx*ny*nz doubles on its device and is owned by the caller;
+ * free it with gw_field_free before gw_destroy. */
+/* A new N-cell double field on the context's device, set to zero. */
+int gw_field_alloc(gw_ctx *ctx, double **field_dev);
+int gw_field_free(gw_ctx *ctx, double *field_dev);
+/* Copy N doubles between host and device memory, or within either (the
+ * direction follows from the pointers); returns when the copy is done. */
+int gw_field_copy(gw_ctx *ctx, double *dst, const double *src);
+
 /* ---- fine-grained entry points on caller-owned device fields (double) ---- */
 /* rhs_diffusion_z!(dphi, phi, cache, t), src/solver.jl:23-31 */
 int gw_rhs_diffusion_z(gw_ctx *ctx, double *dphi_dev, const double *phi_dev);
@@ -122,12 +152,37 @@ int gw_advection(gw_ctx *ctx, double *phi_dev, double dt, double t);
  * temp = integrator.uprev (clobbered), t = integrator.t, dt = t - tprev. */
 int gw_adi_adv(gw_ctx *ctx, double *u_dev, double *temp_dev, double t, double dt);
 
-/* Inlet temperature schedule of a GW_INLET_SCHEDULE context: T_in(t) linear
+/* Inlet temperature schedule of a GW_INLET_SCHEDULE context (or the schedule
+ * a GW_INLET_EXPRESSION program reads with GW_OP_SCHED): T_in(t) linear
  * between the n points (times strictly increasing), held constant before the
  * first and after the last.  Evaluated where the reference calls
  * inlet_model(bh, T_outlet, t) (src/solver.jl:349-350): at the step's end time
  * in the first advection and half a step later in the second. */
 int gw_set_inlet_schedule(gw_ctx *ctx, int n, const double *times, const double *values);
+
+/* Inlet program of a GW_INLET_EXPRESSION context: a postfix sequence of n
+ * operations (n <= GW_PROGRAM_MAX) evaluated for every borehole wherever the
+ * reference calls inlet_model(bh, T_outlet, t) (src/solver.jl:349-350), each
+ * operation one correctly rounded double operation.  Operands go on a stack
+ * (depth <= 16); the program must leave exactly one value, the inlet
+ * temperature.  GW_OP_SCHED reads the context's schedule
+ * (gw_set_inlet_schedule, which GW_INLET_EXPRESSION contexts also take).
+ * Example, T_in = max(5, T_out - dT(t)):
+ *   CONST 5, TOUT, TIME, SCHED, SUB, MAX. */
+#define GW_PROGRAM_MAX 64
+#define GW_OP_CONST 0   /* push args[i] */
+#define GW_OP_TOUT 1    /* push T_outlet of the borehole (cache.T_outlet[bh]) */
+#define GW_OP_TIME 2    /* push t */
+#define GW_OP_BH 3      /* push the borehole index (0-based) */
+#define GW_OP_SCHED 4   /* x -> schedule(x) */
+#define GW_OP_NEG 5     /* x -> -x */
+#define GW_OP_ADD 6     /* a b -> a + b */
+#define GW_OP_SUB 7     /* a b -> a - b */
+#define GW_OP_MUL 8     /* a b -> a * b */
+#define GW_OP_DIV 9     /* a b -> a / b */
+#define GW_OP_MIN 10    /* a b -> min(a, b) */
+#define GW_OP_MAX 11    /* a b -> max(a, b) */
+int gw_set_inlet_program(gw_ctx *ctx, int n, const int *ops, const double *args);
 
 /* dst = sum_i coeffs[i] * srcs[i] over the context's N = nx*ny*nz cells, n <= 8
  * device fields (dst may be one of them).  The vector updates an ODE
@@ -150,6 +205,22 @@ int gw_step(gw_ctx *ctx, double t0, double dt, int nsteps, int max_stages);
  * (on = 0).  Both give bitwise identical results.  gw_get_info reports the
  * setting (overlap). */
 int gw_set_overlap(gw_ctx *ctx, int on);
+/* Options of the mixed step (GW_PREC_MIXED contexts; 0 = the default form):
+ *  GW_MIXED_ROCK2_F64  ROCK2 stages accumulated in double over the float
+ *                      field, rounded into it once per step (the FP64 pipe
+ *                      makes the column kernel several times slower);
+ *  GW_MIXED_REFINE     after each float line solve, the residual of the
+ *                      half step's equation in double and one correction
+ *                      solve (a second pass over the field per half step).
+ * No counterpart in the reference, which runs in one precision. */
+#define GW_MIXED_ROCK2_F64 1
+#define GW_MIXED_REFINE 2
+int gw_set_mixed_options(gw_ctx *ctx, int flags);
+
+/* Half-step kernel of this context (0 .. GW_TILINGS-1, see GW_TILINGS); all
+ * give the same field bitwise except the segmented tiling 6.  gw_create picks
+ * the default; gw_get_info reports the setting (tiling). */
+int gw_set_tiling(gw_ctx *ctx, int tiling);
 /* Stage count gw_step uses for dt (and whether its interval covers dt*lambda). */
 int gw_rock2_stages(gw_ctx *ctx, double dt, int max_stages, int *stages, int *covered);
 
@@ -224,9 +295,11 @@ int gw_tridiag_batch(int precision, int ngroups, const long long *group_off, con
  *
  * Who needs it: a host integrator that owns every device buffer itself --
  * e.g. a Julia caller whose arrays come from its own pool allocator and must
- * keep the device footprint fixed after set-up, or a caller recording the
- * step into its own CUDA graph, where cudaMalloc is not allowed.  This entry
- * point calls no cudaMalloc, cudaFree or allocating library routine.
+ * keep the device footprint fixed after set-up, or a process that reserves
+ * its share of a GPU shared with other jobs once at start-up and may not
+ * grow it during the run.  This entry point calls no cudaMalloc, cudaFree or
+ * allocating library routine, and waits for its own work on the context's
+ * stream before it returns.
  *
  * Its scratch (outlet means and per-level annulus means) lives in one
  * file-scope device array of 65536 doubles (512 KiB) that every GPU which

@@ -45,6 +45,10 @@ typedef struct {
     /* advection index lists, cache.jl:9-44 (0-based i, j, bh) */
     int n_inner, n_outer, countz;
     int *idx;            /* 3 * (n_inner + n_outer): inner list then outer list */
+    unsigned char *last; /* 1 where entry q is the last one of its (i, j) column */
+    int prog_n;          /* kind 3: inlet program, postfix GW_OP_* codes and constants */
+    int *prog_op;
+    double *prog_arg;
     double *u_tmp;       /* (n_inner + n_outer) x countz, ij fastest (cache.jl:41) */
     double *T_outlet;    /* nbh */
     long *T_outlet_counter;
@@ -110,8 +114,8 @@ void ogw_destroy(void *h) {
     if (!c) return;
     free(c->gx); free(c->gy); free(c->gz); free(c->bh);
     free(c->k_layers); free(c->rhoc_layers); free(c->depths);
-    free(c->idx); free(c->u_tmp); free(c->T_outlet); free(c->T_outlet_counter);
-    free(c->sched_t); free(c->sched_T);
+    free(c->idx); free(c->last); free(c->u_tmp); free(c->T_outlet); free(c->T_outlet_counter);
+    free(c->sched_t); free(c->sched_T); free(c->prog_op); free(c->prog_arg);
     free(c);
 }
 
@@ -184,6 +188,19 @@ void *ogw_create(int nx, int ny, int nz, const double *gx, const double *gy, con
     memcpy(c->idx, inner, sizeof(int) * 3 * ni);
     memcpy(c->idx + 3 * ni, outer, sizeof(int) * 3 * no);
     free(inner); free(outer);
+    /* boreholes whose pipes share a column list it more than once; the
+     * reference's copy-back (solver.jl:391-396) then writes it from several
+     * work items in parallel.  Restated deterministically, as a sequential
+     * run of that loop leaves it: the later list entry wins. */
+    c->last = (unsigned char *)malloc((size_t)(ni + no + 1));
+    {
+        int *lastq = (int *)malloc(sizeof(int) * (size_t)nx * ny);
+        for (size_t e = 0; e < (size_t)nx * ny; ++e) lastq[e] = -1;
+        for (int q = 0; q < ni + no; ++q) lastq[(size_t)c->idx[3 * q] * ny + c->idx[3 * q + 1]] = q;
+        for (int q = 0; q < ni + no; ++q)
+            c->last[q] = lastq[(size_t)c->idx[3 * q] * ny + c->idx[3 * q + 1]] == q;
+        free(lastq);
+    }
     double max_h = -INFINITY;
     for (int b = 0; b < nbh; ++b) if (c->bh[b].h > max_h) max_h = c->bh[b].h;
     int cz = 0;
@@ -369,9 +386,60 @@ static double schedule_at(const octx_t *c, double t) {
     return fma(a, c->sched_T[hi] - c->sched_T[lo], c->sched_T[lo]);
 }
 
+/* kind 3: a CustomInlet whose closure (bh, T_outlet, t) -> T_in is given as a
+ * postfix program: 0 push constant, 1 push T_outlet[bh], 2 push t, 3 push bh,
+ * 4 x -> schedule(x), 5 x -> -x, 6..11 a b -> a+b, a-b, a*b, a/b, fmin, fmax
+ * (the codes of include/gw_gb300.h's GW_OP_*).  The program is checked when it
+ * is set, so the stack stays within its 16 slots. */
+static double program_at(const octx_t *c, int bh, double t) {
+    double st[16];
+    int sp = 0;
+    for (int i = 0; i < c->prog_n; ++i) {
+        switch (c->prog_op[i]) {
+            case 0: st[sp++] = c->prog_arg[i]; break;
+            case 1: st[sp++] = c->T_outlet[bh]; break;
+            case 2: st[sp++] = t; break;
+            case 3: st[sp++] = (double)bh; break;
+            case 4: st[sp - 1] = schedule_at(c, st[sp - 1]); break;
+            case 5: st[sp - 1] = -st[sp - 1]; break;
+            case 6: --sp; st[sp - 1] = st[sp - 1] + st[sp]; break;
+            case 7: --sp; st[sp - 1] = st[sp - 1] - st[sp]; break;
+            case 8: --sp; st[sp - 1] = st[sp - 1] * st[sp]; break;
+            case 9: --sp; st[sp - 1] = st[sp - 1] / st[sp]; break;
+            case 10: --sp; st[sp - 1] = fmin(st[sp - 1], st[sp]); break;
+            case 11: --sp; st[sp - 1] = fmax(st[sp - 1], st[sp]); break;
+            default: break;
+        }
+    }
+    return st[0];
+}
+
 static double inlet_value(const octx_t *c, int bh, double t) {
     if (c->inlet_kind == 2) return schedule_at(c, t);
+    if (c->inlet_kind == 3) return program_at(c, bh, t);
     return c->inlet_kind == 0 ? c->inlet_param : c->T_outlet[bh] - c->inlet_param;
+}
+
+/* Returns 0, or -1 if the program is malformed (the library's own checks). */
+int ogw_set_program(void *h, int n, const int *op, const double *arg) {
+    octx_t *c = (octx_t *)h;
+    int depth = 0;
+    if (n < 1 || n > 64) return -1;
+    for (int i = 0; i < n; ++i) {
+        if (op[i] < 0 || op[i] > 11) return -1;
+        if (op[i] <= 3) ++depth;
+        else if (op[i] <= 5) { if (depth < 1) return -1; }
+        else { if (depth < 2) return -1; --depth; }
+        if (depth > 16) return -1;
+    }
+    if (depth != 1) return -1;
+    free(c->prog_op); free(c->prog_arg);
+    c->prog_op = (int *)malloc(sizeof(int) * n);
+    c->prog_arg = (double *)malloc(sizeof(double) * n);
+    memcpy(c->prog_op, op, sizeof(int) * n);
+    memcpy(c->prog_arg, arg, sizeof(double) * n);
+    c->prog_n = n;
+    return 0;
 }
 
 void ogw_set_schedule(void *h, int n, const double *t, const double *T) {
@@ -445,6 +513,7 @@ void ogw_advection(void *h, double *phi, double dt, double t) {
     /* solver.jl:391-396 */
 #pragma omp parallel for schedule(static)
     for (int q = 0; q < ncol; ++q) {
+        if (!c->last[q]) continue;
         int i = c->idx[3 * q], j = c->idx[3 * q + 1];
         for (int k = 0; k < cz; ++k) phi[IDX(c, k, j, i)] = c->u_tmp[(size_t)q + (size_t)ncol * k];
     }

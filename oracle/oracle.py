@@ -54,6 +54,8 @@ def lib():
         _lp = ctypes.POINTER(ctypes.c_longlong)
         L.ogw_tridiag_batch.argtypes = [ctypes.c_int, _lp, _ip, _dp, _dp, _dp, _dp, _dp]
         L.ogw_set_schedule.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
+        L.ogw_set_program.restype = ctypes.c_int
+        L.ogw_set_program.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp]
         L.ogw_set_threads.restype = ctypes.c_int
         L.ogw_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -83,17 +85,24 @@ class Oracle:
         bh = np.array([b.args() for b in boreholes], dtype=np.float64).ravel()
         kl, rl, dl = (np.array(v, dtype=np.float64) for v in materials.layers())
         m8 = np.array(materials.fixed(), dtype=np.float64)
-        if inlet_model.kind not in (0, 1, 2):
-            raise ValueError("oracle supports ConstantInlet, HeatExchangerInlet and ScheduleInlet")
+        if inlet_model.kind not in (0, 1, 2, 3):
+            raise ValueError("oracle supports ConstantInlet, HeatExchangerInlet, ScheduleInlet and "
+                             "ExpressionInlet")
         self.nbh = len(boreholes)
         self._keep = (bh, kl, rl, dl, m8)
         self.h = L.ogw_create(self.nx, self.ny, self.nz, _p(self.gx), _p(self.gy), _p(self.gz),
                               self.nbh, _p(bh), len(kl), _p(kl), _p(rl), _p(dl), _p(m8),
                               inlet_model.kind, inlet_model.param)
-        if inlet_model.kind == 2:
-            st = np.ascontiguousarray(inlet_model.times, dtype=np.float64)
-            sv = np.ascontiguousarray(inlet_model.values, dtype=np.float64)
+        sched = inlet_model if inlet_model.kind == 2 else getattr(inlet_model, "schedule", None)
+        if sched is not None:
+            st = np.ascontiguousarray(sched.times, dtype=np.float64)
+            sv = np.ascontiguousarray(sched.values, dtype=np.float64)
             L.ogw_set_schedule(self.h, len(st), _p(st), _p(sv))
+        if inlet_model.kind == 3:
+            ops = np.ascontiguousarray(inlet_model.ops, dtype=np.int32)
+            args = np.ascontiguousarray(inlet_model.args, dtype=np.float64)
+            if L.ogw_set_program(self.h, len(ops), ops.ctypes.data_as(_ip), _p(args)) != 0:
+                raise ValueError("malformed inlet program")
         self.temp = np.zeros(self.shape, order="F")
         self._work = None
 
