@@ -433,6 +433,11 @@ int gw_destroy(gw_ctx *c) {
     if (c->ev_a) cudaEventDestroy(c->ev_a);
     if (c->ev_px) cudaEventDestroy(c->ev_px);
     if (c->stream2) { cudaStreamSynchronize(c->stream2); cudaStreamDestroy(c->stream2); }
+    if (c->snap_stream) { cudaStreamSynchronize(c->snap_stream); cudaStreamDestroy(c->snap_stream); }
+    for (int b = 0; b < 2; ++b) {
+        if (c->ev_conv[b]) cudaEventDestroy(c->ev_conv[b]);
+        if (c->ev_copy[b]) cudaEventDestroy(c->ev_copy[b]);
+    }
     gw_adjoint_release(c);
     for (void *p : c->allocations) if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -802,6 +807,66 @@ int gw_profile_kernels(gw_ctx *c, double dt, int reps, double *ms_out) {
     }
     GW_CUDA(cudaMemcpyAsync(u, bak, bytes, cudaMemcpyDeviceToDevice, c->stream));
     return sync(c);
+}
+
+int gw_snapshot_host_alloc(gw_ctx *c, float **host) {
+    if (!c || !host) return gw_fail(GW_ERR_ARG, "NULL argument");
+    *host = nullptr;
+    int rc = set_device(c);
+    if (rc) return rc;
+    GW_CUDA(cudaMallocHost((void **)host, ncell(c) * sizeof(float)));
+    return GW_OK;
+}
+
+int gw_snapshot_host_free(gw_ctx *c, float *host) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
+    if (!host) return GW_OK;
+    int rc = set_device(c);
+    if (rc || (rc = gw_snapshot_wait(c))) return rc;
+    GW_CUDA(cudaFreeHost(host));
+    return GW_OK;
+}
+
+int gw_snapshot(gw_ctx *c, float *host_dst) {
+    if (!c || !host_dst) return gw_fail(GW_ERR_ARG, "NULL argument");
+    int rc = set_device(c);
+    if (rc) return rc;
+    const size_t bytes = ncell(c) * sizeof(float);
+    if (!c->snap_stream) {
+        GW_CUDA(cudaStreamCreateWithFlags(&c->snap_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            GW_CUDA(cudaEventCreateWithFlags(&c->ev_conv[b], cudaEventDisableTiming));
+            GW_CUDA(cudaEventCreateWithFlags(&c->ev_copy[b], cudaEventDisableTiming));
+            if ((rc = dalloc(c, &c->d_snap[b], ncell(c)))) return rc;
+        }
+    }
+    const int b = c->snap_next;
+    // the staging buffer may still be on its way to the host: the device waits
+    if (c->snap_pending[b]) GW_CUDA(cudaStreamWaitEvent(c->stream, c->ev_copy[b], 0));
+    if ((rc = gw_launch_snapshot(c, c->d_snap[b]))) return rc;
+    GW_CUDA(cudaEventRecord(c->ev_conv[b], c->stream));
+    GW_CUDA(cudaStreamWaitEvent(c->snap_stream, c->ev_conv[b], 0));
+    GW_CUDA(cudaMemcpyAsync(host_dst, c->d_snap[b], bytes, cudaMemcpyDeviceToHost, c->snap_stream));
+    GW_CUDA(cudaEventRecord(c->ev_copy[b], c->snap_stream));
+    c->snap_pending[b] = true;
+    c->snap_next = b ^ 1;
+    // the conversion (a fraction of a step) has finished when the call
+    // returns, so the caller may change the state or T_ref at once; only the
+    // copy to the host runs on
+    GW_CUDA(cudaEventSynchronize(c->ev_conv[b]));
+    return GW_OK;
+}
+
+int gw_snapshot_wait(gw_ctx *c) {
+    if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
+    int rc = set_device(c);
+    if (rc) return rc;
+    for (int b = 0; b < 2; ++b)
+        if (c->snap_pending[b]) {
+            GW_CUDA(cudaEventSynchronize(c->ev_copy[b]));
+            c->snap_pending[b] = false;
+        }
+    return GW_OK;
 }
 
 int gw_get_outlet(gw_ctx *c, double *T) {

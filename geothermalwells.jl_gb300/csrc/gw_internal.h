@@ -147,6 +147,13 @@ struct gw_ctx {
 
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_step_ms = 0.0;
+    // asynchronous snapshots (gw_snapshot): two float staging buffers, the
+    // copy stream and per-buffer events (converted, copied)
+    float *d_snap[2] = {nullptr, nullptr};
+    cudaStream_t snap_stream = nullptr;
+    cudaEvent_t ev_conv[2] = {nullptr, nullptr}, ev_copy[2] = {nullptr, nullptr};
+    bool snap_pending[2] = {false, false};
+    int snap_next = 0;
     // graph cache for gw_step
     cudaGraphExec_t graph = nullptr;
     double graph_dt = -1.0;
@@ -203,6 +210,8 @@ int gw_launch_check_finite(gw_ctx *c, const double *u, size_t n);
 int gw_launch_lincomb(gw_ctx *c, double *dst, int n, const double *w, const double *const *src);
 // u = col[k] in every column (col: nz device doubles)
 int gw_launch_broadcast_column(gw_ctx *c, double *u, const double *col);
+// dst = float(T) of the context's state (theta + T_ref in the mixed path)
+int gw_launch_snapshot(gw_ctx *c, float *dst);
 int gw_ensure_factors(gw_ctx *c, double h);
 int gw_set_step_time(gw_ctx *c, double t0, double dt);
 int gw_prepare_step(gw_ctx *c, double dt, int s, int nsteps);

@@ -420,6 +420,28 @@ int gw_launch_lincomb(gw_ctx *c, double *dst, int n, const double *w, const doub
     return GW_OK;
 }
 
+// Snapshot conversion: float temperatures of the state, rounded once from
+// the double value (theta + T_ref in the mixed path).
+__global__ void k_snapshot_f64(float *__restrict__ dst, const double *__restrict__ u, size_t n) {
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        dst[q] = (float)u[q];
+}
+__global__ void k_snapshot_theta(float *__restrict__ dst, const float *__restrict__ th,
+                                 const double *__restrict__ Tref, size_t n, int nz) {
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        dst[q] = (float)((double)th[q] + Tref[q % nz]);
+}
+
+int gw_launch_snapshot(gw_ctx *c, float *dst) {
+    const size_t N = (size_t)c->nx * c->ny * c->nz;
+    if (c->precision == GW_PREC_MIXED)
+        k_snapshot_theta<<<152 * 8, 256, 0, c->stream>>>(dst, c->f_u, c->d_Tref, N, c->nz);
+    else
+        k_snapshot_f64<<<152 * 8, 256, 0, c->stream>>>(dst, c->d_u, N);
+    GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}
+
 int gw_launch_broadcast_column(gw_ctx *c, double *u, const double *col) {
     const size_t N = (size_t)c->nx * c->ny * c->nz;
     k_broadcast_column<<<152 * 8, 256, 0, c->stream>>>(u, col, N, c->nz);

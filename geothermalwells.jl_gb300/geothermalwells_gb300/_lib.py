@@ -88,6 +88,10 @@ SIGNATURES = {
     "gw_set_tiling": (_i, [_vp, _i]),
     "gw_set_mixed_options": (_i, [_vp, _i]),
     "gw_rock2_stages": (_i, [_vp, _d, _i, _ip, _ip]),
+    "gw_snapshot_host_alloc": (_i, [_vp, ctypes.POINTER(_vp)]),
+    "gw_snapshot_host_free": (_i, [_vp, _vp]),
+    "gw_snapshot": (_i, [_vp, _vp]),
+    "gw_snapshot_wait": (_i, [_vp]),
     "gw_get_outlet": (_i, [_vp, _dp]),
     "gw_get_outlet_series": (_i, [_vp, _dp, _i]),
     "gw_get_energy": (_i, [_vp, _dp]),

@@ -9,6 +9,7 @@ for driving the hot path from an external integrator.
 :func:`solve` is the fused path: it keeps the state on the device and runs
 ROCK2 + ADI + advection steps as one captured CUDA graph per step.
 """
+import ctypes
 import math
 
 import numpy as np
@@ -162,8 +163,19 @@ def solve(prob, alg, *, dt, adaptive=False, save_everystep=False, callback=None,
         stops |= set(save_steps)
         if callback.print_every_n > 0:
             stops |= set(range(callback.print_every_n, nsteps + 1, callback.print_every_n))
+    # saved fields: float snapshots converted on the device and copied to
+    # pinned host buffers on a second stream while the next steps run; they
+    # are handed to the callback once every copy has landed
+    snaps = []
+
+    def snapshot(ts):
+        ptr = ctypes.c_void_p()
+        _lib.check(L.gw_snapshot_host_alloc(cache.ctx, ctypes.byref(ptr)))
+        snaps.append((ts, ptr))
+        _lib.check(L.gw_snapshot(cache.ctx, ptr))
+
     if 0 in save_steps:
-        callback.save(save_steps[0], cache.get_field())
+        snapshot(save_steps[0])
     series = []
     done = 0
     for stop in sorted(x for x in stops if x > 0):
@@ -178,7 +190,13 @@ def solve(prob, alg, *, dt, adaptive=False, save_everystep=False, callback=None,
             if callback.print_every_n > 0 and done % callback.print_every_n == 0:
                 callback.print_step(done, t)
             if done in save_steps:
-                callback.save(save_steps[done], cache.get_field())
+                snapshot(save_steps[done])
+    if snaps:
+        _lib.check(L.gw_snapshot_wait(cache.ctx))
+        for ts, ptr in snaps:
+            host = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_float)), shape=(cache.N,))
+            callback.save(ts, host.reshape(cache.shape, order="F").copy(order="F"))
+            _lib.check(L.gw_snapshot_host_free(cache.ctx, ptr))
     energy = np.zeros(cache.N_bh)
     _lib.check(L.gw_get_energy(cache.ctx, _lib.dptr(energy)))
     outlet = np.concatenate(series) if series else np.zeros((0, cache.N_bh))

@@ -224,6 +224,23 @@ int gw_set_tiling(gw_ctx *ctx, int tiling);
 /* Stage count gw_step uses for dt (and whether its interval covers dt*lambda). */
 int gw_rock2_stages(gw_ctx *ctx, double dt, int max_stages, int *stages, int *covered);
 
+/* ---- snapshots: asynchronous float copies of the state ----
+ * save_and_print_callback's SavingCallback (src/cache.jl:132-184) copies u to
+ * the host at every saveat time and keeps it as Float32.  gw_snapshot
+ * converts the context's u to float temperatures on the device and starts
+ * the copy into host_dst (N floats, (k, j, i) order) on a second stream; it
+ * returns once the conversion is done (a fraction of a step) without waiting
+ * for the copy, which overlaps the gw_step calls that follow.  host_dst must
+ * stay untouched until gw_snapshot_wait returns.  Two device staging buffers
+ * alternate; a third snapshot started before the first copy has landed makes
+ * the device (not the host) wait for it.  The overlap needs pinned host
+ * memory (gw_snapshot_host_alloc); with pageable memory the copy completes
+ * before gw_snapshot returns. */
+int gw_snapshot_host_alloc(gw_ctx *ctx, float **host);
+int gw_snapshot_host_free(gw_ctx *ctx, float *host);
+int gw_snapshot(gw_ctx *ctx, float *host_dst);
+int gw_snapshot_wait(gw_ctx *ctx);
+
 /* cache.T_outlet after the last advection (src/solver.jl:253-257). */
 int gw_get_outlet(gw_ctx *ctx, double *T_outlet);
 /* Outlet temperature after each of the last gw_step call's steps, nsteps x nbh. */
