@@ -1,6 +1,8 @@
 // gw_api.cu -- the extern "C" entry points declared in include/gw_gb300.h.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -163,6 +165,12 @@ int gw_cuda_fail(cudaError_t e, const char *what) {
     return GW_ERR_CUDA;
 }
 
+#ifndef GW_DEBUG
+void gw_debug_register(int, const void *, size_t) {}
+void gw_debug_unregister(int, const void *) {}
+int gw_debug_status(int) { return GW_OK; }
+#endif
+
 // Recompute the Thomas factors of (I - h A_x) and (I - h A_y) when h changes
 // (in double; the mixed path gets them rounded to float).
 // Start time and step size of the steps about to run, read on the device by
@@ -190,6 +198,13 @@ double gw_schedule_at(const gw_ctx *c, double t) {
 
 int gw_ensure_factors(gw_ctx *c, double h) {
     if (h == c->factors_h) return GW_OK;
+    if (!c->host_setup) {
+        GW_CUDA(cudaStreamSynchronize(c->stream));
+        int rc = gw_factors_device(c, h);
+        if (rc) return rc;
+        c->factors_h = h;
+        return GW_OK;
+    }
     std::vector<double> cxm, cxp, cym, cyp, czm, czp;
     gw_build_coefs(c, cxm, cxp, cym, cyp, czm, czp);
     std::vector<double> a, ib, cu;
@@ -254,6 +269,10 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
     if (!out) return gw_fail(GW_ERR_ARG, "out is NULL");
     *out = nullptr;
     gw_ctx *c = new gw_ctx();
+    // tables on the GPU unless GW_HOST_SETUP is set (the host builders give
+    // the same values bitwise; tests compare the two paths)
+    const char *hs = std::getenv("GW_HOST_SETUP");
+    c->host_setup = hs && *hs && *hs != '0';
     int rc = gw_setup_host(c, desc);
     if (rc) { delete c; return rc; }
     if (c->nbh > 1024) { delete c; return gw_fail(GW_ERR_ARG, "at most 1024 boreholes"); }
@@ -266,18 +285,31 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         return fail(gw_cuda_fail(e, "cudaEventCreate"));
 
     // material model as coefficient tables (double always: the fine-grained
-    // entry points work on double fields)
-    std::vector<double> cxm, cxp, cym, cyp, czm, czp;
-    gw_build_coefs(c, cxm, cxp, cym, cyp, czm, czp);
-    c->h_czm = czm;
-    c->h_czp = czp;
-    if ((rc = upload(c, &c->c64.cxm, cxm)) || (rc = upload(c, &c->c64.cxp, cxp)) ||
-        (rc = upload(c, &c->c64.cym, cym)) || (rc = upload(c, &c->c64.cyp, cyp)) ||
-        (rc = upload(c, &c->c64.czm, czm)) || (rc = upload(c, &c->c64.czp, czp)))
-        return fail(rc);
-    if ((rc = dalloc(c, &c->c64.fx.a, cxm.size())) || (rc = dalloc(c, &c->c64.fx.ib, cxm.size())) ||
-        (rc = dalloc(c, &c->c64.fx.cu, cxm.size())) || (rc = dalloc(c, &c->c64.fy.a, cym.size())) ||
-        (rc = dalloc(c, &c->c64.fy.ib, cym.size())) || (rc = dalloc(c, &c->c64.fy.cu, cym.size())))
+    // entry points work on double fields), built on the GPU, or on the host
+    // (GW_HOST_SETUP, or if the GPU's column grouping met a hash collision)
+    const size_t ntab = (size_t)c->n_zclass * c->nx * c->ny;   // x and y tables
+    {
+        double *cx[2], *cy[2], *cz[2];
+        if (!c->host_setup && (rc = gw_setup_tables_device(c, cx, cy, cz)) != GW_OK) {
+            if (rc != GW_ERR_UNSUPPORTED) return fail(rc);
+            c->host_setup = true;   // two material sequences with one hash: group exactly on the host
+            gw_build_profiles(c);
+        }
+    }
+    if (c->host_setup) {
+        std::vector<double> cxm, cxp, cym, cyp, czm, czp;
+        gw_build_coefs(c, cxm, cxp, cym, cyp, czm, czp);
+        c->h_czm = czm;
+        c->h_czp = czp;
+        if ((rc = upload(c, &c->c64.cxm, cxm)) || (rc = upload(c, &c->c64.cxp, cxp)) ||
+            (rc = upload(c, &c->c64.cym, cym)) || (rc = upload(c, &c->c64.cyp, cyp)) ||
+            (rc = upload(c, &c->c64.czm, czm)) || (rc = upload(c, &c->c64.czp, czp)))
+            return fail(rc);
+    }
+    const size_t nztab = (size_t)c->n_profiles * c->nz;
+    if ((rc = dalloc(c, &c->c64.fx.a, ntab)) || (rc = dalloc(c, &c->c64.fx.ib, ntab)) ||
+        (rc = dalloc(c, &c->c64.fx.cu, ntab)) || (rc = dalloc(c, &c->c64.fy.a, ntab)) ||
+        (rc = dalloc(c, &c->c64.fy.ib, ntab)) || (rc = dalloc(c, &c->c64.fy.cu, ntab)))
         return fail(rc);
     std::vector<int> order((size_t)c->nx * c->ny);
     for (size_t q = 0; q < order.size(); ++q) order[q] = (int)q;
@@ -386,21 +418,27 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
             (rc = dalloc(c, &c->d_fref64, (size_t)c->n_profiles * c->nz)) ||
             (rc = dalloc(c, &c->d_Tref, c->nz)))
             return fail(rc);
-        if ((rc = upload(c, &c->c32.cxm, to_float(cxm))) || (rc = upload(c, &c->c32.cxp, to_float(cxp))) ||
-            (rc = upload(c, &c->c32.cym, to_float(cym))) || (rc = upload(c, &c->c32.cyp, to_float(cyp))) ||
-            (rc = upload(c, &c->c32.czm, to_float(czm))) || (rc = upload(c, &c->c32.czp, to_float(czp))))
+        if ((rc = dalloc(c, &c->c32.cxm, ntab)) || (rc = dalloc(c, &c->c32.cxp, ntab)) ||
+            (rc = dalloc(c, &c->c32.cym, ntab)) || (rc = dalloc(c, &c->c32.cyp, ntab)) ||
+            (rc = dalloc(c, &c->c32.czm, nztab)) || (rc = dalloc(c, &c->c32.czp, nztab)) ||
+            (rc = gw_tables_to_float(c, c->c32.cxm, c->c64.cxm, ntab)) ||
+            (rc = gw_tables_to_float(c, c->c32.cxp, c->c64.cxp, ntab)) ||
+            (rc = gw_tables_to_float(c, c->c32.cym, c->c64.cym, ntab)) ||
+            (rc = gw_tables_to_float(c, c->c32.cyp, c->c64.cyp, ntab)) ||
+            (rc = gw_tables_to_float(c, c->c32.czm, c->c64.czm, nztab)) ||
+            (rc = gw_tables_to_float(c, c->c32.czp, c->c64.czp, nztab)))
             return fail(rc);
-        if ((rc = dalloc(c, &c->c32.fx.a, cxm.size())) || (rc = dalloc(c, &c->c32.fx.ib, cxm.size())) ||
-            (rc = dalloc(c, &c->c32.fx.cu, cxm.size())) || (rc = dalloc(c, &c->c32.fy.a, cym.size())) ||
-            (rc = dalloc(c, &c->c32.fy.ib, cym.size())) || (rc = dalloc(c, &c->c32.fy.cu, cym.size())) ||
-            (rc = dalloc(c, &c->c32.hx, 4 * cxm.size())) || (rc = dalloc(c, &c->c32.hy, 4 * cym.size())))
+        if ((rc = dalloc(c, &c->c32.fx.a, ntab)) || (rc = dalloc(c, &c->c32.fx.ib, ntab)) ||
+            (rc = dalloc(c, &c->c32.fx.cu, ntab)) || (rc = dalloc(c, &c->c32.fy.a, ntab)) ||
+            (rc = dalloc(c, &c->c32.fy.ib, ntab)) || (rc = dalloc(c, &c->c32.fy.cu, ntab)) ||
+            (rc = dalloc(c, &c->c32.hx, 4 * ntab)) || (rc = dalloc(c, &c->c32.hy, 4 * ntab)))
             return fail(rc);
         c->f_g1 = c->f_temp + N;
         GW_CUDA(cudaMemset(c->f_u, 0, N * sizeof(float)));
         std::vector<double> zero(c->nz, 0.0);
         if ((rc = set_reference_profile(c, zero.data()))) return fail(rc);
     } else {
-        if ((rc = dalloc(c, &c->c64.hx, 4 * cxm.size())) || (rc = dalloc(c, &c->c64.hy, 4 * cym.size())))
+        if ((rc = dalloc(c, &c->c64.hx, 4 * ntab)) || (rc = dalloc(c, &c->c64.hy, 4 * ntab)))
             return fail(rc);
         if ((rc = dalloc(c, &c->d_u, N)) || (rc = dalloc(c, &c->d_temp, N)) || (rc = dalloc(c, &c->d_g1, N)) ||
             (rc = dalloc(c, &c->d_tp, (size_t)ncol * c->nz)) ||

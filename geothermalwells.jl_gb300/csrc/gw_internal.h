@@ -134,6 +134,7 @@ struct gw_ctx {
     int rock2_nt = 256;               // threads per block of the ROCK2 column kernel
     int half_cfg = 0;                 // half-step tiling (gw_fused.cu kTileHW/kTileHR)
     bool fused = false;
+    bool host_setup = false;          // tables built on the host (GW_HOST_SETUP), else on the GPU
     int modular_reason = 0;           // GW_MODULAR_* bits when !fused
     // mixed path state (GW_PREC_MIXED): theta = T - T_ref(z) in float
     float *f_u = nullptr, *f_temp = nullptr, *f_g1 = nullptr, *f_tp = nullptr, *f_pp = nullptr;
@@ -168,6 +169,13 @@ struct gw_ctx {
     struct GwAdj *adj = nullptr;      // adjoint tables (gw_adjoint.cu), built on first use
 };
 
+// debug build (GW_DEBUG): device allocations registered for the kernels'
+// bounds checks (gw_debug.cuh); no-ops in the normal build
+void gw_debug_register(int device, const void *p, size_t bytes);
+void gw_debug_unregister(int device, const void *p);
+// GW_ERR_ARG if a bounds check failed since the last call (and clears it)
+int gw_debug_status(int device);
+
 // error reporting
 int gw_fail(int code, const std::string &msg);
 int gw_cuda_fail(cudaError_t e, const char *what);
@@ -179,6 +187,7 @@ int gw_cuda_fail(cudaError_t e, const char *what);
 
 // setup (gw_setup.cpp)
 int gw_setup_host(gw_ctx *c, const gw_desc *d);
+void gw_build_profiles(gw_ctx *c);   // host path of the column profiles
 void gw_build_coefs(const gw_ctx *c, std::vector<double> &cxm, std::vector<double> &cxp,
                     std::vector<double> &cym, std::vector<double> &cyp,
                     std::vector<double> &czm, std::vector<double> &czp);
@@ -193,6 +202,12 @@ void gw_build_adjoint_tables(const gw_ctx *c, std::vector<double> &wxm, std::vec
                              std::vector<double> &wzm, std::vector<double> &wzp,
                              std::vector<unsigned char> &rock, std::vector<int> &layer);
 void gw_adjoint_release(gw_ctx *c);
+// gw_setup_dev.cu: column profiles, coefficient tables (c64, owned by the
+// context; cx/cy/cz receive the (m, p) pointers), Thomas factors and half
+// tables on the GPU, bitwise the host builders' values.
+int gw_setup_tables_device(gw_ctx *c, double **cx, double **cy, double **cz);
+int gw_tables_to_float(gw_ctx *c, float *dst, const double *src, size_t n);
+int gw_factors_device(gw_ctx *c, double h);
 int gw_rock2_choose(double dt, double eigen_est, int max_stages, int *s, int *covered);
 void gw_rock2_coefs(int s, const double **mu, const double **nu, const double **kappa,
                     double *sigma, double *tau);

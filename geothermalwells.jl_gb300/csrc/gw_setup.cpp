@@ -67,6 +67,38 @@ bool strictly_increasing(const double *g, int n) {
 
 }  // namespace
 
+// Column profiles: columns whose (k, rho_c) sequences over the z-classes
+// agree share their z coefficients; ids in order of first appearance
+// (i, then j).
+void gw_build_profiles(gw_ctx *c) {
+    std::vector<int> rep(c->n_zclass, -1);
+    for (int k = 0; k < c->nz; ++k)
+        if (rep[c->zclass[k]] < 0) rep[c->zclass[k]] = k;
+    // column profiles: columns whose (k, rho_c) sequences over z-classes agree
+    c->colprof.assign((size_t)c->nx * c->ny, 0);
+    std::map<std::vector<double>, int> prof;
+    for (int i = 0; i < c->nx; ++i)
+        for (int j = 0; j < c->ny; ++j) {
+            std::vector<double> key;
+            key.reserve(2 * c->n_zclass);
+            for (int zc = 0; zc < c->n_zclass; ++zc) {
+                double z = c->gz[rep[zc]];
+                key.push_back(mat_k(c, c->gx[i], c->gy[j], z));
+                key.push_back(mat_rhoc(c, c->gx[i], c->gy[j], z));
+            }
+            auto it = prof.find(key);
+            int id;
+            if (it == prof.end()) {
+                id = (int)prof.size();
+                prof.emplace(std::move(key), id);
+            } else {
+                id = it->second;
+            }
+            c->colprof[(size_t)i * c->ny + j] = id;
+        }
+    c->n_profiles = (int)prof.size();
+}
+
 // Builds everything create_cache does on the host (src/cache.jl:9-44,55-65)
 // plus the z-classes: maximal sets of levels on which every depth comparison
 // of the material model (layers, z <= h, z <= h + 3, z <= insulation_depth)
@@ -168,29 +200,9 @@ int gw_setup_host(gw_ctx *c, const gw_desc *d) {
     }
     c->n_zclass = (int)rep.size();
 
-    // column profiles: columns whose (k, rho_c) sequences over z-classes agree
-    c->colprof.assign((size_t)c->nx * c->ny, 0);
-    std::map<std::vector<double>, int> prof;
-    for (int i = 0; i < c->nx; ++i)
-        for (int j = 0; j < c->ny; ++j) {
-            std::vector<double> key;
-            key.reserve(2 * c->n_zclass);
-            for (int zc = 0; zc < c->n_zclass; ++zc) {
-                double z = c->gz[rep[zc]];
-                key.push_back(mat_k(c, c->gx[i], c->gy[j], z));
-                key.push_back(mat_rhoc(c, c->gx[i], c->gy[j], z));
-            }
-            auto it = prof.find(key);
-            int id;
-            if (it == prof.end()) {
-                id = (int)prof.size();
-                prof.emplace(std::move(key), id);
-            } else {
-                id = it->second;
-            }
-            c->colprof[(size_t)i * c->ny + j] = id;
-        }
-    c->n_profiles = (int)prof.size();
+    // column profiles: on the host path here, else grouped on the GPU
+    // (gw_setup_dev.cu)
+    if (c->host_setup) gw_build_profiles(c);
 
     // src/cache.jl:9-44 create_advection_index_lists
     std::vector<int> ii, ij, ib, oi, oj, ob;

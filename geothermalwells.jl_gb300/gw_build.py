@@ -19,7 +19,8 @@ OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgw_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["gw_setup.cpp", "gw_api.cu", "gw_kernels.cu", "gw_fused.cu", "gw_tridiag.cu", "gw_batch.cu", "gw_noalloc.cu", "gw_adjoint.cu"]
+SOURCES = ["gw_setup.cpp", "gw_setup_dev.cu", "gw_api.cu", "gw_kernels.cu", "gw_fused.cu", "gw_tridiag.cu",
+           "gw_batch.cu", "gw_noalloc.cu", "gw_adjoint.cu"]
 
 
 def nvcc():

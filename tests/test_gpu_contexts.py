@@ -122,3 +122,32 @@ def test_device_fields_round_trip(gwlib):
     _lib.check(L.gw_field_free(c.ctx, pa))
     _lib.check(L.gw_field_free(c.ctx, pb))
     c.close()
+
+
+SETUP_CASES = {
+    "small_layers_3wells": lambda: W.small_case(nbh=3, n_layers=3, insulation_depth=40.0, inlet="hx"),
+    "well_array_example": W.example_well_array,
+    "2mm": W.single_well_2mm,
+    "ensemble_design": lambda: (lambda d: dict(d, T0=W.initial_field(d), dt=600.0))(W.ensemble()[1]),
+}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", list(SETUP_CASES))
+def test_device_setup_equals_host_setup(name, precision, gwlib, monkeypatch):
+    """The material classification, column profiles, coefficient tables and
+    Thomas factors built on the GPU (the default) give the host builders'
+    tables bitwise: the steps of both contexts agree bit for bit."""
+    w = SETUP_CASES[name]()
+    monkeypatch.setenv("GW_HOST_SETUP", "1")
+    host = make(w, precision)
+    monkeypatch.delenv("GW_HOST_SETUP")
+    dev = make(w, precision)
+    ih, id_ = info(host), info(dev)
+    assert (ih.n_zclass, ih.n_profiles, ih.countxy_inner, ih.countxy_outer) == \
+        (id_.n_zclass, id_.n_profiles, id_.countxy_inner, id_.countxy_outer)
+    a = run(host, w, 3)
+    b = run(dev, w, 3)
+    assert np.array_equal(a.u[-1], b.u[-1])
+    assert np.array_equal(a.T_outlet, b.T_outlet)
+    host.close(); dev.close()
