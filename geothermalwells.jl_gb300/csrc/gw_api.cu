@@ -7,11 +7,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
 #include "gw_fused.h"
 #include "gw_internal.h"
+#include "gw_debug.cuh"
 
 namespace {
 thread_local std::string g_err;
@@ -23,6 +25,7 @@ int dalloc(gw_ctx *c, T **p, size_t n) {
     if (e != cudaSuccess) return gw_cuda_fail(e, "cudaMalloc");
     c->allocations.push_back((void *)*p);
     c->device_bytes += (long long)(n * sizeof(T));
+    gw_debug_register(c->device, *p, n * sizeof(T));
     return GW_OK;
 }
 
@@ -165,7 +168,73 @@ int gw_cuda_fail(cudaError_t e, const char *what) {
     return GW_ERR_CUDA;
 }
 
-#ifndef GW_DEBUG
+// the instrumented translation units' registry binders (gw_debug.cuh)
+int gw_debug_bind_fused(GwDbgRegistry *r);
+
+#ifdef GW_DEBUG
+// The allocation registry of the debug build, one per device: a host list
+// mirrored into a device GwDbgRegistry whose address every instrumented
+// translation unit holds in constant memory.
+namespace {
+std::mutex g_dbg_mutex;
+struct DbgDevice {
+    GwDbgRegistry *reg = nullptr;
+    std::vector<std::pair<unsigned long long, unsigned long long>> ranges;
+};
+DbgDevice g_dbg[64];
+
+void dbg_sync(int dev) {   // with g_dbg_mutex held and dev current
+    DbgDevice &D = g_dbg[dev];
+    if (!D.reg) {
+        if (cudaMalloc((void **)&D.reg, sizeof(GwDbgRegistry)) != cudaSuccess) { D.reg = nullptr; return; }
+        cudaMemset(D.reg, 0, sizeof(GwDbgRegistry));
+        gw_debug_bind_fused(D.reg);
+    }
+    const unsigned n = (unsigned)std::min<size_t>(D.ranges.size(), GW_DBG_MAX_ALLOC);
+    std::vector<unsigned long long> b(n), e(n);
+    for (unsigned i = 0; i < n; ++i) { b[i] = D.ranges[i].first; e[i] = D.ranges[i].second; }
+    cudaDeviceSynchronize();   // no instrumented kernel reads the registry meanwhile
+    cudaMemcpy(&D.reg->count, &n, sizeof(n), cudaMemcpyHostToDevice);
+    if (n) {
+        cudaMemcpy(D.reg->base, b.data(), n * sizeof(unsigned long long), cudaMemcpyHostToDevice);
+        cudaMemcpy(D.reg->end, e.data(), n * sizeof(unsigned long long), cudaMemcpyHostToDevice);
+    }
+}
+}  // namespace
+
+void gw_debug_register(int dev, const void *p, size_t bytes) {
+    if (dev < 0 || dev >= 64 || !p) return;
+    std::lock_guard<std::mutex> lock(g_dbg_mutex);
+    const unsigned long long a = (unsigned long long)p;
+    g_dbg[dev].ranges.emplace_back(a, a + bytes);
+    dbg_sync(dev);
+}
+
+void gw_debug_unregister(int dev, const void *p) {
+    if (dev < 0 || dev >= 64 || !p) return;
+    std::lock_guard<std::mutex> lock(g_dbg_mutex);
+    auto &r = g_dbg[dev].ranges;
+    for (size_t i = 0; i < r.size(); ++i)
+        if (r[i].first == (unsigned long long)p) { r.erase(r.begin() + (long)i); break; }
+    dbg_sync(dev);
+}
+
+int gw_debug_status(int dev) {
+    if (dev < 0 || dev >= 64 || !g_dbg[dev].reg) return GW_OK;
+    unsigned fail = 0;
+    unsigned long long addr = 0;
+    GwDbgRegistry *r = g_dbg[dev].reg;
+    GW_CUDA(cudaDeviceSynchronize());
+    GW_CUDA(cudaMemcpy(&fail, &r->fail, sizeof(fail), cudaMemcpyDeviceToHost));
+    GW_CUDA(cudaMemcpy(&addr, &r->addr, sizeof(addr), cudaMemcpyDeviceToHost));
+    if (!fail) return GW_OK;
+    const unsigned zero = 0;
+    GW_CUDA(cudaMemcpy(&r->fail, &zero, sizeof(unsigned), cudaMemcpyHostToDevice));
+    char msg[160];
+    std::snprintf(msg, sizeof msg, "debug bounds check failed: site %u, address/offset 0x%llx", fail - 1, addr);
+    return gw_fail(GW_ERR_ARG, msg);
+}
+#else
 void gw_debug_register(int, const void *, size_t) {}
 void gw_debug_unregister(int, const void *) {}
 int gw_debug_status(int) { return GW_OK; }
@@ -477,7 +546,7 @@ int gw_destroy(gw_ctx *c) {
         if (c->ev_copy[b]) cudaEventDestroy(c->ev_copy[b]);
     }
     gw_adjoint_release(c);
-    for (void *p : c->allocations) if (p) cudaFree(p);
+    for (void *p : c->allocations) if (p) { gw_debug_unregister(c->device, p); cudaFree(p); }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return GW_OK;
@@ -801,7 +870,7 @@ int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
     GW_CUDA(cudaEventRecord(c->ev0, c->stream));
     for (int n = 0; n < nsteps; ++n) GW_CUDA(cudaGraphLaunch(c->graph, c->stream));
     GW_CUDA(cudaEventRecord(c->ev1, c->stream));
-    if ((rc = sync(c))) return rc;
+    if ((rc = sync(c)) || (rc = gw_debug_status(c->device))) return rc;
     float ms = 0.f;
     GW_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     c->last_step_ms = ms;
@@ -844,7 +913,8 @@ int gw_profile_kernels(gw_ctx *c, double dt, int reps, double *ms_out) {
         ms_out[part] = total / reps;
     }
     GW_CUDA(cudaMemcpyAsync(u, bak, bytes, cudaMemcpyDeviceToDevice, c->stream));
-    return sync(c);
+    if ((rc = sync(c))) return rc;
+    return gw_debug_status(c->device);
 }
 
 int gw_snapshot_host_alloc(gw_ctx *c, float **host) {

@@ -237,6 +237,7 @@ int gw_batch_step(gw_batch *b, double dt, int nsteps, int max_stages) {
     for (int k = 0; k < nsteps % kSteps; ++k) GW_CUDA(cudaGraphLaunch(b->graph1, b->stream));
     GW_CUDA(cudaEventRecord(b->ev1, b->stream));
     GW_CUDA(cudaStreamSynchronize(b->stream));
+    if ((rc = gw_debug_status(b->device))) return rc;
     float ms = 0.f;
     GW_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     b->last_ms = ms;

@@ -27,6 +27,7 @@
 #include "gw_internal.h"
 #include "gw_fused.h"
 #include "gw_inlet.cuh"
+#include "gw_debug.cuh"
 
 namespace {
 
@@ -171,8 +172,10 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) 
     // The column is padded to nt * LPT levels: pad levels start at zero and
     // have zero coefficients, so they never feed a real level (the real
     // bottom level's cp is 0) and every thread owns exactly LPT levels.
-    for (int k = nz + t; k < nt * LPT; k += nt) { stage[spad(k)] = T(0); stage[nzs + spad(k)] = T(0); }
-    if (t < 2) { s_hi[t][0] = C(0); s_lo[t][nt] = C(0); }
+    for (int k = nz + t; k < nt * LPT; k += nt) {
+        if (GW_OK_D(stage + nzs + spad(k), smem_raw, 201)) { stage[spad(k)] = T(0); stage[nzs + spad(k)] = T(0); }
+    }
+    if (t < 2 && GW_OK_I(nt, 257, 202)) { s_hi[t][0] = C(0); s_lo[t][nt] = C(0); }
     // thread t copies levels t + nt i, whose padded slots are spad(t) + nts i
     const int st0 = spad(t), nts = nt + nt / 32;
     auto fetch = [&](long long col, int buf) {
@@ -180,15 +183,15 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) 
         const T *g = u + col * nz + t;
 #pragma unroll
         for (int i = 0; i < LPT; ++i)
-            if (t + nt * i < nz) cp_async<sizeof(T)>(d + nts * i, g + nt * i, true);
+            if (t + nt * i < nz && GW_OK_D(d + nts * i, smem_raw, 203) && GW_OK_G(g + nt * i, 204))
+                cp_async<sizeof(T)>(d + nts * i, g + nt * i, true);
         cp_async_commit();
     };
     auto exchange = [&](const C (&v)[LPT], C &left, C &right) {
-        s_lo[xb][t] = v[0];
-        s_hi[xb][t + 1] = v[LPT - 1];
+        if (GW_OK_I(t + 1, 257, 205)) { s_lo[xb][t] = v[0]; s_hi[xb][t + 1] = v[LPT - 1]; }
         __syncthreads();
-        left = s_hi[xb][t];
-        right = s_lo[xb][t + 1];
+        left = GW_OK_I(t + 1, 257, 205) ? s_hi[xb][t] : C(0);
+        right = GW_OK_I(t + 1, 257, 205) ? s_lo[xb][t + 1] : C(0);
         xb ^= 1;
     };
     auto apply = [&](const C (&v)[LPT], const C (&cm)[LPT], const C (&cp)[LPT], int i, C left,
@@ -204,9 +207,9 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) 
     int buf = 0;
     // column indices and profiles run one column ahead of their use, so their
     // loads are not on the per-column chain
-    long long col = it < ncols ? order[it] : 0;
-    long long col_n = it + gridDim.x < ncols ? order[it + gridDim.x] : 0;
-    int p_cur = it < ncols ? colprof[col] : 0;
+    long long col = it < ncols && GW_OK_G(order + it, 206) ? order[it] : 0;
+    long long col_n = it + gridDim.x < ncols && GW_OK_G(order + it + gridDim.x, 206) ? order[it + gridDim.x] : 0;
+    int p_cur = it < ncols && GW_OK_G(colprof + col, 207) ? colprof[col] : 0;
     if (it < ncols) fetch(col, 0);
     for (; it < ncols; it += gridDim.x, buf ^= 1) {
         const long long nxt = it + gridDim.x;
@@ -214,8 +217,8 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) 
         long long col_nn = 0;
         if (nxt < ncols) {
             fetch(col_n, buf ^ 1);
-            if (nxt + gridDim.x < ncols) col_nn = order[nxt + gridDim.x];
-            p_cur = colprof[col_n];
+            if (nxt + gridDim.x < ncols && GW_OK_G(order + nxt + gridDim.x, 206)) col_nn = order[nxt + gridDim.x];
+            p_cur = GW_OK_G(colprof + col_n, 207) ? colprof[col_n] : 0;
             cp_async_wait<1>();
         } else {
             cp_async_wait<0>();
@@ -226,16 +229,16 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) 
             for (int i = 0; i < LPT; ++i) {
                 const bool ok = kb + i < nz;
                 const size_t q = (size_t)p * nz + kb + i;
-                cm[i] = ok ? __ldg(czm + q) : C(0);
-                cp[i] = ok ? __ldg(czp + q) : C(0);
-                fr[i] = (INC && fref && ok) ? __ldg(fref + q) : C(0);
+                cm[i] = ok && GW_OK_G(czm + q, 208) ? __ldg(czm + q) : C(0);
+                cp[i] = ok && GW_OK_G(czp + q, 208) ? __ldg(czp + q) : C(0);
+                fr[i] = (INC && fref && ok && GW_OK_G(fref + q, 209)) ? __ldg(fref + q) : C(0);
             }
         }
         __syncthreads();
         T *st = stage + (size_t)buf * nzs;
         C base[LPT], F0[LPT], prev[LPT], cur[LPT];
 #pragma unroll
-        for (int i = 0; i < LPT; ++i) base[i] = (C)st[spad(kb + i)];
+        for (int i = 0; i < LPT; ++i) base[i] = GW_OK_D(st + spad(kb + i), smem_raw, 210) ? (C)st[spad(kb + i)] : C(0);
         C left, right;
         exchange(base, left, right);
         if (INC) {
@@ -292,13 +295,14 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) 
             C a = apply(q, cm, cp, i, left, right);
             if (INC) a += F0[i];
             const C y = q[i] + hts * a + c3 * (q[i] - cur[i]);
-            st[spad(kb + i)] = (T)(INC ? base[i] + y : y);
+            if (GW_OK_D(st + spad(kb + i), smem_raw, 210)) st[spad(kb + i)] = (T)(INC ? base[i] + y : y);
         }
         __syncthreads();
         T *uc = u + col * nz + t;
 #pragma unroll
         for (int i = 0; i < LPT; ++i)
-            if (t + nt * i < nz) uc[nt * i] = st[st0 + nts * i];
+            if (t + nt * i < nz && GW_OK_G(uc + nt * i, 211) && GW_OK_D(st + st0 + nts * i, smem_raw, 212))
+                uc[nt * i] = st[st0 + nts * i];
         __syncthreads();   // this buffer is refilled by the next iteration's fetch
         col = col_n;
         col_n = col_nn;
@@ -344,26 +348,30 @@ __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int ch = blockIdx.y + kChunkRows * blockIdx.z;   // chunk rows of at most 65535
     if (k >= nz || ch >= nchunks) return;
+    if (!GW_OK_G(chunks + ch, 301) || !GW_OK_G(zclass + k, 302)) return;
     const int4 C = chunks[ch];   // (borehole, first column, end column, outer?)
     const int zc = zclass[k];
     const T hh = (T)h;
+    // debug build: every global load checked (nothing in the normal build)
+    auto ld = [&](const T *p) -> T { return GW_OK_G(p, 304) ? *p : T(0); };
     auto sweep = [&](int q) {
-        const int i = pi[q], j = pj[q];
+        const int i = GW_OK_G(pi + q, 303) ? pi[q] : 0, j = GW_OK_G(pj + q, 303) ? pj[q] : 0;
         const long long c = k + (long long)nz * (j + (long long)ny * i);
-        const T xc = src[c];
+        const T xc = ld(src + c);
         T xp, xm;
         size_t t;
         if (dir == GW_DIR_X) {
             const long long st = (long long)nz * ny;
-            xp = (i < nx - 1) ? src[c + st] : xc;
-            xm = (i > 0) ? src[c - st] : xc;
+            xp = (i < nx - 1) ? ld(src + c + st) : xc;
+            xm = (i > 0) ? ld(src + c - st) : xc;
             t = ((size_t)zc * ny + j) * nx + i;
         } else {
-            xp = (j < ny - 1) ? src[c + nz] : xc;
-            xm = (j > 0) ? src[c - nz] : xc;
+            xp = (j < ny - 1) ? ld(src + c + nz) : xc;
+            xm = (j > 0) ? ld(src + c - nz) : xc;
             t = ((size_t)zc * nx + i) * ny + j;
         }
-        const T a = __ldg(cpt + t) * (xp - xc) - __ldg(cmt + t) * (xc - xm);
+        const T a = (GW_OK_G(cpt + t, 305) ? __ldg(cpt + t) : T(0)) * (xp - xc) -
+                    (GW_OK_G(cmt + t, 305) ? __ldg(cmt + t) : T(0)) * (xc - xm);
         return fma(hh, a, xc);
     };
     // four columns per round: their loads are independent and overlap; the
@@ -376,18 +384,18 @@ __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *
         for (int u = 0; u < 4; ++u) v[u] = sweep(q + u);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            tp[(size_t)(q + u) * nz + k] = v[u];
+            if (GW_OK_G(tp + (size_t)(q + u) * nz + k, 306)) tp[(size_t)(q + u) * nz + k] = v[u];
             acc += (double)v[u];
         }
     }
     for (; q < C.z; ++q) {
         const T v = sweep(q);
-        tp[(size_t)q * nz + k] = v;
+        if (GW_OK_G(tp + (size_t)q * nz + k, 306)) tp[(size_t)q * nz + k] = v;
         acc += (double)v;
     }
     // absolute temperature: add T_ref once per column summed
-    if (Tref) acc += (double)(C.z - C.y) * Tref[k];
-    part[(size_t)ch * nz + k] = acc;
+    if (Tref && GW_OK_G(Tref + k, 308)) acc += (double)(C.z - C.y) * Tref[k];
+    if (GW_OK_G(part + (size_t)ch * nz + k, 307)) part[(size_t)ch * nz + k] = acc;
 }
 
 constexpr int kReduceWarps = 8;   // warps of k_pipe_reduce, splitting a borehole's chunks
@@ -403,6 +411,7 @@ __global__ void __launch_bounds__(32 * kReduceWarps) k_pipe_reduce(double *__res
                                                      const GwBhDev *__restrict__ bh, int nz) {
     __shared__ double s_red[32 * kReduceWarps];
     const int b = blockIdx.y;
+    if (!GW_OK_G(bh + b, 311) || !GW_OK_GB(bchunk + 4 * b, 4 * sizeof(int), 312)) return;
     const GwBhDev B = bh[b];
     // chunks of b: inner [bchunk[4b], bchunk[4b+1]), outer [bchunk[4b+2], bchunk[4b+3])
     const int i0 = bchunk[4 * b], i1 = bchunk[4 * b + 1], o0 = bchunk[4 * b + 2], o1 = bchunk[4 * b + 3];
@@ -410,29 +419,30 @@ __global__ void __launch_bounds__(32 * kReduceWarps) k_pipe_reduce(double *__res
     const int k = blockIdx.x * 32 + lane;
     double sacc = 0.0;
     if (k < nz)
-        for (int ch = o0 + w; ch < o1; ch += kReduceWarps) sacc += part[(size_t)ch * nz + k];
+        for (int ch = o0 + w; ch < o1; ch += kReduceWarps)
+            sacc += GW_OK_G(part + (size_t)ch * nz + k, 313) ? part[(size_t)ch * nz + k] : 0.0;
     s_red[threadIdx.x] = sacc;
     __syncthreads();
     if (w == 0 && k < nz) {
         double m = s_red[lane];
 #pragma unroll
         for (int q = 1; q < kReduceWarps; ++q) m += s_red[32 * q + lane];
-        mean[(size_t)b * nz + k] = m / (double)B.outer_count;
+        if (GW_OK_G(mean + (size_t)b * nz + k, 314)) mean[(size_t)b * nz + k] = m / (double)B.outer_count;
     }
     if (blockIdx.x != 0) return;   // the whole block: the outlet is block 0's
     __syncthreads();   // every read of s_red above is done
-    const int nlev = nlev_b[b];
+    const int nlev = GW_OK_G(nlev_b + b, 315) ? nlev_b[b] : 0;
     const int total = nlev * (i1 - i0);
     double acc = 0.0;
     for (int e = threadIdx.x; e < total; e += blockDim.x)   // level fastest: coalesced
-        acc += part[(size_t)(i0 + e / nlev) * nz + e % nlev];
+        acc += GW_OK_G(part + (size_t)(i0 + e / nlev) * nz + e % nlev, 313) ? part[(size_t)(i0 + e / nlev) * nz + e % nlev] : 0.0;
     s_red[threadIdx.x] = acc;
     __syncthreads();
     for (int r = blockDim.x / 2; r > 0; r >>= 1) {
         if (threadIdx.x < r) s_red[threadIdx.x] += s_red[threadIdx.x + r];
         __syncthreads();
     }
-    if (threadIdx.x == 0) outlet[b] = s_red[0] / (double)((long long)B.inner_count * nlev);
+    if (threadIdx.x == 0 && GW_OK_G(outlet + b, 316)) outlet[b] = s_red[0] / (double)((long long)B.inner_count * nlev);
 }
 
 // Outlet window of kernel_accumulate_outlet! (src/solver.jl:273-281) for a
@@ -540,8 +550,10 @@ __global__ void __launch_bounds__(128) k_advect_c(T *__restrict__ pp, const T *_
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int ch = blockIdx.y + kChunkRows * blockIdx.z;
     if (k >= countz || ch >= nchunks) return;
+    if (!GW_OK_G(chunks + ch, 321)) return;
     const int4 C = chunks[ch];   // (borehole, first column, end column, annulus?)
     const int b = C.x;
+    if (!GW_OK_G(tab + ((size_t)b * countz + k) * 2 + C.w, 322)) return;
     const GwAdvRec r = tab[((size_t)b * countz + k) * 2 + C.w];
     T *out = pp + k;
     if (r.type == kAdvInlet || r.type == kAdvTurn) {
@@ -554,11 +566,13 @@ __global__ void __launch_bounds__(128) k_advect_c(T *__restrict__ pp, const T *_
             v = __fma_rn(r.alpha, m[r.ir], __dmul_rn(__dsub_rn(1.0, r.alpha), m[r.il]));
         }
         const T o = (T)(Tref ? v - Tref[k] : v);
-        for (int q = C.y; q < C.z; ++q) out[(size_t)q * countz] = o;
+        for (int q = C.y; q < C.z; ++q)
+            if (GW_OK_G(out + (size_t)q * countz, 325)) out[(size_t)q * countz] = o;
         return;
     }
     if (r.type == kAdvKeep) {
         for (int q = C.y; q < C.z; ++q) {
+            if (!GW_OK_G(tp + (size_t)q * nz + k, 326) || !GW_OK_G(out + (size_t)q * countz, 325)) continue;
             const double v = absT(tp[(size_t)q * nz + k], Tref, k);
             out[(size_t)q * countz] = (T)(Tref ? v - Tref[k] : v);
         }
@@ -570,6 +584,8 @@ __global__ void __launch_bounds__(128) k_advect_c(T *__restrict__ pp, const T *_
         const float a = (float)r.alpha, a1 = 1.0f - a, dref = (float)r.dref;
         for (int q = C.y; q < C.z; ++q) {
             const T *col = tp + (size_t)q * nz;
+            if (!GW_OK_G(col + r.ir, 326) || !GW_OK_G(col + r.il, 326) || !GW_OK_G(out + (size_t)q * countz, 325))
+                continue;
             out[(size_t)q * countz] = (T)(fmaf(a, (float)col[r.ir], a1 * (float)col[r.il]) + dref);
         }
         return;
@@ -577,6 +593,8 @@ __global__ void __launch_bounds__(128) k_advect_c(T *__restrict__ pp, const T *_
     const double a1 = __dsub_rn(1.0, r.alpha);
     for (int q = C.y; q < C.z; ++q) {
         const T *col = tp + (size_t)q * nz;
+        if (!GW_OK_G(col + r.ir, 326) || !GW_OK_G(col + r.il, 326) || !GW_OK_G(out + (size_t)q * countz, 325))
+            continue;
         const double v = __fma_rn(r.alpha, absT(col[r.ir], Tref, r.ir), __dmul_rn(a1, absT(col[r.il], Tref, r.il)));
         out[(size_t)q * countz] = (T)(Tref ? v - Tref[k] : v);
     }
@@ -638,10 +656,11 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     // element (k, line m, row l): x-lines (k, j=m, i=l), y-lines (k, i=m, j=l)
     const long long mst = XL ? (long long)nz : (long long)nz * ny;
     const long long rst = XL ? (long long)nz * ny : (long long)nz;
-    const size_t fb = ((size_t)zclass[kc] * nl + mc) * N;
+    const size_t fb = ((size_t)(GW_OK_G(zclass + kc, 112) ? zclass[kc] : 0) * nl + mc) * N;
     const int *pline = pipe_line + (size_t)mc * N;
     // lines through no pipe column skip the per-row pipe lookup (most lines)
-    const bool pipe_levels = k < countz && __ldg(pipe_line + (size_t)nl * N + mc) != 0;
+    const bool pipe_levels = k < countz && GW_OK_G(pipe_line + (size_t)nl * N + mc, 113) &&
+                             __ldg(pipe_line + (size_t)nl * N + mc) != 0;
     const Quad<T> *hql = hq + fb;
     T *dl = dst + k + m * mst;   // row 0 of this thread's line
     const int nchunk = (N + HR - 1) / HR;
@@ -657,6 +676,13 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
         sok[rep] = mm < HW + 2 && kok && gm >= 0 && gm < nl;
         gs[rep] = sok[rep] ? src + k + (long long)gm * mst : src;
     }
+    // debug build: tile copies and tile reads checked (nothing in the normal build)
+    auto tile_copy = [&](T *ds, const T *gp, bool ok) {
+        if (!GW_OK_D(ds, smem_raw, 101)) return;
+        ok = ok && GW_OK_G(gp, 102);
+        cp_async<sizeof(T)>(ds, ok ? (const void *)gp : (const void *)src, ok);
+    };
+    auto rd = [&](const T *p) -> T { return GW_OK_D(p, smem_raw, 103) ? *p : T(0); };
     auto load_chunk = [&](int ch, int buf) {
         T *t = tile + buf * kTile;
         const int l0 = ch * HR;
@@ -668,18 +694,18 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
             T *d = t + (warp + rep * HW) * 32 + lane;
             if (full) {
 #pragma unroll
-                for (int r = 0; r < HR; ++r) cp_async<sizeof(T)>(d + r * kRow, sok[rep] ? (const void *)(g + r * rst) : (const void *)src, sok[rep]);
+                for (int r = 0; r < HR; ++r) tile_copy(d + r * kRow, g + r * rst, sok[rep]);
             } else {
                 for (int r = 0; r < HR; ++r) {
-                    const bool ok = sok[rep] && l0 + r < N;
-                    cp_async<sizeof(T)>(d + r * kRow, ok ? (const void *)(g + r * rst) : (const void *)src, ok);
+                    tile_copy(d + r * kRow, g + r * rst, sok[rep] && l0 + r < N);
                 }
             }
         }
         cp_async_commit();
     };
     // warp-uniform: does this line cross a pipe column at any level?
-    const bool line_pipe = __ldg(pipe_line + (size_t)nl * N + mc) != 0;
+    const bool line_pipe = GW_OK_G(pipe_line + (size_t)nl * N + mc, 113) &&
+                           __ldg(pipe_line + (size_t)nl * N + mc) != 0;
 
     T y = T(0);
     T *dr = dl;
@@ -703,14 +729,14 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                 T xm[kHG], xc[kHG], xp[kHG];
 #pragma unroll
                 for (int g = 0; g < kHG; ++g) {
-                    q[g] = qc[r0 + g];
+                    q[g] = GW_OK_G(qc + r0 + g, 104) ? qc[r0 + g] : Quad<T>{};
                     const T *rw = row + (r0 + g) * kRow;
-                    xm[g] = rw[0]; xc[g] = rw[32]; xp[g] = rw[64];
+                    xm[g] = rd(rw); xc[g] = rd(rw + 32); xp[g] = rd(rw + 64);
                 }
 #pragma unroll
                 for (int g = 0; g < kHG; ++g) {
                     y = fma(q[g].x, xc[g], fma(q[g].y, xp[g], fma(q[g].z, xm[g], -q[g].w * y)));
-                    if (active) *dr = y;
+                    if (active && GW_OK_G(dr, 108)) *dr = y;
                     dr += rst;
                 }
             }
@@ -725,21 +751,21 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                 int pq[kHG];
 #pragma unroll
                 for (int g = 0; g < kHG; ++g) {
-                    q[g] = qc[r0 + g];
+                    q[g] = GW_OK_G(qc + r0 + g, 104) ? qc[r0 + g] : Quad<T>{};
                     const T *rw = row + (r0 + g) * kRow;
-                    xm[g] = rw[0]; xc[g] = rw[32]; xp[g] = rw[64];
-                    pq[g] = pipe_levels ? __ldg(pline + l0 + r0 + g) : -1;
+                    xm[g] = rd(rw); xc[g] = rd(rw + 32); xp[g] = rd(rw + 64);
+                    pq[g] = pipe_levels && GW_OK_G(pline + l0 + r0 + g, 105) ? __ldg(pline + l0 + r0 + g) : -1;
                 }
 #pragma unroll
                 for (int g = 0; g < kHG; ++g) {
-                    pv[g] = pq[g] >= 0 ? pp[(size_t)pq[g] * countz + k] : T(0);
-                    iv[g] = pq[g] >= 0 ? __ldg(fib + fb + l0 + r0 + g) : T(0);
+                    pv[g] = pq[g] >= 0 && GW_OK_G(pp + (size_t)pq[g] * countz + k, 106) ? pp[(size_t)pq[g] * countz + k] : T(0);
+                    iv[g] = pq[g] >= 0 && GW_OK_G(fib + fb + l0 + r0 + g, 107) ? __ldg(fib + fb + l0 + r0 + g) : T(0);
                 }
 #pragma unroll
                 for (int g = 0; g < kHG; ++g) {
                     const T ay = q[g].w * y;
                     y = pq[g] >= 0 ? fma(pv[g], iv[g], -ay) : fma(q[g].x, xc[g], fma(q[g].y, xp[g], fma(q[g].z, xm[g], -ay)));
-                    if (active) *dr = y;
+                    if (active && GW_OK_G(dr, 108)) *dr = y;
                     dr += rst;
                 }
             }
@@ -747,14 +773,16 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
             const int rmax = min(HR, N - l0);
             for (int r = 0; r < rmax; ++r) {
                 const int l = l0 + r;
-                const Quad<T> q = qc[r];
+                const Quad<T> q = GW_OK_G(qc + r, 104) ? qc[r] : Quad<T>{};
                 const T *rw = row + r * kRow;
                 const T ay = q.w * y;
-                T yn = fma(q.x, rw[32], fma(q.y, rw[64], fma(q.z, rw[0], -ay)));
-                const int pq = pipe_levels ? __ldg(pline + l) : -1;
-                if (pq >= 0) yn = fma(pp[(size_t)pq * countz + k], __ldg(fib + fb + l), -ay);
+                T yn = fma(q.x, rd(rw + 32), fma(q.y, rd(rw + 64), fma(q.z, rd(rw), -ay)));
+                const int pq = pipe_levels && GW_OK_G(pline + l, 105) ? __ldg(pline + l) : -1;
+                if (pq >= 0)
+                    yn = fma(GW_OK_G(pp + (size_t)pq * countz + k, 106) ? pp[(size_t)pq * countz + k] : T(0),
+                             GW_OK_G(fib + fb + l, 107) ? __ldg(fib + fb + l) : T(0), -ay);
                 y = yn;
-                if (active) *dr = y;
+                if (active && GW_OK_G(dr, 108)) *dr = y;
                 dr += rst;
             }
         }
@@ -771,21 +799,24 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     if (l - kHB + 1 >= 0) {
         T cur[kHB], cuc[kHB];
 #pragma unroll
-        for (int b = 0; b < kHB; ++b) { cur[b] = pc[-(long long)b * rst]; cuc[b] = __ldg(cuf + l - b); }
+        for (int b = 0; b < kHB; ++b) {
+            cur[b] = GW_OK_G(pc - (long long)b * rst, 109) ? pc[-(long long)b * rst] : T(0);
+            cuc[b] = GW_OK_G(cuf + l - b, 110) ? __ldg(cuf + l - b) : T(0);
+        }
         while (l - kHB + 1 >= 0) {
             const bool more = l - 2 * kHB + 1 >= 0;
             T nxt[kHB], cun[kHB];
             if (more) {
 #pragma unroll
                 for (int b = 0; b < kHB; ++b) {
-                    nxt[b] = pc[-(long long)(b + kHB) * rst];
-                    cun[b] = __ldg(cuf + l - kHB - b);
+                    nxt[b] = GW_OK_G(pc - (long long)(b + kHB) * rst, 109) ? pc[-(long long)(b + kHB) * rst] : T(0);
+                    cun[b] = GW_OK_G(cuf + l - kHB - b, 110) ? __ldg(cuf + l - kHB - b) : T(0);
                 }
             }
 #pragma unroll
             for (int b = 0; b < kHB; ++b) {
                 x = cur[b] - cuc[b] * x;
-                __stcs(pc - (long long)b * rst, x);
+                if (GW_OK_G(pc - (long long)b * rst, 111)) __stcs(pc - (long long)b * rst, x);
             }
             pc -= (long long)kHB * rst;
             l -= kHB;
@@ -795,8 +826,8 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
         }
     }
     for (; l >= 0; --l) {
-        x = *pc - __ldg(cuf + l) * x;
-        __stcs(pc, x);
+        x = (GW_OK_G(pc, 109) ? *pc : T(0)) - (GW_OK_G(cuf + l, 110) ? __ldg(cuf + l) : T(0)) * x;
+        if (GW_OK_G(pc, 111)) __stcs(pc, x);
         pc -= rst;
     }
 }
@@ -966,27 +997,60 @@ __global__ void __launch_bounds__(128) k_half_refine(float *__restrict__ x, floa
         const size_t q = ((size_t)zc * N + l) * nl + m;
         return fma(h, __ldg(ecp + q) * (up - uc) - __ldg(ecm + q) * (uc - um), uc);
     };
+    // rows in batches of kRB: the batch's loads are independent of the
+    // recurrence and issue together, ahead of it
+    constexpr int kRB = 8;
     double xm = 0.0, xc = x[e0], y = 0.0;
-    for (int l = 0; l < N; ++l) {
-        const double xp = l + 1 < N ? (double)x[e0 + (l + 1) * rst] : 0.0;
-        const double cm = __ldg(lcm + lb + l), cp = __ldg(lcp + lb + l);
-        double ax = (1.0 + h * (cm + cp)) * xc;
-        if (l > 0) ax -= h * cm * xm;
-        if (l + 1 < N) ax -= h * cp * xp;
-        const double r = b_at(l) - ax;
-        y = (r - (double)__ldg(fa + lb + l) * y) * (double)__ldg(fib + lb + l);
-        yb[e0 + l * rst] = (float)y;
-        xm = xc;
-        xc = xp;
+    for (int l0 = 0; l0 < N; l0 += kRB) {
+        double xn[kRB], bb[kRB], cm[kRB], cp[kRB], fa_[kRB], fi_[kRB];
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) {
+            const int l = l0 + r;
+            if (l < N) {
+                xn[r] = l + 1 < N ? (double)x[e0 + (l + 1) * rst] : 0.0;
+                bb[r] = b_at(l);
+                cm[r] = __ldg(lcm + lb + l); cp[r] = __ldg(lcp + lb + l);
+                fa_[r] = (double)__ldg(fa + lb + l); fi_[r] = (double)__ldg(fib + lb + l);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) {
+            const int l = l0 + r;
+            if (l < N) {
+                const double xp = xn[r];
+                double ax = (1.0 + h * (cm[r] + cp[r])) * xc;
+                if (l > 0) ax -= h * cm[r] * xm;
+                if (l + 1 < N) ax -= h * cp[r] * xp;
+                y = (bb[r] - ax - fa_[r] * y) * fi_[r];
+                yb[e0 + l * rst] = (float)y;
+                xm = xc;
+                xc = xp;
+            }
+        }
     }
     // back substitution of the correction, added to x (x_{N-1} first)
     double d = y;
     long long e = e0 + (long long)(N - 1) * rst;
     x[e] = (float)((double)x[e] + d);
-    for (int l = N - 2; l >= 0; --l) {
-        e -= rst;
-        d = (double)yb[e] - (double)__ldg(fcu + lb + l) * d;
-        x[e] = (float)((double)x[e] + d);
+    for (int l1 = N - 2; l1 >= 0; l1 -= kRB) {
+        float yv[kRB], xv[kRB];
+        double cu[kRB];
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) {
+            const int l = l1 - r;
+            if (l >= 0) {
+                const long long el = e0 + (long long)l * rst;
+                yv[r] = yb[el]; xv[r] = x[el]; cu[r] = (double)__ldg(fcu + lb + l);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) {
+            const int l = l1 - r;
+            if (l >= 0) {
+                d = (double)yv[r] - cu[r] * d;
+                x[e0 + (long long)l * rst] = (float)((double)xv[r] + d);
+            }
+        }
     }
 }
 
@@ -1480,3 +1544,6 @@ int gw_fused_prepare_refine(gw_ctx *c) {
         return gw_fail(GW_ERR_ARG, "GW_MIXED_REFINE needs a fused GW_PREC_MIXED context");
     return GW_OK;
 }
+
+// debug build: point this translation unit's checks at the allocation registry
+GW_DEBUG_BIND(gw_debug_bind_fused)

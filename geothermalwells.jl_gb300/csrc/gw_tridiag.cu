@@ -19,6 +19,10 @@
 
 namespace {
 
+// Rows are processed in batches of kB: a batch's loads (independent of the
+// recurrences) issue together ahead of the dependent chain.
+constexpr int kB = 8;
+
 __global__ void __launch_bounds__(128) k_tri_f64(const double *__restrict__ a, const double *__restrict__ b,
                                                  const double *__restrict__ c, const double *__restrict__ d,
                                                  double *__restrict__ x, double *__restrict__ cs,
@@ -30,20 +34,40 @@ __global__ void __launch_bounds__(128) k_tri_f64(const double *__restrict__ a, c
     const long long o = goff[g] + lane;
     const int L = glen[g];
     double cp = 0.0, dp = 0.0;
-    for (int r = 0; r < L; ++r) {
-        const long long e = o + 32LL * r;
-        const double ar = a[e];
-        const double rden = 1.0 / fma(-ar, cp, b[e]);
-        cp = c[e] * rden;
-        dp = fma(-ar, dp, d[e]) * rden;
-        cs[e] = cp;
-        x[e] = dp;
+    for (int r0 = 0; r0 < L; r0 += kB) {
+        double av[kB], bv[kB], cv[kB], dv[kB];
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 + u < L) {
+                const long long e = o + 32LL * (r0 + u);
+                av[u] = a[e]; bv[u] = b[e]; cv[u] = c[e]; dv[u] = d[e];
+            }
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 + u < L) {
+                const long long e = o + 32LL * (r0 + u);
+                const double rden = 1.0 / fma(-av[u], cp, bv[u]);
+                cp = cv[u] * rden;
+                dp = fma(-av[u], dp, dv[u]) * rden;
+                cs[e] = cp;
+                x[e] = dp;
+            }
     }
     double xn = dp;
-    for (int r = L - 2; r >= 0; --r) {
-        const long long e = o + 32LL * r;
-        xn = fma(-cs[e], xn, x[e]);
-        x[e] = xn;
+    for (int r0 = L - 2; r0 >= 0; r0 -= kB) {
+        double cv[kB], xv[kB];
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 - u >= 0) {
+                const long long e = o + 32LL * (r0 - u);
+                cv[u] = cs[e]; xv[u] = x[e];
+            }
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 - u >= 0) {
+                xn = fma(-cv[u], xn, xv[u]);
+                x[o + 32LL * (r0 - u)] = xn;
+            }
     }
 }
 
@@ -61,22 +85,42 @@ __global__ void __launch_bounds__(128) k_tri_mix1(const double *__restrict__ a, 
     const int L = glen[g];
     float *fc = fs, *fr = fs + n, *fd = fs + 2 * n;
     float cp = 0.f, dp = 0.f;
-    for (int r = 0; r < L; ++r) {
-        const long long e = o + 32LL * r;
-        const float ar = (float)a[e];
-        const float rden = 1.0f / fmaf(-ar, cp, (float)b[e]);
-        cp = (float)c[e] * rden;
-        dp = fmaf(-ar, dp, (float)d[e]) * rden;
-        fc[e] = cp;
-        fr[e] = rden;
-        fd[e] = dp;
+    for (int r0 = 0; r0 < L; r0 += kB) {
+        float av[kB], bv[kB], cv[kB], dv[kB];
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 + u < L) {
+                const long long e = o + 32LL * (r0 + u);
+                av[u] = (float)a[e]; bv[u] = (float)b[e]; cv[u] = (float)c[e]; dv[u] = (float)d[e];
+            }
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 + u < L) {
+                const long long e = o + 32LL * (r0 + u);
+                const float rden = 1.0f / fmaf(-av[u], cp, bv[u]);
+                cp = cv[u] * rden;
+                dp = fmaf(-av[u], dp, dv[u]) * rden;
+                fc[e] = cp;
+                fr[e] = rden;
+                fd[e] = dp;
+            }
     }
     float xn = dp;
     x[o + 32LL * (L - 1)] = (double)xn;
-    for (int r = L - 2; r >= 0; --r) {
-        const long long e = o + 32LL * r;
-        xn = fmaf(-fc[e], xn, fd[e]);
-        x[e] = (double)xn;
+    for (int r0 = L - 2; r0 >= 0; r0 -= kB) {
+        float cv[kB], dv[kB];
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 - u >= 0) {
+                const long long e = o + 32LL * (r0 - u);
+                cv[u] = fc[e]; dv[u] = fd[e];
+            }
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 - u >= 0) {
+                xn = fmaf(-cv[u], xn, dv[u]);
+                x[o + 32LL * (r0 - u)] = (double)xn;
+            }
     }
 }
 
@@ -95,21 +139,43 @@ __global__ void __launch_bounds__(128) k_tri_mix2(const double *__restrict__ a, 
     float *fe = fs + 2 * n;   // reuses the d' slot for the correction's forward values
     double xm = 0.0, xc = x[o];
     float ep = 0.f;
-    for (int r = 0; r < L; ++r) {
-        const long long e = o + 32LL * r;
-        const double xp = r + 1 < L ? x[e + 32] : 0.0;
-        const double res = d[e] - fma(a[e], xm, fma(b[e], xc, c[e] * xp));
-        ep = fmaf(-(float)a[e], ep, (float)res) * fr[e];
-        fe[e] = ep;
-        xm = xc;
-        xc = xp;
+    for (int r0 = 0; r0 < L; r0 += kB) {
+        double av[kB], bv[kB], cv[kB], dv[kB], xp[kB];
+        float rv[kB];
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 + u < L) {
+                const long long e = o + 32LL * (r0 + u);
+                av[u] = a[e]; bv[u] = b[e]; cv[u] = c[e]; dv[u] = d[e]; rv[u] = fr[e];
+                xp[u] = r0 + u + 1 < L ? x[e + 32] : 0.0;
+            }
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 + u < L) {
+                const double res = dv[u] - fma(av[u], xm, fma(bv[u], xc, cv[u] * xp[u]));
+                ep = fmaf(-(float)av[u], ep, (float)res) * rv[u];
+                fe[o + 32LL * (r0 + u)] = ep;
+                xm = xc;
+                xc = xp[u];
+            }
     }
     float en = ep;
     x[o + 32LL * (L - 1)] += (double)en;
-    for (int r = L - 2; r >= 0; --r) {
-        const long long e = o + 32LL * r;
-        en = fmaf(-fc[e], en, fe[e]);
-        x[e] += (double)en;
+    for (int r0 = L - 2; r0 >= 0; r0 -= kB) {
+        float cv[kB], ev[kB];
+        double xv[kB];
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 - u >= 0) {
+                const long long e = o + 32LL * (r0 - u);
+                cv[u] = fc[e]; ev[u] = fe[e]; xv[u] = x[e];
+            }
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (r0 - u >= 0) {
+                en = fmaf(-cv[u], en, ev[u]);
+                x[o + 32LL * (r0 - u)] = xv[u] + (double)en;
+            }
     }
 }
 

@@ -9,7 +9,9 @@ import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 PKG_ROOT = os.path.dirname(_HERE)
-LIB_PATH = os.path.join(PKG_ROOT, "lib", "libgw_gb300.so")
+# GW_LIB selects another build of the library (the bounds-checking debug
+# build, lib/libgw_gb300_debug.so)
+LIB_PATH = os.environ.get("GW_LIB") or os.path.join(PKG_ROOT, "lib", "libgw_gb300.so")
 
 GW_OK, GW_ERR_ARG, GW_ERR_CUDA, GW_ERR_NONFINITE, GW_ERR_TIMEOUT, GW_ERR_UNSUPPORTED = range(6)
 GW_PREC_FP64, GW_PREC_MIXED = 0, 1

@@ -30,10 +30,19 @@ def nvcc():
     return exe
 
 
-def _compile(src, verbose):
-    obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
+# The debug build (-DGW_DEBUG, lib/libgw_gb300_debug.so): the fused step's
+# kernels check every global and shared-memory access (csrc/gw_debug.cuh) and
+# report a failed check as GW_ERR_ARG instead of touching the address.
+DEBUG_LIB = os.path.join(OUT_DIR, "libgw_gb300_debug.so")
+DEBUG_OBJ_DIR = os.path.join(HERE, "_build_debug")
+
+
+def _compile(src, verbose, debug=False):
+    obj = os.path.join(DEBUG_OBJ_DIR if debug else OBJ_DIR, os.path.basename(src) + ".o")
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
            "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj]
+    if debug:
+        cmd.insert(1, "-DGW_DEBUG")
     if src.endswith(".cpp"):
         cmd[cmd.index("-c"):cmd.index("-c")] = ["-x", "cu"]
     if verbose:
@@ -44,34 +53,36 @@ def _compile(src, verbose):
     return obj, r.stdout + r.stderr
 
 
-def _stale():
-    if not os.path.exists(LIB):
+def _stale(lib=LIB):
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     deps.append(os.path.join(os.path.dirname(HERE), "include", "gw_gb300.h"))
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def build(force=False, verbose=False):
-    """Compile the library if any source is newer than it; returns its path."""
-    if not force and not _stale():
-        return LIB
-    os.makedirs(OBJ_DIR, exist_ok=True)
+def build(force=False, verbose=False, debug=False):
+    """Compile the library (debug=True: the bounds-checking debug build) if
+    any source is newer than it; returns its path."""
+    lib = DEBUG_LIB if debug else LIB
+    if not force and not _stale(lib):
+        return lib
+    os.makedirs(DEBUG_OBJ_DIR if debug else OBJ_DIR, exist_ok=True)
     os.makedirs(OUT_DIR, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+        results = list(ex.map(lambda s: _compile(s, verbose, debug), SOURCES))
     if verbose:
         for _, log in results:
             sys.stderr.write(log)
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", tmp] + [o for o, _ in results]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc link failed:\n%s%s" % (r.stdout, r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, debug="--debug" in sys.argv))
