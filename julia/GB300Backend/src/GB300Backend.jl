@@ -64,7 +64,8 @@ import ChainRulesCore
 import JLD2
 using Libdl
 
-export GB300, GB300Cache, GB300Field, ScheduleInlet, AdjointDesign, outlet_series, extracted_heat
+export GB300, GB300Cache, GB300Field, ScheduleInlet, ExpressionInlet, AdjointDesign, outlet_series,
+       extracted_heat, set_mixed_options!
 
 # ---------------------------------------------------------------------------
 # the library
@@ -98,6 +99,11 @@ function check(rc)
 end
 
 const GW_INLET_CONSTANT, GW_INLET_HEAT_EXCHANGER, GW_INLET_SCHEDULE = 0, 1, 2
+const GW_INLET_EXPRESSION = 3
+# postfix operations of an expression inlet (GW_OP_* of the header)
+const GW_OP_CONST, GW_OP_TOUT, GW_OP_TIME, GW_OP_BH, GW_OP_SCHED, GW_OP_NEG = 0, 1, 2, 3, 4, 5
+const GW_OP_ADD, GW_OP_SUB, GW_OP_MUL, GW_OP_DIV, GW_OP_MIN, GW_OP_MAX = 6, 7, 8, 9, 10, 11
+const GW_MIXED_ROCK2_F64, GW_MIXED_REFINE = 1, 2
 const GW_DIR = (x = Cint(0), y = Cint(1), z = Cint(2))
 
 # ---------------------------------------------------------------------------
@@ -190,6 +196,103 @@ function (m::ScheduleInlet)(bh_idx, T_outlet_values, t)
 end
 
 """
+    ExpressionInlet(ex; schedule = nothing)
+
+A `CustomInlet` whose closure `(bh, T_outlet, t) -> T_in` is arithmetic: the
+expression `ex` (a quoted Julia expression) over `T_out` (the borehole's
+outlet temperature, `T_outlet[bh]`), `t`, `bh` (1-based, as in Julia),
+numbers, `+ - * /`, unary `-`, `min`, `max` and `sched(x)` (the optional
+piecewise-linear `schedule = (times, values)` at `x`).  A heat pump that takes
+ΔT(t) out of the outlet but never cools the inlet below 5 °C:
+
+    ExpressionInlet(:(max(5.0, T_out - sched(t))); schedule = ([0.0, 3600.0], [3.0, 6.0]))
+
+It is compiled to the postfix program of `GW_INLET_EXPRESSION`
+(`gw_set_inlet_program`), which the GPU evaluates in double where the
+reference calls the inlet model (`src/solver.jl:349-350`); calling the object
+evaluates the same program on the host, so it also runs on the reference's
+`CPU()` backend.
+"""
+struct ExpressionInlet <: GeothermalWells.AbstractInletModel
+    ex::Any
+    ops::Vector{Cint}
+    args::Vector{Float64}
+    schedule::Union{Nothing,ScheduleInlet}
+end
+
+function ExpressionInlet(ex; schedule = nothing)
+    sched = schedule === nothing ? nothing : ScheduleInlet(schedule[1], schedule[2])
+    ops, args = Cint[], Float64[]
+    emit(op, a = 0.0) = (push!(ops, op); push!(args, Float64(a)); nothing)
+    binops = Dict(:+ => GW_OP_ADD, :- => GW_OP_SUB, :* => GW_OP_MUL, :/ => GW_OP_DIV)
+    function walk(n)
+        n isa Real && !(n isa Bool) && return emit(GW_OP_CONST, n)
+        n === :T_out && return emit(GW_OP_TOUT)
+        n === :t && return emit(GW_OP_TIME)
+        if n === :bh   # 1-based in Julia: the library's index is 0-based
+            emit(GW_OP_BH); emit(GW_OP_CONST, 1.0); return emit(GW_OP_ADD)
+        end
+        n isa Expr && n.head === :call || throw(ArgumentError("unsupported element in the inlet expression: $n"))
+        f, a = n.args[1], n.args[2:end]
+        if f === :- && length(a) == 1
+            walk(a[1]); return emit(GW_OP_NEG)
+        elseif f === :+ && length(a) == 1
+            return walk(a[1])
+        elseif haskey(binops, f) && length(a) >= 2
+            walk(a[1])
+            for x in a[2:end]   # Julia folds a + b + c into one call
+                walk(x); emit(binops[f])
+            end
+            return nothing
+        elseif f in (:min, :max) && length(a) >= 2
+            walk(a[1])
+            for x in a[2:end]
+                walk(x); emit(f === :min ? GW_OP_MIN : GW_OP_MAX)
+            end
+            return nothing
+        elseif f === :sched && length(a) == 1
+            sched === nothing && throw(ArgumentError("sched(...) needs ExpressionInlet(ex; schedule = (times, values))"))
+            walk(a[1]); return emit(GW_OP_SCHED)
+        end
+        throw(ArgumentError("unsupported call in the inlet expression: $n"))
+    end
+    walk(ex)
+    depth, top = 0, 0
+    for o in ops
+        depth += o <= GW_OP_BH ? 1 : (o <= GW_OP_NEG ? 0 : -1)
+        top = max(top, depth)
+    end
+    (length(ops) > 64 || top > 16) &&
+        throw(ArgumentError("inlet expression too long (at most 64 operations, stack depth 16)"))
+    return ExpressionInlet(ex, ops, args, sched)
+end
+
+function (m::ExpressionInlet)(bh_idx, T_outlet_values, t)
+    st = Float64[]
+    for (o, a) in zip(m.ops, m.args)
+        if o == GW_OP_CONST
+            push!(st, a)
+        elseif o == GW_OP_TOUT
+            push!(st, Float64(T_outlet_values[bh_idx]))
+        elseif o == GW_OP_TIME
+            push!(st, Float64(t))
+        elseif o == GW_OP_BH
+            push!(st, Float64(bh_idx - 1))
+        elseif o == GW_OP_SCHED
+            st[end] = m.schedule(bh_idx, T_outlet_values, st[end])
+        elseif o == GW_OP_NEG
+            st[end] = -st[end]
+        else
+            b = pop!(st)
+            x = st[end]
+            st[end] = o == GW_OP_ADD ? x + b : o == GW_OP_SUB ? x - b : o == GW_OP_MUL ? x * b :
+                      o == GW_OP_DIV ? (b == 0 ? Inf : x / b) : o == GW_OP_MIN ? min(x, b) : max(x, b)
+        end
+    end
+    return st[1]
+end
+
+"""
 The cache `create_cache(; backend = GB300(), ...)` returns: the library
 context plus the fields the reference's functions read from their cache
 (`src/cache.jl:55-116`), so `ADI_and_ADV_callback!` and `eigen_estimator`
@@ -240,6 +343,20 @@ function info(c::GB300Cache)
     return r[]
 end
 
+"""
+    set_mixed_options!(cache; rock2_f64 = false, refine = false)
+
+The mixed step's two optional double-precision parts (`gw_set_mixed_options`):
+`rock2_f64` accumulates the ROCK2 stages in double over the float field,
+`refine` follows every float line solve with its residual in double and one
+correction solve.  FP64 contexts ignore them.
+"""
+function set_mixed_options!(c::GB300Cache; rock2_f64::Bool = false, refine::Bool = false)
+    flags = (rock2_f64 ? GW_MIXED_ROCK2_F64 : 0) | (refine ? GW_MIXED_REFINE : 0)
+    check(ccall(fn(:gw_set_mixed_options), Cint, (Ptr{Cvoid}, Cint), c.ctx, flags))
+    return c
+end
+
 function destroy!(c::GB300Cache)
     if getfield(c, :ctx) != C_NULL
         ccall(fn(:gw_destroy), Cint, (Ptr{Cvoid},), getfield(c, :ctx))
@@ -256,8 +373,10 @@ rock_layers(m::GeothermalWells.StratifiedMaterialProperties) =
 inlet_kind(m::GeothermalWells.ConstantInlet) = (GW_INLET_CONSTANT, Float64(m.T_const))
 inlet_kind(m::GeothermalWells.HeatExchangerInlet) = (GW_INLET_HEAT_EXCHANGER, Float64(m.ΔT))
 inlet_kind(m::ScheduleInlet) = (GW_INLET_SCHEDULE, 0.0)
+inlet_kind(m::ExpressionInlet) = (GW_INLET_EXPRESSION, 0.0)
 inlet_kind(::GeothermalWells.CustomInlet) =
-    throw(ArgumentError("CustomInlet closures cannot cross the C ABI; tabulate T_in(t) as a ScheduleInlet"))
+    throw(ArgumentError("CustomInlet closures cannot cross the C ABI; write T_in as a ScheduleInlet " *
+                        "(T_in(t)) or an ExpressionInlet (arithmetic in T_out, t, bh)"))
 
 """
     create_cache(; backend, gridx, gridy, gridz, materials, boreholes, inlet_model)
@@ -285,9 +404,15 @@ function create_cache(; backend, gridx, gridy, gridz, materials, boreholes, inle
                      backend.precision === :mixed ? 1 : 0, backend.device))
         check(ccall(fn(:gw_create), Cint, (Ref{Desc}, Ref{Ptr{Cvoid}}), d, ctx))
     end
-    if inlet_model isa ScheduleInlet
+    sched = inlet_model isa ScheduleInlet ? inlet_model :
+            inlet_model isa ExpressionInlet ? inlet_model.schedule : nothing
+    if sched !== nothing
         check(ccall(fn(:gw_set_inlet_schedule), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ptr{Cdouble}),
-                    ctx[], length(inlet_model.times), inlet_model.times, inlet_model.values))
+                    ctx[], length(sched.times), sched.times, sched.values))
+    end
+    if inlet_model isa ExpressionInlet
+        check(ccall(fn(:gw_set_inlet_program), Cint, (Ptr{Cvoid}, Cint, Ptr{Cint}, Ptr{Cdouble}),
+                    ctx[], length(inlet_model.ops), inlet_model.ops, inlet_model.args))
     end
     r = Ref{GwInfo}()
     check(ccall(fn(:gw_get_info), Cint, (Ptr{Cvoid}, Ref{GwInfo}), ctx[], r))
@@ -569,7 +694,10 @@ end
 function save!(cb::GB300Callback, cache::GB300Cache, t)
     T = zeros(Float64, cache.Nz, cache.Ny, cache.Nx)
     check(ccall(fn(:gw_get_field), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), cache.ctx, T))
-    u = Float32.(T)
+    save!(cb, t, Float32.(T))
+end
+
+function save!(cb::GB300Callback, t, u::Array{Float32,3})
     if cb.write_to_jld
         isdir(cb.data_folder_dir) || mkdir(cb.data_folder_dir)
         cb.file_counter[] += 1
@@ -632,8 +760,18 @@ function SciMLBase.solve(prob::SciMLBase.ODEProblem{<:Array{Float64,3},<:Any,tru
         end
         union!(stops, keys(save_steps))
         callback.print_every_n > 0 && union!(stops, callback.print_every_n:callback.print_every_n:nsteps)
-        haskey(save_steps, 0) && save!(callback, cache, save_steps[0])
     end
+    # saved fields: Float32 snapshots converted on the device and copied to
+    # pinned host buffers on a second stream while the next steps run
+    # (gw_snapshot); handed to the callback once every copy has landed
+    snaps = Tuple{Float64,Ptr{Cfloat}}[]
+    function snapshot(ts)
+        ptr = Ref{Ptr{Cfloat}}(C_NULL)
+        check(ccall(fn(:gw_snapshot_host_alloc), Cint, (Ptr{Cvoid}, Ref{Ptr{Cfloat}}), cache.ctx, ptr))
+        push!(snaps, (ts, ptr[]))
+        check(ccall(fn(:gw_snapshot), Cint, (Ptr{Cvoid}, Ptr{Cfloat}), cache.ctx, ptr[]))
+    end
+    haskey(save_steps, 0) && snapshot(save_steps[0])
     series = Matrix{Float64}[]
     done = 0
     for stop in sort!(collect(filter(>(0), stops)))
@@ -646,7 +784,15 @@ function SciMLBase.solve(prob::SciMLBase.ODEProblem{<:Array{Float64,3},<:Any,tru
         done = stop
         if callback !== nothing
             callback.print_every_n > 0 && done % callback.print_every_n == 0 && print_step(done, t0 + done * dt)
-            haskey(save_steps, done) && save!(callback, cache, save_steps[done])
+            haskey(save_steps, done) && snapshot(save_steps[done])
+        end
+    end
+    if !isempty(snaps)
+        check(ccall(fn(:gw_snapshot_wait), Cint, (Ptr{Cvoid},), cache.ctx))
+        for (ts, ptr) in snaps
+            u = copy(unsafe_wrap(Array, ptr, (cache.Nz, cache.Ny, cache.Nx)))
+            check(ccall(fn(:gw_snapshot_host_free), Cint, (Ptr{Cvoid}, Ptr{Cfloat}), cache.ctx, ptr))
+            save!(callback, ts, u)
         end
     end
     energy = zeros(Float64, cache.N_bh)
