@@ -342,6 +342,10 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
     // the same values bitwise; tests compare the two paths)
     const char *hs = std::getenv("GW_HOST_SETUP");
     c->host_setup = hs && *hs && *hs != '0';
+    // the mixed step's ROCK2 on the block kernel instead of the window kernel
+    // (the two give the same field bitwise; tests compare them)
+    const char *rb = std::getenv("GW_ROCK2_BLOCK");
+    c->rock2_block = rb && *rb && *rb != '0';
     int rc = gw_setup_host(c, desc);
     if (rc) { delete c; return rc; }
     if (c->nbh > 1024) { delete c; return gw_fail(GW_ERR_ARG, "at most 1024 boreholes"); }

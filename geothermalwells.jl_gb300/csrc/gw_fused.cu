@@ -309,6 +309,189 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) 
     }
 }
 
+// Mixed path, ROCK2 by windows: the same stages as k_rock2_reg<float, true>,
+// level for level the same arithmetic, without block barriers.  A warp owns a
+// window of W = 32 LPT consecutive levels of a column (lane l: levels
+// ws + l LPT + i) and exchanges run ends with warp shuffles.  A window's
+// outermost level has no neighbour outside the window; the error that leaves
+// there reaches one level further inward per A evaluation, i.e. s - 1 levels
+// over the s evaluations of an s-stage step (F0 and the stages reuse the
+// start value).  So interior windows overlap by 2 s levels and store only
+// their levels at least s from an interior edge.  Window w starts at level
+// w (W - 2 s); the last window reaches the column's end (padding levels are
+// zero-filled with zero coefficients, as in k_rock2_reg).
+// Warps are independent: warp g of the grid owns window g % nwin of its
+// columns (every (g / nwin)-th of the profile-sorted order, so the window's
+// coefficient rows stay in registers), and streams them through a private
+// ring of NB staging buffers (NB - 1 windows in flight) with cp.async.
+// S3: the instance for s = 3 (one recurrence stage, no g_{j-2} to keep).
+template <int LPT, int NB, bool S3>
+__global__ void __launch_bounds__(256, 3) k_rock2_win(float *__restrict__ u, const int *__restrict__ order,
+                                                      const int *__restrict__ colprof,
+                                                      const float *__restrict__ czm,
+                                                      const float *__restrict__ czp,
+                                                      const float *__restrict__ fref,
+                                                      const float *__restrict__ sc, int s, int nz,
+                                                      int ncols, int nwin) {
+    constexpr int W = 32 * LPT;
+    constexpr int WS = W + W / 32;   // padded slots of one staging buffer
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int g = blockIdx.x * (blockDim.x >> 5) + wib;
+    const int slots = gridDim.x * (blockDim.x >> 5) / nwin;   // column slots
+    if (g >= slots * nwin) return;   // warps beyond the last whole set of windows
+    const int w = g % nwin;
+    const int slot = g / nwin;
+    float *ring = reinterpret_cast<float *>(smem_raw) + (size_t)wib * NB * WS;
+    const int ws = w * (W - 2 * s);                      // first level of the window
+    const int lo = w == 0 ? 0 : ws + s;                  // stored levels [lo, hi)
+    const int hi = w == nwin - 1 ? nz : ws + W - s;
+    const int kb = ws + lane * LPT;                      // this lane's run
+    const int nrec = S3 ? 1 : s - 2;
+    const unsigned FULL = 0xffffffffu;
+    // lane l copies window levels l + 32 i into slots spad(l + 32 i)
+    auto fetch = [&](int col, int buf) {
+        float *d = ring + (size_t)buf * WS;
+        const float *gcol = u + (size_t)col * nz;
+#pragma unroll
+        for (int i = 0; i < LPT; ++i) {
+            const int j = lane + 32 * i, k = ws + j;
+            const bool ok = k < nz;
+            if (GW_OK_D(d + spad(j), smem_raw, 220) && (!ok || GW_OK_G(gcol + k, 221)))
+                cp_async<4>(d + spad(j), ok ? (const void *)(gcol + k) : (const void *)gcol, ok);
+        }
+    };
+    auto exchange = [&](const float (&v)[LPT], float &left, float &right) {
+        const float a = __shfl_up_sync(FULL, v[LPT - 1], 1);
+        const float b = __shfl_down_sync(FULL, v[0], 1);
+        left = lane == 0 ? 0.f : a;
+        right = lane == 31 ? 0.f : b;
+    };
+    auto apply = [&](const float (&v)[LPT], const float (&cm)[LPT], const float (&cp)[LPT], int i,
+                     float left, float right) {
+        const float gc = v[i];
+        const float gm = i == 0 ? left : v[i > 0 ? i - 1 : 0];
+        const float gp = i + 1 < LPT ? v[i + 1 < LPT ? i + 1 : i] : right;
+        return cp[i] * (gp - gc) - cm[i] * (gc - gm);
+    };
+    const int stride = slots;
+    int it = slot;
+    // columns (and profiles) of the items it + q stride, q < NB; the column of
+    // item it + NB stride is read one item ahead of its fetch
+    int cq[NB];
+    int pq[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+        const long long iq = it + (long long)q * stride;
+        cq[q] = iq < ncols && GW_OK_G(order + iq, 222) ? order[iq] : -1;
+    }
+#pragma unroll
+    for (int q = 0; q < NB - 1; ++q) {
+        pq[q] = cq[q] >= 0 && GW_OK_G(colprof + cq[q], 223) ? colprof[cq[q]] : 0;
+        if (cq[q] >= 0) fetch(cq[q], q);
+        cp_async_commit();
+    }
+    float cm[LPT], cp[LPT], fr[LPT];
+    int pcur = -1, buf = 0, bnext = NB - 1;
+    for (; it < ncols; it += stride) {
+        // the item NB - 1 ahead goes into the buffer the previous item used
+        __syncwarp();
+        if (cq[NB - 1] >= 0) fetch(cq[NB - 1], bnext);
+        cp_async_commit();
+        pq[NB - 1] = cq[NB - 1] >= 0 && GW_OK_G(colprof + cq[NB - 1], 223) ? colprof[cq[NB - 1]] : 0;
+        const long long iahead = it + (long long)NB * stride;
+        const int cahead = iahead < ncols && GW_OK_G(order + iahead, 222) ? order[iahead] : -1;
+        const int col = cq[0];
+        const int p = pq[0];
+        if (p != pcur) {   // warp-uniform
+            pcur = p;
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) {
+                const bool ok = kb + i < nz;
+                const size_t q = (size_t)p * nz + kb + i;
+                cm[i] = ok && GW_OK_G(czm + q, 224) ? __ldg(czm + q) : 0.f;
+                cp[i] = ok && GW_OK_G(czp + q, 224) ? __ldg(czp + q) : 0.f;
+                fr[i] = fref && ok && GW_OK_G(fref + q, 225) ? __ldg(fref + q) : 0.f;
+            }
+        }
+        cp_async_wait<NB - 1>();
+        __syncwarp();
+        float *st = ring + (size_t)buf * WS;
+        float F0[LPT], prev[LPT], cur[LPT];
+        float left, right;
+        {   // the start values are read again from st at the end
+            float base[LPT];
+#pragma unroll
+            for (int i = 0; i < LPT; ++i)
+                base[i] = GW_OK_D(st + spad(lane * LPT + i), smem_raw, 226) ? st[spad(lane * LPT + i)] : 0.f;
+            exchange(base, left, right);
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) {
+                F0[i] = fr[i] + apply(base, cm, cp, i, left, right);
+                prev[i] = 0.f;
+                cur[i] = 0.f;
+            }
+        }
+        // increment form: g = base + delta, A g = F0 + A delta
+        for (int j = 0; j < nrec; ++j) {
+            const float hmu = sc[2 * j], kap = sc[2 * j + 1];
+            if (j == 0) {
+#pragma unroll
+                for (int i = 0; i < LPT; ++i) { prev[i] = cur[i]; cur[i] = hmu * F0[i]; }
+                continue;
+            }
+            exchange(cur, left, right);
+            float out[LPT];
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) {
+                float a = apply(cur, cm, cp, i, left, right);
+                a += F0[i];
+                out[i] = cur[i] + hmu * a + kap * (cur[i] - prev[i]);
+            }
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) { prev[i] = cur[i]; cur[i] = out[i]; }
+        }
+        const float hs = sc[2 * nrec], hts = sc[2 * nrec + 1], c3 = sc[2 * nrec + 2];
+        float q[LPT];
+        if (nrec == 0) {
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) q[i] = hs * F0[i];
+        } else {
+            exchange(cur, left, right);
+#pragma unroll
+            for (int i = 0; i < LPT; ++i) {
+                float a = apply(cur, cm, cp, i, left, right);
+                a += F0[i];
+                q[i] = cur[i] + hs * a;
+            }
+        }
+        exchange(q, left, right);
+        // each lane updates its own run's slots: start value + increment
+#pragma unroll
+        for (int i = 0; i < LPT; ++i) {
+            float a = apply(q, cm, cp, i, left, right);
+            a += F0[i];
+            const float y = q[i] + hts * a + c3 * (q[i] - cur[i]);
+            if (GW_OK_D(st + spad(lane * LPT + i), smem_raw, 226))
+                st[spad(lane * LPT + i)] = st[spad(lane * LPT + i)] + y;
+        }
+        __syncwarp();
+        float *uc = u + (size_t)col * nz;
+#pragma unroll
+        for (int i = 0; i < LPT; ++i) {
+            const int j = lane + 32 * i, k = ws + j;
+            if (k >= lo && k < hi && GW_OK_G(uc + k, 227) && GW_OK_D(st + spad(j), smem_raw, 226))
+                uc[k] = st[spad(j)];
+        }
+#pragma unroll
+        for (int q2 = 0; q2 < NB - 1; ++q2) { cq[q2] = cq[q2 + 1]; pq[q2] = pq[q2 + 1]; }
+        cq[NB - 1] = cahead;
+        buf = buf + 1 == NB ? 0 : buf + 1;
+        bnext = bnext + 1 == NB ? 0 : bnext + 1;
+    }
+    cp_async_wait<0>();
+}
+
 // ---------------------------------------------------------------------------
 // 2. pipe columns
 
@@ -1137,12 +1320,59 @@ const double *stage_table<double>(gw_ctx *c) { return c->d_stage; }
 template <>
 const float *stage_table<float>(gw_ctx *c) { return c->f_stage; }
 
+// Window kernel: staging buffers per warp, warps per block.
+constexpr int kWinNB = 3, kWinWarps = 8;
+inline size_t win_smem(int lpt) { return (size_t)kWinWarps * kWinNB * (32 * lpt + lpt) * sizeof(float); }
+
+// Levels per lane and window count of k_rock2_win for nz levels and s stages:
+// among 4..8 levels per lane, the fewest padded levels (windows x W); 0 when
+// the halo (s levels per interior edge) would exceed a quarter of the window.
+inline int rock2_win_lpt(int nz, int s, int *nwin) {
+    int best = 0, bn = 0;
+    long long bw = 0;
+    for (int L = 8; L >= 4; --L) {
+        const int W = 32 * L;
+        if (8 * s > W) continue;
+        const int n = nz <= W ? 1 : 1 + (nz - W + (W - 2 * s) - 1) / (W - 2 * s);
+        if (n > 64) continue;
+        if (!best || (long long)n * W < bw) { best = L; bn = n; bw = (long long)n * W; }
+    }
+    *nwin = bn;
+    return best;
+}
+
+template <int LPT>
+int launch_rock2_win(gw_ctx *c, int s, int nwin, float *u, const float *czm, const float *czp,
+                     const float *fref, const int *order, long long ncols) {
+    auto kern = s == 3 ? k_rock2_win<LPT, kWinNB, true> : k_rock2_win<LPT, kWinNB, false>;
+    const long long per_sm = c->rock2w_per_sm[LPT] > 0 ? c->rock2w_per_sm[LPT] : 1;
+    const long long need = (ncols * nwin + kWinWarps - 1) / kWinWarps;   // one warp per window
+    long long grid = std::min(per_sm * c->sms, need);
+    grid = std::max(grid, (long long)(nwin + kWinWarps - 1) / kWinWarps);   // one whole set of windows
+    kern<<<(unsigned)grid, 32 * kWinWarps, win_smem(LPT), c->stream>>>(
+        u, order, c->d_colprof, czm, czp, fref, c->f_stage, s, c->nz, (int)ncols, nwin);
+    GW_CUDA(cudaGetLastError());
+    return GW_OK;
+}
+
 template <typename T, bool INC>
 int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *fref,
                    const int *order = nullptr, long long ncols = -1) {
     if (!order) order = c->d_colorder;
     if (ncols < 0) ncols = (long long)c->nx * c->ny;
     if (ncols == 0) return GW_OK;
+    if constexpr (sizeof(T) == 4 && INC) {
+        int nwin = 0;
+        const int wl = c->rock2_block ? 0 : rock2_win_lpt(c->nz, s, &nwin);
+        switch (wl) {
+            case 4: return launch_rock2_win<4>(c, s, nwin, u, czm, czp, fref, order, ncols);
+            case 5: return launch_rock2_win<5>(c, s, nwin, u, czm, czp, fref, order, ncols);
+            case 6: return launch_rock2_win<6>(c, s, nwin, u, czm, czp, fref, order, ncols);
+            case 7: return launch_rock2_win<7>(c, s, nwin, u, czm, czp, fref, order, ncols);
+            case 8: return launch_rock2_win<8>(c, s, nwin, u, czm, czp, fref, order, ncols);
+            default: break;
+        }
+    }
     const int lpt = rock2_lpt(c->nz, sizeof(T) == 4);
     unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid ? ncols : c->rock2_grid);
     switch (lpt) {
@@ -1434,6 +1664,19 @@ int gw_fused_prepare(gw_ctx *c) {
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     if (e != cudaSuccess) return gw_cuda_fail(e, "cudaDeviceGetAttribute");
     c->rock2_grid = (per_sm > 0 ? per_sm : 1) * sms;
+    c->sms = sms;
+    if (mix) {   // the window kernel, per levels-per-lane instance
+        auto occ = [&](auto kern, int L) {
+            int n = 0;
+            const cudaError_t r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, 32 * kWinWarps, win_smem(L));
+            c->rock2w_per_sm[L] = n;
+            return r;
+        };
+        if ((e = occ(k_rock2_win<4, kWinNB, false>, 4)) || (e = occ(k_rock2_win<5, kWinNB, false>, 5)) ||
+            (e = occ(k_rock2_win<6, kWinNB, false>, 6)) || (e = occ(k_rock2_win<7, kWinNB, false>, 7)) ||
+            (e = occ(k_rock2_win<8, kWinNB, false>, 8)))
+            return gw_cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor(k_rock2_win)");
+    }
     return GW_OK;
 }
 

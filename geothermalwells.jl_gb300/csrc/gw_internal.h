@@ -132,6 +132,9 @@ struct gw_ctx {
     double *d_pp = nullptr;           // double path: [ncol][countz] advected pipe values
     int rock2_grid = 0;
     int rock2_nt = 256;               // threads per block of the ROCK2 column kernel
+    int sms = 0;                      // multiprocessors of the context's GPU
+    int rock2w_per_sm[9] = {};        // resident blocks per SM of the window ROCK2 kernel, by LPT
+    bool rock2_block = false;         // mixed ROCK2 on the block kernel (GW_ROCK2_BLOCK), not by windows
     int half_cfg = 0;                 // half-step tiling (gw_fused.cu kTileHW/kTileHR)
     bool fused = false;
     bool host_setup = false;          // tables built on the host (GW_HOST_SETUP), else on the GPU
