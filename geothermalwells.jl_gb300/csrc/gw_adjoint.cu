@@ -750,6 +750,17 @@ int forward_store(gw_ctx *c, const double *un, StepStore<double> &S, double dt, 
     return GW_OK;
 }
 
+// The context's state keeps its columns pz apart (the mixed path's padded
+// level pitch), the adjoint's buffers nz apart: states cross with pitched
+// copies (a plain copy when the pitches agree, as in FP64).
+template <typename T>
+int state_copy(gw_ctx *c, T *dst, int dpitch, const T *src, int spitch) {
+    GW_CUDA(cudaMemcpy2DAsync(dst, (size_t)dpitch * sizeof(T), src, (size_t)spitch * sizeof(T),
+                              (size_t)c->nz * sizeof(T), (size_t)c->nx * c->ny, cudaMemcpyDeviceToDevice,
+                              c->stream));
+    return GW_OK;
+}
+
 // Mixed path: the ROCK2 stages of theta from un (for the conductivity terms),
 // then the fused ROCK2 columns and first half step on the context's state
 // (u* and u1 copied out, the pipe columns of the two advections' inputs kept
@@ -774,11 +785,11 @@ int forward_store(gw_ctx *c, const float *un, StepStore<float> &S, double dt, in
     k_zstage_theta<<<nb, kB, 0, c->stream>>>(S.g[s - 2], gm1, nullptr, c->d_colprof, c->c32.czm, c->c32.czp,
                                              c->f_fref, c->nz, (long long)c->nx * c->ny, (float)(dt * sigma), 0.f);
     GW_CUDA(cudaGetLastError());
-    GW_CUDA(cudaMemcpyAsync(c->f_u, un, bytes, cudaMemcpyDeviceToDevice, c->stream));
     int rc;
-    if ((rc = gw_fused_adjoint_store(c, dt, s, S.tpA, S.tpC))) return rc;
-    GW_CUDA(cudaMemcpyAsync(S.ustar, c->f_u, bytes, cudaMemcpyDeviceToDevice, c->stream));
-    GW_CUDA(cudaMemcpyAsync(S.u1, c->f_temp, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    if ((rc = state_copy(c, c->f_u, c->pz, un, c->nz)) || (rc = gw_fused_adjoint_store(c, dt, s, S.tpA, S.tpC)) ||
+        (rc = state_copy(c, S.ustar, c->nz, (const float *)c->f_u, c->pz)) ||
+        (rc = state_copy(c, S.u1, c->nz, (const float *)c->f_temp, c->pz)))
+        return rc;
     return launch_osum(c);
 }
 
@@ -937,11 +948,11 @@ int adjoint_run(gw_ctx *c, double dt, int nsteps, int max_stages, int s, int che
     GW_CUDA(cudaEventRecord(e0, c->stream));
     int rc;
     for (int q = 0; q < nseg; ++q) {
-        GW_CUDA(cudaMemcpyAsync(ckpt[q], u, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        if ((rc = state_copy(c, ckpt[q], c->nz, (const T *)u, c->pz))) return rc;
         const int n = std::min(K, nsteps - q * K);
         if ((rc = gw_step(c, (double)q * K * dt, dt, n, max_stages))) return rc;
     }
-    GW_CUDA(cudaMemcpyAsync(uN, u, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    if ((rc = state_copy(c, uN, c->nz, (const T *)u, c->pz))) return rc;
     GW_CUDA(cudaEventRecord(e1, c->stream));
     GW_CUDA(cudaMemcpyAsync(E.data(), c->d_energy, sizeof(double) * c->nbh, cudaMemcpyDeviceToHost, c->stream));
     GW_CUDA(cudaMemcpyAsync(O.data(), c->d_outlet, sizeof(double) * c->nbh, cudaMemcpyDeviceToHost, c->stream));
@@ -957,10 +968,11 @@ int adjoint_run(gw_ctx *c, double dt, int nsteps, int max_stages, int s, int che
     for (int q = nseg - 1; q >= 0; --q) {
         const int n = std::min(K, nsteps - q * K);
         GW_CUDA(cudaMemcpyAsync(seg[0], ckpt[q], bytes, cudaMemcpyDeviceToDevice, c->stream));
-        GW_CUDA(cudaMemcpyAsync(u, ckpt[q], bytes, cudaMemcpyDeviceToDevice, c->stream));
+        if ((rc = state_copy(c, u, c->pz, (const T *)ckpt[q], c->nz))) return rc;
         for (int m = 1; m <= n; ++m) {
-            if ((rc = gw_step(c, (double)(q * K + m - 1) * dt, dt, 1, max_stages))) return rc;
-            GW_CUDA(cudaMemcpyAsync(seg[m], u, bytes, cudaMemcpyDeviceToDevice, c->stream));
+            if ((rc = gw_step(c, (double)(q * K + m - 1) * dt, dt, 1, max_stages)) ||
+                (rc = state_copy(c, seg[m], c->nz, (const T *)u, c->pz)))
+                return rc;
         }
         for (int m = n - 1; m >= 0; --m) {
             const bool last = q * K + m == nsteps - 1;
@@ -981,7 +993,7 @@ int adjoint_run(gw_ctx *c, double dt, int nsteps, int max_stages, int s, int che
         }
     }
     // leave the context as gw_step over nsteps would (field, outlet, energy)
-    GW_CUDA(cudaMemcpyAsync(u, uN, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    if ((rc = state_copy(c, u, c->pz, (const T *)uN, c->nz))) return rc;
     for (int b = 0; b < c->nbh; ++b) E[b] += E0[b];
     GW_CUDA(cudaMemcpyAsync(c->d_energy, E.data(), sizeof(double) * c->nbh, cudaMemcpyHostToDevice, c->stream));
     GW_CUDA(cudaMemcpyAsync(c->d_outlet, O.data(), sizeof(double) * c->nbh, cudaMemcpyHostToDevice, c->stream));

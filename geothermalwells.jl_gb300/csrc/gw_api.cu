@@ -158,6 +158,10 @@ int set_reference_profile(gw_ctx *c, const double *T) {
 }
 }  // namespace
 
+// a device float array owned by the context (freed by gw_destroy; counted in
+// device_bytes; registered with the debug build's bounds checks)
+int gw_dalloc_f(gw_ctx *c, float **p, size_t n) { return dalloc(c, p, n); }
+
 int gw_fail(int code, const std::string &msg) {
     g_err = msg;
     return code;
@@ -320,6 +324,7 @@ int gw_prepare_step(gw_ctx *c, double dt, int s, int nsteps) {
     c->last_nsteps = nsteps;
     if (nsteps == 0) return GW_OK;
     if ((rc = gw_ensure_factors(c, dt / 2))) return rc;
+    if (c->fused && mixed(c) && (rc = gw_fused_refine_tables(c, dt / 2))) return rc;
     if (c->fused && (c->tables_dt != dt || c->tables_s != s)) {
         if ((rc = upload_stages(c, dt, s)) || (rc = gw_fused_set_dt(c, dt))) return rc;
         c->tables_dt = dt;
@@ -346,6 +351,9 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
     // (the two give the same field bitwise; tests compare them)
     const char *rb = std::getenv("GW_ROCK2_BLOCK");
     c->rock2_block = rb && *rb && *rb != '0';
+    // the refinement's residual in double (k_half_refine) instead of double-float
+    const char *rf = std::getenv("GW_REFINE_F64");
+    c->refine_f64 = rf && *rf && *rf != '0';
     int rc = gw_setup_host(c, desc);
     if (rc) { delete c; return rc; }
     if (c->nbh > 1024) { delete c; return gw_fail(GW_ERR_ARG, "at most 1024 boreholes"); }
@@ -479,12 +487,17 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         (rc = dalloc(c, &c->d_nlev, c->nbh)) ||
         (rc = dalloc(c, &c->d_outlet, c->nbh)) || (rc = dalloc(c, &c->d_energy, c->nbh)) ||
         (rc = dalloc(c, &c->d_stage, GW_STAGE_TABLE)) || (rc = dalloc(c, &c->f_stage, GW_STAGE_TABLE)) ||
-        (rc = dalloc(c, &c->d_step_counter, 1)) || (rc = dalloc(c, &c->d_flag, 1)) ||
+        (rc = dalloc(c, &c->d_step_counter, 1)) || (rc = dalloc(c, &c->d_flag, 1)) || (rc = dalloc(c, &c->d_err, 1)) ||
         (rc = dalloc(c, &c->d_time, 2)) || (rc = dalloc(c, &c->d_inlet, c->nbh)))
         return fail(rc);
+    // the mixed path's float fields keep columns pz = nz rounded up to 4 apart,
+    // so every column starts on 16 bytes (tensor-map tiles need 16-byte
+    // strides); the padding levels stay 0 and no kernel reads them
+    c->pz = mixed(c) ? (c->nz + 3) / 4 * 4 : c->nz;
+    const size_t NF = gw_field_slots(c);
     if (mixed(c)) {
         // f_temp and f_g1 are one block, so together they can stage a double field
-        if ((rc = dalloc(c, &c->f_u, N)) || (rc = dalloc(c, &c->f_temp, 2 * N)) ||
+        if ((rc = dalloc(c, &c->f_u, NF)) || (rc = dalloc(c, &c->f_temp, 2 * NF)) ||
             (rc = dalloc(c, &c->f_tp, (size_t)ncol * c->nz)) ||
             (rc = dalloc(c, &c->f_pp, (size_t)ncol * c->countz)) ||
             (rc = dalloc(c, &c->f_fref, (size_t)c->n_profiles * c->nz)) ||
@@ -506,8 +519,9 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
             (rc = dalloc(c, &c->c32.fy.ib, ntab)) || (rc = dalloc(c, &c->c32.fy.cu, ntab)) ||
             (rc = dalloc(c, &c->c32.hx, 4 * ntab)) || (rc = dalloc(c, &c->c32.hy, 4 * ntab)))
             return fail(rc);
-        c->f_g1 = c->f_temp + N;
-        GW_CUDA(cudaMemset(c->f_u, 0, N * sizeof(float)));
+        c->f_g1 = c->f_temp + NF;
+        GW_CUDA(cudaMemset(c->f_u, 0, NF * sizeof(float)));
+        GW_CUDA(cudaMemset(c->f_temp, 0, 2 * NF * sizeof(float)));
         std::vector<double> zero(c->nz, 0.0);
         if ((rc = set_reference_profile(c, zero.data()))) return fail(rc);
     } else {
@@ -520,6 +534,7 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         GW_CUDA(cudaMemset(c->d_u, 0, N * sizeof(double)));
     }
     GW_CUDA(cudaMemset(c->d_outlet, 0, c->nbh * sizeof(double)));
+    GW_CUDA(cudaMemset(c->d_err, 0, sizeof(int)));
     GW_CUDA(cudaMemset(c->d_energy, 0, c->nbh * sizeof(double)));
     c->modular_reason = (gw_fused_supported(c) ? 0 : GW_MODULAR_NZ) |
                         (unique_cols ? 0 : GW_MODULAR_SHARED_COLUMN);
@@ -636,7 +651,7 @@ int gw_init_thermal_gradient(gw_ctx *c, double T_surface, double gradient) {
         // T_ref is the first column, so theta = T - T_ref is exactly 0 everywhere
         if ((rc = set_reference_profile(c, col.data()))) return rc;
         c->tables_dt = -1.0;
-        GW_CUDA(cudaMemsetAsync(c->f_u, 0, ncell(c) * sizeof(float), c->stream));
+        GW_CUDA(cudaMemsetAsync(c->f_u, 0, gw_field_slots(c) * sizeof(float), c->stream));
         return sync(c);
     }
     GW_CUDA(cudaMemcpyAsync(c->d_temp, col.data(), c->nz * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -874,7 +889,7 @@ int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
     GW_CUDA(cudaEventRecord(c->ev0, c->stream));
     for (int n = 0; n < nsteps; ++n) GW_CUDA(cudaGraphLaunch(c->graph, c->stream));
     GW_CUDA(cudaEventRecord(c->ev1, c->stream));
-    if ((rc = sync(c)) || (rc = gw_debug_status(c->device))) return rc;
+    if ((rc = sync(c)) || (rc = gw_debug_status(c->device)) || (rc = gw_fused_status(c))) return rc;
     float ms = 0.f;
     GW_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     c->last_step_ms = ms;
@@ -898,10 +913,9 @@ int gw_profile_kernels(gw_ctx *c, double dt, int reps, double *ms_out) {
     if ((rc = upload_stages(c, dt, s)) || (rc = gw_fused_set_dt(c, dt))) return rc;
     c->tables_dt = dt;
     c->tables_s = s;
-    const size_t N = ncell(c);
     void *u = mixed(c) ? (void *)c->f_u : (void *)c->d_u;
     void *bak = mixed(c) ? (void *)c->f_g1 : (void *)c->d_g1;
-    const size_t bytes = N * (mixed(c) ? sizeof(float) : sizeof(double));
+    const size_t bytes = gw_field_slots(c) * (mixed(c) ? sizeof(float) : sizeof(double));
     GW_CUDA(cudaMemcpyAsync(bak, u, bytes, cudaMemcpyDeviceToDevice, c->stream));
     for (int part = 0; part < GW_KERNEL_COUNT; ++part) {
         float total = 0.f;

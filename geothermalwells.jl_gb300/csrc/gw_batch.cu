@@ -140,7 +140,7 @@ int gw_batch_autotune(gw_batch *b, double dt, int reps, int *tiling_out) {
     for (int d = 0; d < n; ++d) clock[d] = b->ctx[d]->t_now;
     for (int d = 0; d < n; ++d) {
         gw_ctx *c = b->ctx[d];
-        const size_t N = (size_t)c->nx * c->ny * c->nz;
+        const size_t N = gw_field_slots(c);   // every slot of the state, padding included
         const bool mix = c->precision == GW_PREC_MIXED;
         GW_CUDA(cudaMemcpyAsync(mix ? (void *)c->f_g1 : (void *)c->d_g1, mix ? (void *)c->f_u : (void *)c->d_u,
                                 N * (mix ? sizeof(float) : sizeof(double)), cudaMemcpyDeviceToDevice, c->stream));
@@ -191,7 +191,7 @@ int gw_batch_autotune(gw_batch *b, double dt, int reps, int *tiling_out) {
         c->half_cfg = cand[arg][d];
         c->graph_dt = -1.0;
         if (tiling_out) tiling_out[d] = cand[arg][d];
-        const size_t N = (size_t)c->nx * c->ny * c->nz;
+        const size_t N = gw_field_slots(c);   // every slot of the state, padding included
         const bool mix = c->precision == GW_PREC_MIXED;
         GW_CUDA(cudaMemcpyAsync(mix ? (void *)c->f_u : (void *)c->d_u, mix ? (void *)c->f_g1 : (void *)c->d_g1,
                                 N * (mix ? sizeof(float) : sizeof(double)), cudaMemcpyDeviceToDevice, c->stream));
@@ -238,6 +238,8 @@ int gw_batch_step(gw_batch *b, double dt, int nsteps, int max_stages) {
     GW_CUDA(cudaEventRecord(b->ev1, b->stream));
     GW_CUDA(cudaStreamSynchronize(b->stream));
     if ((rc = gw_debug_status(b->device))) return rc;
+    for (gw_ctx *c : b->ctx)
+        if ((rc = gw_fused_status(c))) return rc;
     float ms = 0.f;
     GW_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     b->last_ms = ms;

@@ -20,9 +20,12 @@
 // converts to absolute temperature in double.  ROCK2 in the mixed path
 // accumulates its stages as increments over the column's start value, so the
 // stored field is rounded once per step.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <mutex>
 
 #include "gw_internal.h"
 #include "gw_fused.h"
@@ -45,6 +48,42 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
+// mbarrier and 3-D tensor-map tile copies (cp.async.bulk.tensor)
+__device__ __forceinline__ void mbar_init(unsigned long long *mb, unsigned count) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(mb);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *mb, unsigned bytes) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(mb);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(a), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned long long *mb, unsigned parity) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(mb);
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded: after the limit the flag is set and the caller goes on (the step
+// then reports an error; no thread leaves the block's barriers)
+__device__ __forceinline__ void mbar_wait(unsigned long long *mb, unsigned parity, int *err) {
+    for (int i = 0; i < (1 << 24); ++i)
+        if (mbar_try(mb, parity)) return;
+    atomicExch(err, 1);
+}
+__device__ __forceinline__ void tma_tile3(void *dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                          unsigned long long *mb) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst), m = (unsigned)__cvta_generic_to_shared(mb);
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(d),
+        "l"((unsigned long long)map), "r"(c0), "r"(c1), "r"(c2), "r"(m)
+        : "memory");
+}
+
 // ---------------------------------------------------------------------------
 // 1. ROCK2 on whole columns
 // sc: per recurrence stage j = 1..s-2: (h mu_j, kappa_j); then (h sigma,
@@ -55,7 +94,7 @@ __global__ void __launch_bounds__(256) k_rock2_col(T *__restrict__ u, const int 
                                                    const T *__restrict__ czp,
                                                    const T *__restrict__ fref,
                                                    const double *__restrict__ sc, int s, int nz,
-                                                   long long ncols) {
+                                                   int pz, long long ncols) {
     // shared memory: base (the column at the step start), b0, and for the
     // increment form F0 = A base (+ source) and b1.  A stage reads its input
     // as a stencil and the stage before it only at its own level, so each
@@ -70,7 +109,7 @@ __global__ void __launch_bounds__(256) k_rock2_col(T *__restrict__ u, const int 
         const int p = colprof[col];
         const T *cmc = czm + (size_t)p * nz;
         const T *cpc = czp + (size_t)p * nz;
-        T *uc = u + col * nz;
+        T *uc = u + col * pz;
         for (int k = threadIdx.x; k < nz; k += blockDim.x) base[k] = uc[k];
         __syncthreads();
         // A_z on a column in shared memory; Neumann ends (src/solver.jl:95-109)
@@ -155,8 +194,8 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) 
                                                    const C *__restrict__ czp,
                                                    const C *__restrict__ fref,
                                                    const C *__restrict__ sc, int s, int nz,
-                                                   long long ncols) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+                                                   int pz, long long ncols) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     // nt = blockDim.x threads (a multiple of 32, at most 256), LPT levels each
     const int nt = blockDim.x;
     T *stage = reinterpret_cast<T *>(smem_raw);   // [2][spad(nt * LPT)]
@@ -180,7 +219,7 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) 
     const int st0 = spad(t), nts = nt + nt / 32;
     auto fetch = [&](long long col, int buf) {
         T *d = stage + (size_t)buf * nzs + st0;
-        const T *g = u + col * nz + t;
+        const T *g = u + col * pz + t;
 #pragma unroll
         for (int i = 0; i < LPT; ++i)
             if (t + nt * i < nz && GW_OK_D(d + nts * i, smem_raw, 203) && GW_OK_G(g + nt * i, 204))
@@ -298,7 +337,7 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) 
             if (GW_OK_D(st + spad(kb + i), smem_raw, 210)) st[spad(kb + i)] = (T)(INC ? base[i] + y : y);
         }
         __syncthreads();
-        T *uc = u + col * nz + t;
+        T *uc = u + col * pz + t;
 #pragma unroll
         for (int i = 0; i < LPT; ++i)
             if (t + nt * i < nz && GW_OK_G(uc + nt * i, 211) && GW_OK_D(st + st0 + nts * i, smem_raw, 212))
@@ -332,10 +371,10 @@ __global__ void __launch_bounds__(256, 3) k_rock2_win(float *__restrict__ u, con
                                                       const float *__restrict__ czp,
                                                       const float *__restrict__ fref,
                                                       const float *__restrict__ sc, int s, int nz,
-                                                      int ncols, int nwin) {
+                                                      int pz, int ncols, int nwin) {
     constexpr int W = 32 * LPT;
     constexpr int WS = W + W / 32;   // padded slots of one staging buffer
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int g = blockIdx.x * (blockDim.x >> 5) + wib;
     const int slots = gridDim.x * (blockDim.x >> 5) / nwin;   // column slots
@@ -352,7 +391,7 @@ __global__ void __launch_bounds__(256, 3) k_rock2_win(float *__restrict__ u, con
     // lane l copies window levels l + 32 i into slots spad(l + 32 i)
     auto fetch = [&](int col, int buf) {
         float *d = ring + (size_t)buf * WS;
-        const float *gcol = u + (size_t)col * nz;
+        const float *gcol = u + (size_t)col * pz;
 #pragma unroll
         for (int i = 0; i < LPT; ++i) {
             const int j = lane + 32 * i, k = ws + j;
@@ -476,7 +515,7 @@ __global__ void __launch_bounds__(256, 3) k_rock2_win(float *__restrict__ u, con
                 st[spad(lane * LPT + i)] = st[spad(lane * LPT + i)] + y;
         }
         __syncwarp();
-        float *uc = u + (size_t)col * nz;
+        float *uc = u + (size_t)col * pz;
 #pragma unroll
         for (int i = 0; i < LPT; ++i) {
             const int j = lane + 32 * i, k = ws + j;
@@ -527,7 +566,7 @@ __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *
                                                     const T *__restrict__ cmt,
                                                     const T *__restrict__ cpt,
                                                     const double *__restrict__ Tref, int nx, int ny,
-                                                    int nz, double h, int dir, int nchunks) {
+                                                    int nz, int pz, double h, int dir, int nchunks) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int ch = blockIdx.y + kChunkRows * blockIdx.z;   // chunk rows of at most 65535
     if (k >= nz || ch >= nchunks) return;
@@ -539,18 +578,18 @@ __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *
     auto ld = [&](const T *p) -> T { return GW_OK_G(p, 304) ? *p : T(0); };
     auto sweep = [&](int q) {
         const int i = GW_OK_G(pi + q, 303) ? pi[q] : 0, j = GW_OK_G(pj + q, 303) ? pj[q] : 0;
-        const long long c = k + (long long)nz * (j + (long long)ny * i);
+        const long long c = k + (long long)pz * (j + (long long)ny * i);
         const T xc = ld(src + c);
         T xp, xm;
         size_t t;
         if (dir == GW_DIR_X) {
-            const long long st = (long long)nz * ny;
+            const long long st = (long long)pz * ny;
             xp = (i < nx - 1) ? ld(src + c + st) : xc;
             xm = (i > 0) ? ld(src + c - st) : xc;
             t = ((size_t)zc * ny + j) * nx + i;
         } else {
-            xp = (j < ny - 1) ? ld(src + c + nz) : xc;
-            xm = (j > 0) ? ld(src + c - nz) : xc;
+            xp = (j < ny - 1) ? ld(src + c + pz) : xc;
+            xm = (j > 0) ? ld(src + c - pz) : xc;
             t = ((size_t)zc * nx + i) * ny + j;
         }
         const T a = (GW_OK_G(cpt + t, 305) ? __ldg(cpt + t) : T(0)) * (xp - xc) -
@@ -815,7 +854,14 @@ struct alignas(4 * sizeof(T)) Quad {
     T x, y, z, w;
 };
 
-template <typename T, bool XL, int HW, int HR>
+// TMA (float field, columns pz apart, pz a multiple of 4): the chunk of the
+// HW + 2 lines is one 3-D tensor-map tile (32 levels x lines x rows, levels
+// beyond nz, lines outside 0..nl-1 and rows beyond N zero-filled, as the
+// cp.async copies fill them), issued by one thread into a ring of NB buffers
+// and awaited on the buffer's mbarrier.  Tile layout: [row][line][32] for the
+// x-lines and the cp.async path, [line][row][32] for TMA y-lines (the tensor's
+// dimensions are levels, j, i).
+template <typename T, bool XL, int HW, int HR, int NB = 2, bool TMA = false>
 __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, const T *__restrict__ src,
                                                         const T *__restrict__ pp,
                                                         const int *__restrict__ pipe_line,
@@ -823,11 +869,17 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                                                         const Quad<T> *__restrict__ hq,
                                                         const T *__restrict__ fib,
                                                         const T *__restrict__ fcu, int nx, int ny,
-                                                        int nz, int countz, int m_begin, int m_end) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *tile = reinterpret_cast<T *>(smem_raw);   // [2][HR][HW + 2][32]
+                                                        int nz, int pz, int countz, int m_begin, int m_end,
+                                                        const __grid_constant__ CUtensorMap tmap, int *err) {
+    static_assert(!TMA || sizeof(T) == 4, "tensor-map tiles: float fields only");
+    static_assert(TMA || NB == 2, "the cp.async path double-buffers");
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T *tile = reinterpret_cast<T *>(smem_raw);   // [NB][tile]
     constexpr int kRow = (HW + 2) * 32;
     constexpr int kTile = HR * kRow;
+    constexpr int kRowS = (TMA && !XL) ? 32 : kRow;        // rows apart in a tile
+    constexpr int kSlotS = (TMA && !XL) ? HR * 32 : 32;    // line slots apart in a tile
+    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(smem_raw + (size_t)NB * kTile * sizeof(T));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nl = XL ? ny : nx;   // lines per level
     const int N = XL ? nx : ny;    // line length
@@ -837,8 +889,8 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     const bool active = kok && m < m_end;
     const int kc = kok ? k : nz - 1, mc = m < m_end ? m : m_end - 1;   // clamped for table reads
     // element (k, line m, row l): x-lines (k, j=m, i=l), y-lines (k, i=m, j=l)
-    const long long mst = XL ? (long long)nz : (long long)nz * ny;
-    const long long rst = XL ? (long long)nz * ny : (long long)nz;
+    const long long mst = XL ? (long long)pz : (long long)pz * ny;
+    const long long rst = XL ? (long long)pz * ny : (long long)pz;
     const size_t fb = ((size_t)(GW_OK_G(zclass + kc, 112) ? zclass[kc] : 0) * nl + mc) * N;
     const int *pline = pipe_line + (size_t)mc * N;
     // lines through no pipe column skip the per-row pipe lookup (most lines)
@@ -869,6 +921,18 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     auto load_chunk = [&](int ch, int buf) {
         T *t = tile + buf * kTile;
         const int l0 = ch * HR;
+        if constexpr (TMA) {
+            if (threadIdx.x == 0) {
+                // the buffer's previous chunk was read through the generic proxy
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                mbar_expect_tx(mbar + buf, (unsigned)(kTile * sizeof(T)));
+                if (XL)
+                    tma_tile3(t, &tmap, k0, m0 - 1, l0, mbar + buf);
+                else
+                    tma_tile3(t, &tmap, k0, l0, m0 - 1, mbar + buf);
+            }
+            return;
+        }
         const bool full = l0 + HR <= N;
 #pragma unroll
         for (int rep = 0; rep < 2; ++rep) {
@@ -892,16 +956,29 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
 
     T y = T(0);
     T *dr = dl;
-    load_chunk(0, 0);
-    for (int ch = 0; ch < nchunk; ++ch) {
-        if (ch + 1 < nchunk) {
-            load_chunk(ch + 1, (ch + 1) & 1);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
+    if constexpr (TMA) {
+        if (threadIdx.x < NB) mbar_init(mbar + threadIdx.x, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         __syncthreads();
-        const T *row = tile + (ch & 1) * kTile + warp * 32 + lane;
+        for (int b = 0; b < NB - 1 && b < nchunk; ++b) load_chunk(b, b);
+    } else {
+        load_chunk(0, 0);
+    }
+    for (int ch = 0; ch < nchunk; ++ch) {
+        const int buf = TMA ? ch % NB : ch & 1;
+        if constexpr (TMA) {
+            if (ch + NB - 1 < nchunk) load_chunk(ch + NB - 1, (ch + NB - 1) % NB);
+            mbar_wait(mbar + buf, (unsigned)((ch / NB) & 1), err);
+        } else {
+            if (ch + 1 < nchunk) {
+                load_chunk(ch + 1, (ch + 1) & 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncthreads();
+        }
+        const T *row = tile + buf * kTile + warp * kSlotS + lane;
         const int l0 = ch * HR;
         const Quad<T> *qc = hql + l0;
         if (l0 + HR <= N && !line_pipe) {
@@ -913,8 +990,8 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
 #pragma unroll
                 for (int g = 0; g < kHG; ++g) {
                     q[g] = GW_OK_G(qc + r0 + g, 104) ? qc[r0 + g] : Quad<T>{};
-                    const T *rw = row + (r0 + g) * kRow;
-                    xm[g] = rd(rw); xc[g] = rd(rw + 32); xp[g] = rd(rw + 64);
+                    const T *rw = row + (r0 + g) * kRowS;
+                    xm[g] = rd(rw); xc[g] = rd(rw + kSlotS); xp[g] = rd(rw + 2 * kSlotS);
                 }
 #pragma unroll
                 for (int g = 0; g < kHG; ++g) {
@@ -935,8 +1012,8 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
 #pragma unroll
                 for (int g = 0; g < kHG; ++g) {
                     q[g] = GW_OK_G(qc + r0 + g, 104) ? qc[r0 + g] : Quad<T>{};
-                    const T *rw = row + (r0 + g) * kRow;
-                    xm[g] = rd(rw); xc[g] = rd(rw + 32); xp[g] = rd(rw + 64);
+                    const T *rw = row + (r0 + g) * kRowS;
+                    xm[g] = rd(rw); xc[g] = rd(rw + kSlotS); xp[g] = rd(rw + 2 * kSlotS);
                     pq[g] = pipe_levels && GW_OK_G(pline + l0 + r0 + g, 105) ? __ldg(pline + l0 + r0 + g) : -1;
                 }
 #pragma unroll
@@ -957,9 +1034,9 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
             for (int r = 0; r < rmax; ++r) {
                 const int l = l0 + r;
                 const Quad<T> q = GW_OK_G(qc + r, 104) ? qc[r] : Quad<T>{};
-                const T *rw = row + r * kRow;
+                const T *rw = row + r * kRowS;
                 const T ay = q.w * y;
-                T yn = fma(q.x, rd(rw + 32), fma(q.y, rd(rw + 64), fma(q.z, rd(rw), -ay)));
+                T yn = fma(q.x, rd(rw + kSlotS), fma(q.y, rd(rw + 2 * kSlotS), fma(q.z, rd(rw), -ay)));
                 const int pq = pipe_levels && GW_OK_G(pline + l, 105) ? __ldg(pline + l) : -1;
                 if (pq >= 0)
                     yn = fma(GW_OK_G(pp + (size_t)pq * countz + k, 106) ? pp[(size_t)pq * countz + k] : T(0),
@@ -969,7 +1046,7 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                 dr += rst;
             }
         }
-        __syncthreads();   // the buffer is refilled two chunks later
+        __syncthreads();   // the buffer is refilled NB - 1 chunks later
     }
     if (!active) return;
     // backward sweep: batches of kHB rows are loaded before the previous
@@ -1036,7 +1113,7 @@ __global__ void __launch_bounds__(32 * HW * S) k_half_seg(T *__restrict__ dst, c
                                                           const Quad<T> *__restrict__ hq,
                                                           const T *__restrict__ fib,
                                                           const T *__restrict__ fcu, int nx, int ny,
-                                                          int nz, int countz, int m_begin, int m_end) {
+                                                          int nz, int pz, int countz, int m_begin, int m_end) {
     __shared__ T s_end[HW][S][32], s_prop[HW][S][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int lw = warp / S, sg = warp % S;
@@ -1047,8 +1124,8 @@ __global__ void __launch_bounds__(32 * HW * S) k_half_seg(T *__restrict__ dst, c
     const bool kok = k < nz;
     const bool active = kok && m < m_end;
     const int kc = kok ? k : nz - 1, mc = m < m_end ? m : m_end - 1;
-    const long long mst = XL ? (long long)nz : (long long)nz * ny;
-    const long long rst = XL ? (long long)nz * ny : (long long)nz;
+    const long long mst = XL ? (long long)pz : (long long)pz * ny;
+    const long long rst = XL ? (long long)pz * ny : (long long)pz;
     const int R = (N + S - 1) / S;                 // rows per segment (<= RMAX)
     const int s0 = sg * R;
     const int len = max(0, min(R, N - s0));
@@ -1158,13 +1235,13 @@ __global__ void __launch_bounds__(128) k_half_refine(float *__restrict__ x, floa
                                                      const float *__restrict__ fa,
                                                      const float *__restrict__ fib,
                                                      const float *__restrict__ fcu, int nx, int ny,
-                                                     int nz, int countz, double h) {
+                                                     int nz, int pz, int countz, double h) {
     const int nl = XL ? ny : nx, N = XL ? nx : ny;
     const int k = blockIdx.x * 32 + (threadIdx.x & 31);
     const int m = blockIdx.y * 4 + (threadIdx.x >> 5);
     if (k >= nz || m >= nl) return;
-    const long long mst = XL ? (long long)nz : (long long)nz * ny;
-    const long long rst = XL ? (long long)nz * ny : (long long)nz;
+    const long long mst = XL ? (long long)pz : (long long)pz * ny;
+    const long long rst = XL ? (long long)pz * ny : (long long)pz;
     const int zc = zclass[k];
     const size_t lb = ((size_t)zc * nl + m) * N;   // line-direction tables
     const bool pipe_levels = k < countz && __ldg(pipe_line + (size_t)nl * N + m) != 0;
@@ -1237,16 +1314,186 @@ __global__ void __launch_bounds__(128) k_half_refine(float *__restrict__ x, floa
     }
 }
 
+// GW_MIXED_REFINE on the FP32 pipe.  The residual r = b - (I - h A_line) x
+// of k_half_refine, computed in double-float arithmetic (a value as an
+// unevaluated sum hi + lo of two floats: about 44 bits) instead of double:
+// GB300 runs float arithmetic at many times its FP64 rate.  Products with a
+// float are exact through fmaf, sums use two-sum (Knuth, Dekker); every
+// operation is a correctly rounded intrinsic, never contracted, so the
+// error-free transformations hold.  The residual depends only on the float
+// solution x and on b, so it is formed for a batch of rows ahead of the
+// correction's recurrence, which runs in float (the correction is small
+// against x: its own rounding is below the float rounding of x + d).
+struct Df {
+    float hi, lo;
+};
+__device__ __forceinline__ Df df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ Df df_fast(float a, float b) {   // |a| >= |b| or a == 0
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ Df df_mul_f(Df a, float b) {
+    const float p = __fmul_rn(a.hi, b);
+    return df_fast(p, __fmaf_rn(a.lo, b, __fmaf_rn(a.hi, b, -p)));
+}
+__device__ __forceinline__ Df df_mul(Df a, Df b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    return df_fast(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, __fmaf_rn(a.hi, b.hi, -p))));
+}
+__device__ __forceinline__ Df df_add(Df a, Df b) {
+    const Df s = df_two_sum(a.hi, b.hi);
+    return df_fast(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ Df df_neg(Df a) { return {-a.hi, -a.lo}; }
+
+// Per step size: h c_m, h c_p (float4: hi, lo, hi, lo) and 1 + h (c_m + c_p)
+// (float2) of one direction's double coefficient table, as double-float.
+__global__ void k_refine_tables(float4 *__restrict__ hmp, float2 *__restrict__ dg,
+                                const double *__restrict__ cm, const double *__restrict__ cp, double h,
+                                size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    auto split = [](double v, float &hi, float &lo) {
+        hi = __double2float_rn(v);
+        lo = __double2float_rn(__dsub_rn(v, (double)hi));
+    };
+    const double a = __dmul_rn(h, cm[i]), b = __dmul_rn(h, cp[i]);
+    const double d = __dadd_rn(1.0, __dmul_rn(h, __dadd_rn(cm[i], cp[i])));
+    float4 q;
+    float2 g;
+    split(a, q.x, q.y);
+    split(b, q.z, q.w);
+    split(d, g.x, g.y);
+    hmp[i] = q;
+    dg[i] = g;
+}
+
+// Line-direction tables lq/lg at [zc][line][row], the other direction's eq at
+// [zc][row][line] (the coefficient layouts of k_half_refine).
+template <bool XL>
+__global__ void __launch_bounds__(128) k_half_refine_df(float *__restrict__ x, float *__restrict__ yb,
+                                                        const float *__restrict__ src,
+                                                        const float *__restrict__ pp,
+                                                        const int *__restrict__ pipe_line,
+                                                        const int *__restrict__ zclass,
+                                                        const float4 *__restrict__ lq,
+                                                        const float2 *__restrict__ lg,
+                                                        const float4 *__restrict__ eq,
+                                                        const float *__restrict__ fa,
+                                                        const float *__restrict__ fib,
+                                                        const float *__restrict__ fcu, int nx, int ny,
+                                                        int nz, int pz, int countz) {
+    const int nl = XL ? ny : nx, N = XL ? nx : ny;
+    const int k = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int m = blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (k >= nz || m >= nl) return;
+    const long long mst = XL ? (long long)pz : (long long)pz * ny;
+    const long long rst = XL ? (long long)pz * ny : (long long)pz;
+    const int zc = zclass[k];
+    const size_t lb = ((size_t)zc * nl + m) * N;   // line-direction tables
+    const bool pipe_levels = k < countz && __ldg(pipe_line + (size_t)nl * N + m) != 0;
+    const int *pline = pipe_line + (size_t)m * N;
+    const long long e0 = k + m * mst;
+    constexpr int kRB = 4;
+    float xm = 0.f, xc = x[e0], y = 0.f;
+    for (int l0 = 0; l0 < N; l0 += kRB) {
+        float xn[kRB], uc[kRB], up[kRB], um[kRB], pv[kRB], fa_[kRB], fi_[kRB];
+        float4 L[kRB], E[kRB];
+        float2 G[kRB];
+        int pq[kRB];
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) {   // the batch's loads, ahead of the arithmetic
+            const int l = l0 + r;
+            if (l < N) {
+                const long long e = e0 + (long long)l * rst;
+                xn[r] = l + 1 < N ? x[e + rst] : 0.f;
+                pq[r] = pipe_levels ? __ldg(pline + l) : -1;
+                pv[r] = pq[r] >= 0 ? pp[(size_t)pq[r] * countz + k] : 0.f;
+                uc[r] = src[e];
+                up[r] = m + 1 < nl ? src[e + mst] : uc[r];
+                um[r] = m > 0 ? src[e - mst] : uc[r];
+                E[r] = __ldg(eq + ((size_t)zc * N + l) * nl + m);
+                L[r] = __ldg(lq + lb + l);
+                G[r] = __ldg(lg + lb + l);
+                fa_[r] = __ldg(fa + lb + l);
+                fi_[r] = __ldg(fib + lb + l);
+            }
+        }
+        float rr[kRB];
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) {   // residuals: depend on x and b only
+            const int l = l0 + r;
+            if (l < N) {
+                Df b;
+                if (pq[r] >= 0) {
+                    b = {pv[r], 0.f};
+                } else {   // b = u + h c_p (u+ - u) - h c_m (u - u-)
+                    const Df t1 = df_mul({E[r].z, E[r].w}, df_two_sum(up[r], -uc[r]));
+                    const Df t2 = df_mul({E[r].x, E[r].y}, df_two_sum(uc[r], -um[r]));
+                    b = df_add(Df{uc[r], 0.f}, df_add(t1, df_neg(t2)));
+                }
+                Df ax = df_mul_f({G[r].x, G[r].y}, xc);   // (1 + h (c_m + c_p)) x_l
+                if (l > 0) ax = df_add(ax, df_neg(df_mul_f({L[r].x, L[r].y}, xm)));
+                if (l + 1 < N) ax = df_add(ax, df_neg(df_mul_f({L[r].z, L[r].w}, xn[r])));
+                const Df res = df_add(b, df_neg(ax));
+                rr[r] = __fadd_rn(res.hi, res.lo);
+                xm = xc;
+                xc = xn[r];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) {   // the correction's forward elimination
+            const int l = l0 + r;
+            if (l < N) {
+                y = (rr[r] - fa_[r] * y) * fi_[r];
+                yb[e0 + (long long)l * rst] = y;
+            }
+        }
+    }
+    // back substitution of the correction, added to x (x_{N-1} first)
+    float d = y;
+    long long e = e0 + (long long)(N - 1) * rst;
+    x[e] = x[e] + d;
+    constexpr int kBB = 8;
+    for (int l1 = N - 2; l1 >= 0; l1 -= kBB) {
+        float yv[kBB], xv[kBB], cu[kBB];
+#pragma unroll
+        for (int r = 0; r < kBB; ++r) {
+            const int l = l1 - r;
+            if (l >= 0) {
+                const long long el = e0 + (long long)l * rst;
+                yv[r] = yb[el]; xv[r] = x[el]; cu[r] = __ldg(fcu + lb + l);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kBB; ++r) {
+            const int l = l1 - r;
+            if (l >= 0) {
+                d = yv[r] - cu[r] * d;
+                x[e0 + (long long)l * rst] = xv[r] + d;
+            }
+        }
+    }
+}
+
 // mixed path field conversion: theta = T - T_ref(z) and back
+// (T: nz levels per column; theta: columns pz floats apart, pz >= nz)
 __global__ void k_to_theta(float *__restrict__ th, const double *__restrict__ T,
-                           const double *__restrict__ Tref, size_t n, int nz) {
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
-        th[q] = (float)(T[q] - Tref[q % nz]);
+                           const double *__restrict__ Tref, size_t n, int nz, int pz) {
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const size_t col = q / nz, k = q - col * nz;
+        th[col * pz + k] = (float)(T[q] - Tref[k]);
+    }
 }
 __global__ void k_from_theta(double *__restrict__ T, const float *__restrict__ th,
-                             const double *__restrict__ Tref, size_t n, int nz) {
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
-        T[q] = (double)th[q] + Tref[q % nz];
+                             const double *__restrict__ Tref, size_t n, int nz, int pz) {
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const size_t col = q / nz, k = q - col * nz;
+        T[q] = (double)th[col * pz + k] + Tref[k];
+    }
 }
 
 template <typename T>
@@ -1350,7 +1597,7 @@ int launch_rock2_win(gw_ctx *c, int s, int nwin, float *u, const float *czm, con
     long long grid = std::min(per_sm * c->sms, need);
     grid = std::max(grid, (long long)(nwin + kWinWarps - 1) / kWinWarps);   // one whole set of windows
     kern<<<(unsigned)grid, 32 * kWinWarps, win_smem(LPT), c->stream>>>(
-        u, order, c->d_colprof, czm, czp, fref, c->f_stage, s, c->nz, (int)ncols, nwin);
+        u, order, c->d_colprof, czm, czp, fref, c->f_stage, s, c->nz, c->pz, (int)ncols, nwin);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }
@@ -1376,16 +1623,16 @@ int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *
     const int lpt = rock2_lpt(c->nz, sizeof(T) == 4);
     unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid ? ncols : c->rock2_grid);
     switch (lpt) {
-        case 2: k_rock2_reg<T, INC, 2><<<grid, c->rock2_nt, reg_smem<T>(2, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 4: k_rock2_reg<T, INC, 4><<<grid, c->rock2_nt, reg_smem<T>(4, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 5: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 5><<<grid, c->rock2_nt, reg_smem<T>(5, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 6: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 6><<<grid, c->rock2_nt, reg_smem<T>(6, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 7: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 7><<<grid, c->rock2_nt, reg_smem<T>(7, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 8: k_rock2_reg<T, INC, 8><<<grid, c->rock2_nt, reg_smem<T>(8, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
-        case 16: k_rock2_reg<T, INC, 16><<<grid, c->rock2_nt, reg_smem<T>(16, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, ncols); break;
+        case 2: k_rock2_reg<T, INC, 2><<<grid, c->rock2_nt, reg_smem<T>(2, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 4: k_rock2_reg<T, INC, 4><<<grid, c->rock2_nt, reg_smem<T>(4, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 5: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 5><<<grid, c->rock2_nt, reg_smem<T>(5, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 6: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 6><<<grid, c->rock2_nt, reg_smem<T>(6, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 7: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 7><<<grid, c->rock2_nt, reg_smem<T>(7, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 8: k_rock2_reg<T, INC, 8><<<grid, c->rock2_nt, reg_smem<T>(8, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 16: k_rock2_reg<T, INC, 16><<<grid, c->rock2_nt, reg_smem<T>(16, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
         default:
             k_rock2_col<T, INC><<<grid, 256, rock2_smem<T>(c->nz), c->stream>>>(u, c->d_colprof, czm, czp, fref,
-                                                                            c->d_stage, s, c->nz, ncols);
+                                                                            c->d_stage, s, c->nz, c->pz, ncols);
     }
     GW_CUDA(cudaGetLastError());
     return GW_OK;
@@ -1401,10 +1648,10 @@ int launch_rock2_f64(gw_ctx *c, int s, const int *order, long long ncols) {
     const unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid64 ? ncols : c->rock2_grid64);
     const double *czm = c->c64.czm, *czp = c->c64.czp, *fr = c->d_fref64, *sc = c->d_stage;
     switch (lpt) {
-        case 2: k_rock2_reg<float, true, 2, double><<<grid, nt, reg_smem<float>(2, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, ncols); break;
-        case 4: k_rock2_reg<float, true, 4, double><<<grid, nt, reg_smem<float>(4, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, ncols); break;
-        case 8: k_rock2_reg<float, true, 8, double><<<grid, nt, reg_smem<float>(8, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, ncols); break;
-        case 16: k_rock2_reg<float, true, 16, double><<<grid, nt, reg_smem<float>(16, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, ncols); break;
+        case 2: k_rock2_reg<float, true, 2, double><<<grid, nt, reg_smem<float>(2, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
+        case 4: k_rock2_reg<float, true, 4, double><<<grid, nt, reg_smem<float>(4, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
+        case 8: k_rock2_reg<float, true, 8, double><<<grid, nt, reg_smem<float>(8, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
+        case 16: k_rock2_reg<float, true, 16, double><<<grid, nt, reg_smem<float>(16, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
         default: return gw_fail(GW_ERR_UNSUPPORTED, "GW_MIXED_ROCK2_F64 supports nz <= 4096");
     }
     GW_CUDA(cudaGetLastError());
@@ -1433,7 +1680,7 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h, cudaStream_t st = n
         const dim3 g = chunk_grid(grid_for(c->nz, 128), c->n_pipe_chunks);
         k_pipe_sweep<T><<<g, 128, 0, st>>>(B.tp, c->d_pipepart, src, c->d_pipe_chunks,
                                                   c->d_pipe_i, c->d_pipe_j, c->d_zclass, cm, cp,
-                                                  B.Tref, c->nx, c->ny, c->nz, h, edir, c->n_pipe_chunks);
+                                                  B.Tref, c->nx, c->ny, c->nz, c->pz, h, edir, c->n_pipe_chunks);
         GW_CUDA(cudaGetLastError());
     }
     dim3 gr((c->nz + 31) / 32, c->nbh);
@@ -1461,16 +1708,45 @@ int launch_pipe(gw_ctx *c, const T *src, int edir, double h, cudaStream_t st = n
 template <typename T>
 size_t half_smem(int cfg) { return 2 * (size_t)kTileHR[cfg] * (kTileHW[cfg] + 2) * 32 * sizeof(T); }
 
-template <typename T, int HW, int HR>
+// tensor-map tiles: ring depth per tiling (the two largest tiles stay at two),
+// shared memory with the ring's mbarriers
+constexpr int kTileNB[6] = {3, 3, 3, 2, 3, 2};
+template <int HW, int HR, int NB>
+constexpr size_t tma_smem() { return (size_t)NB * HR * (HW + 2) * 32 * sizeof(float) + 8 * NB; }
+
+// the tensor map of src's tiles, or null (another buffer, or no maps)
+inline const CUtensorMap *tile_map(const gw_ctx *c, const void *src, int xlines, int cfg) {
+    if (!c->tma_ok || cfg < 0 || cfg >= 6) return nullptr;
+    const int b = src == (const void *)c->f_u ? 0 : src == (const void *)c->f_temp ? 1 : -1;
+    return b < 0 ? nullptr : &c->tmaps[b][xlines ? 0 : 1][cfg];
+}
+
+template <typename T, int HW, int HR, int NB>
 void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, const Quad<T> *hq,
-                 const GwFactors<T> &f, const T *pp, size_t smem, int mb, int me) {
+                 const GwFactors<T> &f, const T *pp, size_t smem, int mb, int me, const CUtensorMap *map) {
+    static const CUtensorMap kNoMap = {};
     dim3 grid((c->nz + 31) / 32, (me - mb + HW - 1) / HW);
+    if constexpr (sizeof(T) == 4) {
+        if (map) {
+            if (xlines)
+                k_half_tile<T, true, HW, HR, NB, true><<<grid, 32 * HW, tma_smem<HW, HR, NB>(), st>>>(
+                    dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
+                    mb, me, *map, c->d_err);
+            else
+                k_half_tile<T, false, HW, HR, NB, true><<<grid, 32 * HW, tma_smem<HW, HR, NB>(), st>>>(
+                    dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
+                    mb, me, *map, c->d_err);
+            return;
+        }
+    }
     if (xlines)
         k_half_tile<T, true, HW, HR><<<grid, 32 * HW, smem, st>>>(
-            dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz, mb, me);
+            dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz, mb, me,
+            kNoMap, c->d_err);
     else
         k_half_tile<T, false, HW, HR><<<grid, 32 * HW, smem, st>>>(
-            dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz, mb, me);
+            dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz, mb, me,
+            kNoMap, c->d_err);
 }
 
 template <typename T>
@@ -1491,11 +1767,11 @@ int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h, int mb = 
             dim3 grid((c->nz + 31) / 32, (me - mb + 1) / 2);
             if (xlines)
                 k_half_seg<T, true, 2, kSegS, kSegR><<<grid, 32 * 2 * kSegS, 0, st>>>(
-                    dst, src, B.pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz,
+                    dst, src, B.pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
                     mb, me);
             else
                 k_half_seg<T, false, 2, kSegS, kSegR><<<grid, 32 * 2 * kSegS, 0, st>>>(
-                    dst, src, B.pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->countz,
+                    dst, src, B.pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
                     mb, me);
             GW_CUDA(cudaGetLastError());
             return GW_OK;
@@ -1503,13 +1779,14 @@ int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h, int mb = 
         cfg = 0;   // lines longer than the segments hold: the tiled kernel
     }
     const size_t sm = half_smem<T>(cfg);
+    const CUtensorMap *map = sizeof(T) == 4 ? tile_map(c, src, xlines, cfg) : nullptr;
     switch (cfg) {
-        case 1: half_launch<T, 8, 16>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
-        case 2: half_launch<T, 8, 8>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
-        case 3: half_launch<T, 4, 32>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
-        case 4: half_launch<T, 2, 16>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
-        case 5: half_launch<T, 8, 32>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
-        default: half_launch<T, 4, 16>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me); break;
+        case 1: half_launch<T, 8, 16, kTileNB[1]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
+        case 2: half_launch<T, 8, 8, kTileNB[2]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
+        case 3: half_launch<T, 4, 32, kTileNB[3]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
+        case 4: half_launch<T, 2, 16, kTileNB[4]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
+        case 5: half_launch<T, 8, 32, kTileNB[5]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
+        default: half_launch<T, 4, 16, kTileNB[0]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
     }
     GW_CUDA(cudaGetLastError());
     return GW_OK;
@@ -1521,34 +1798,106 @@ int launch_refine(gw_ctx *c, float *x, const float *src, int xlines, double h) {
     const int nl = xlines ? c->ny : c->nx;
     dim3 grid((c->nz + 31) / 32, (nl + 3) / 4);
     const GwFactors<float> &f = xlines ? c->c32.fx : c->c32.fy;
+    if (!c->refine_f64) {
+        // tables allocated by gw_fused_prepare_refine and filled for this
+        // step size by gw_fused_refine_tables, both before any capture
+        if (!c->f_rq[0] || c->rq_h != h) return gw_fail(GW_ERR_ARG, "refinement tables not prepared for this step size");
+        const int dl = xlines ? 0 : 1;
+        if (xlines)
+            k_half_refine_df<true><<<grid, 128, 0, c->stream>>>(x, c->f_g1, src, c->f_pp, c->d_pipe_lx, c->d_zclass,
+                                                                c->f_rq[dl], c->f_rg[dl], c->f_rq[1 - dl], f.a, f.ib,
+                                                                f.cu, c->nx, c->ny, c->nz, c->pz, c->countz);
+        else
+            k_half_refine_df<false><<<grid, 128, 0, c->stream>>>(x, c->f_g1, src, c->f_pp, c->d_pipe_ly, c->d_zclass,
+                                                                 c->f_rq[dl], c->f_rg[dl], c->f_rq[1 - dl], f.a, f.ib,
+                                                                 f.cu, c->nx, c->ny, c->nz, c->pz, c->countz);
+        GW_CUDA(cudaGetLastError());
+        return GW_OK;
+    }
     if (xlines)
         k_half_refine<true><<<grid, 128, 0, c->stream>>>(x, c->f_g1, src, c->f_pp, c->d_pipe_lx, c->d_zclass,
                                                          c->c64.cxm, c->c64.cxp, c->c64.cym, c->c64.cyp, f.a,
-                                                         f.ib, f.cu, c->nx, c->ny, c->nz, c->countz, h);
+                                                         f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz, h);
     else
         k_half_refine<false><<<grid, 128, 0, c->stream>>>(x, c->f_g1, src, c->f_pp, c->d_pipe_ly, c->d_zclass,
                                                           c->c64.cym, c->c64.cyp, c->c64.cxm, c->c64.cxp, f.a,
-                                                          f.ib, f.cu, c->nx, c->ny, c->nz, c->countz, h);
+                                                          f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz, h);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
 }
 
-template <typename T, int HW, int HR>
+template <typename T, int HW, int HR, int NB>
 cudaError_t half_attr() {
     const int sm = (int)(2 * (size_t)HR * (HW + 2) * 32 * sizeof(T));
     cudaError_t e = cudaFuncSetAttribute(k_half_tile<T, true, HW, HR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_half_tile<T, false, HW, HR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if ((e = cudaFuncSetAttribute(k_half_tile<T, false, HW, HR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm)))
+        return e;
+    if constexpr (sizeof(T) == 4) {
+        const int st = (int)tma_smem<HW, HR, NB>();
+        if ((e = cudaFuncSetAttribute(k_half_tile<T, true, HW, HR, NB, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, st)))
+            return e;
+        return cudaFuncSetAttribute(k_half_tile<T, false, HW, HR, NB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    st);
+    }
+    return cudaSuccess;
 }
 
 template <typename T>
 cudaError_t half_attrs() {
     cudaError_t e;
-    if ((e = half_attr<T, 8, 16>()) != cudaSuccess || (e = half_attr<T, 4, 16>()) != cudaSuccess ||
-        (e = half_attr<T, 8, 8>()) != cudaSuccess || (e = half_attr<T, 4, 32>()) != cudaSuccess ||
-        (e = half_attr<T, 2, 16>()) != cudaSuccess || (e = half_attr<T, 8, 32>()) != cudaSuccess)
+    if ((e = half_attr<T, 8, 16, kTileNB[1]>()) != cudaSuccess || (e = half_attr<T, 4, 16, kTileNB[0]>()) != cudaSuccess ||
+        (e = half_attr<T, 8, 8, kTileNB[2]>()) != cudaSuccess || (e = half_attr<T, 4, 32, kTileNB[3]>()) != cudaSuccess ||
+        (e = half_attr<T, 2, 16, kTileNB[4]>()) != cudaSuccess || (e = half_attr<T, 8, 32, kTileNB[5]>()) != cudaSuccess)
         return e;
     return cudaSuccess;
+}
+
+// cuTensorMapEncodeTiled, from the driver through the runtime (no link to
+// the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+// The mixed path's half-step tensor maps: per source buffer (f_u, f_temp),
+// line direction and tiling, the field as a (levels, j, i) tensor with the
+// padded column pitch, box 32 levels x (lines + 2) x rows for the x-lines and
+// 32 x rows x (lines + 2) for the y-lines, out-of-range elements read as 0.
+// Without the driver's encoder (or a map it rejects) the half step keeps its
+// cp.async copies.
+void encode_tile_maps(gw_ctx *c) {
+    c->tma_ok = false;
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc || c->precision != GW_PREC_MIXED || c->pz % 4) return;
+    const cuuint64_t dims[3] = {(cuuint64_t)c->nz, (cuuint64_t)c->ny, (cuuint64_t)c->nx};
+    const cuuint64_t strides[2] = {(cuuint64_t)c->pz * sizeof(float), (cuuint64_t)c->pz * c->ny * sizeof(float)};
+    const cuuint32_t es[3] = {1, 1, 1};
+    float *bufs[2] = {c->f_u, c->f_temp};
+    for (int b = 0; b < 2; ++b)
+        for (int d = 0; d < 2; ++d)
+            for (int cfg = 0; cfg < 6; ++cfg) {
+                const cuuint32_t lines = (cuuint32_t)kTileHW[cfg] + 2, rows = (cuuint32_t)kTileHR[cfg];
+                const cuuint32_t box[3] = {32, d == 0 ? lines : rows, d == 0 ? rows : lines};
+                if (enc(&c->tmaps[b][d][cfg], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, bufs[b], dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                    return;
+            }
+    c->tma_ok = true;
 }
 
 template <typename T>
@@ -1677,6 +2026,9 @@ int gw_fused_prepare(gw_ctx *c) {
             (e = occ(k_rock2_win<8, kWinNB, false>, 8)))
             return gw_cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor(k_rock2_win)");
     }
+    // tensor-map tiles for the mixed half steps (GW_HALF_CPASYNC=1 keeps cp.async)
+    const char *hc = std::getenv("GW_HALF_CPASYNC");
+    if (!(hc && *hc && *hc != '0')) encode_tile_maps(c);
     return GW_OK;
 }
 
@@ -1729,7 +2081,8 @@ int gw_fused_time_part(gw_ctx *c, double dt, int s, int part) {
 }
 
 int gw_fused_check_finite(gw_ctx *c) {
-    size_t n = (size_t)c->nx * c->ny * c->nz;
+    // every slot of the field, padding levels (always 0) included
+    size_t n = (size_t)c->nx * c->ny * c->pz;
     GW_CUDA(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
     if (c->precision == GW_PREC_MIXED)
         k_finite<float><<<1216, 256, 0, c->stream>>>(c->f_u, n, c->d_flag);
@@ -1743,7 +2096,7 @@ int gw_fused_set_theta(gw_ctx *c, const double *T_host) {
     const size_t n = (size_t)c->nx * c->ny * c->nz;
     double *stage = reinterpret_cast<double *>(c->f_temp);   // f_temp and f_g1: 8 n bytes
     GW_CUDA(cudaMemcpyAsync(stage, T_host, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    k_to_theta<<<1216, 256, 0, c->stream>>>(c->f_u, stage, c->d_Tref, n, c->nz);
+    k_to_theta<<<1216, 256, 0, c->stream>>>(c->f_u, stage, c->d_Tref, n, c->nz, c->pz);
     GW_CUDA(cudaGetLastError());
     GW_CUDA(cudaStreamSynchronize(c->stream));
     return GW_OK;
@@ -1752,7 +2105,7 @@ int gw_fused_set_theta(gw_ctx *c, const double *T_host) {
 int gw_fused_get_theta(gw_ctx *c, double *T_host) {
     const size_t n = (size_t)c->nx * c->ny * c->nz;
     double *stage = reinterpret_cast<double *>(c->f_temp);
-    k_from_theta<<<1216, 256, 0, c->stream>>>(stage, c->f_u, c->d_Tref, n, c->nz);
+    k_from_theta<<<1216, 256, 0, c->stream>>>(stage, c->f_u, c->d_Tref, n, c->nz, c->pz);
     GW_CUDA(cudaGetLastError());
     GW_CUDA(cudaMemcpyAsync(T_host, stage, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     GW_CUDA(cudaStreamSynchronize(c->stream));
@@ -1785,7 +2138,42 @@ int gw_fused_prepare_rock2_f64(gw_ctx *c) {
 int gw_fused_prepare_refine(gw_ctx *c) {
     if (c->precision != GW_PREC_MIXED || !c->fused)
         return gw_fail(GW_ERR_ARG, "GW_MIXED_REFINE needs a fused GW_PREC_MIXED context");
+    if (c->refine_f64 || c->f_rq[0]) return GW_OK;
+    const size_t n = (size_t)c->n_zclass * c->nx * c->ny;
+    for (int d = 0; d < 2; ++d) {
+        float *a = nullptr, *g = nullptr;
+        int rc;
+        if ((rc = gw_dalloc_f(c, &a, 4 * n)) || (rc = gw_dalloc_f(c, &g, 2 * n))) return rc;
+        c->f_rq[d] = reinterpret_cast<float4 *>(a);
+        c->f_rg[d] = reinterpret_cast<float2 *>(g);
+    }
+    c->rq_h = -1.0;
     return GW_OK;
+}
+
+// the double-float refinement tables for half-step size h (no-op when
+// GW_MIXED_REFINE is off, runs in double, or the tables hold h already)
+int gw_fused_refine_tables(gw_ctx *c, double h) {
+    if (!(c->mixed_flags & GW_MIXED_REFINE) || c->refine_f64 || c->rq_h == h) return GW_OK;
+    if (!c->f_rq[0]) return gw_fail(GW_ERR_ARG, "refinement tables not allocated");
+    const size_t n = (size_t)c->n_zclass * c->nx * c->ny;
+    k_refine_tables<<<grid_for((long long)n, 256), 256, 0, c->stream>>>(c->f_rq[0], c->f_rg[0], c->c64.cxm,
+                                                                        c->c64.cxp, h, n);
+    k_refine_tables<<<grid_for((long long)n, 256), 256, 0, c->stream>>>(c->f_rq[1], c->f_rg[1], c->c64.cym,
+                                                                        c->c64.cyp, h, n);
+    GW_CUDA(cudaGetLastError());
+    c->rq_h = h;
+    return GW_OK;
+}
+
+// GW_ERR_CUDA if a kernel's bounded wait ran out since the last check
+int gw_fused_status(gw_ctx *c) {
+    if (!c->d_err) return GW_OK;
+    int flag = 0;
+    GW_CUDA(cudaMemcpy(&flag, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!flag) return GW_OK;
+    GW_CUDA(cudaMemset(c->d_err, 0, sizeof(int)));
+    return gw_fail(GW_ERR_CUDA, "a half-step tile did not arrive within its wait limit");
 }
 
 // debug build: point this translation unit's checks at the allocation registry

@@ -9,8 +9,13 @@ int gw_fused_prepare(gw_ctx *c);
 // Mixed contexts: launch shape of the ROCK2 column kernel with double stages
 // over the float field (GW_MIXED_ROCK2_F64); GW_ERR_UNSUPPORTED beyond its nz.
 int gw_fused_prepare_rock2_f64(gw_ctx *c);
-// Mixed contexts: check that GW_MIXED_REFINE can run (fused mixed step).
+// Mixed contexts: check that GW_MIXED_REFINE can run (fused mixed step) and
+// allocate its double-float tables (outside any stream capture).
 int gw_fused_prepare_refine(gw_ctx *c);
+// the double-float refinement tables for half-step size h, before the step's capture
+int gw_fused_refine_tables(gw_ctx *c, double h);
+// GW_ERR_CUDA if a kernel's bounded wait ran out since the last check (and clear the flag)
+int gw_fused_status(gw_ctx *c);
 // Build the step-size dependent tables (advection departures) for dt.
 int gw_fused_set_dt(gw_ctx *c, double dt);
 // Enqueue one full step (ROCK2 columns, two half steps, record) on c->stream.

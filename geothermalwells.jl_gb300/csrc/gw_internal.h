@@ -1,6 +1,7 @@
 // gw_internal.h -- device context and kernel launch interface shared by the
 // translation units of libgw_gb300.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
@@ -133,8 +134,17 @@ struct gw_ctx {
     int rock2_grid = 0;
     int rock2_nt = 256;               // threads per block of the ROCK2 column kernel
     int sms = 0;                      // multiprocessors of the context's GPU
+    int pz = 0;                       // level pitch of the fused fields: nz (FP64), nz rounded up to 4 (mixed)
+    // mixed path: 3-D tensor maps of the half-step tiles, [source: f_u, f_temp][x-, y-lines][tiling]
+    CUtensorMap tmaps[2][2][6];
+    bool tma_ok = false;              // maps encoded (else the half step copies with cp.async)
+    int *d_err = nullptr;             // set by a kernel whose bounded wait ran out
     int rock2w_per_sm[9] = {};        // resident blocks per SM of the window ROCK2 kernel, by LPT
     bool rock2_block = false;         // mixed ROCK2 on the block kernel (GW_ROCK2_BLOCK), not by windows
+    bool refine_f64 = false;          // GW_MIXED_REFINE residual in double (GW_REFINE_F64), not double-float
+    float4 *f_rq[2] = {nullptr, nullptr};   // refinement tables per direction (x, y): h c_m, h c_p as double-float
+    float2 *f_rg[2] = {nullptr, nullptr};   //   and 1 + h (c_m + c_p)
+    double rq_h = -1.0;               // step size those tables hold
     int half_cfg = 0;                 // half-step tiling (gw_fused.cu kTileHW/kTileHR)
     bool fused = false;
     bool host_setup = false;          // tables built on the host (GW_HOST_SETUP), else on the GPU
@@ -180,6 +190,9 @@ void gw_debug_unregister(int device, const void *p);
 int gw_debug_status(int device);
 
 // error reporting
+// slots of one fused-step field: nx ny columns, pz apart
+inline size_t gw_field_slots(const gw_ctx *c) { return (size_t)c->nx * c->ny * c->pz; }
+int gw_dalloc_f(gw_ctx *c, float **p, size_t n);
 int gw_fail(int code, const std::string &msg);
 int gw_cuda_fail(cudaError_t e, const char *what);
 #define GW_CUDA(call)                                                    \

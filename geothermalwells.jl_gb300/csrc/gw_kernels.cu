@@ -426,16 +426,19 @@ __global__ void k_snapshot_f64(float *__restrict__ dst, const double *__restrict
     for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
         dst[q] = (float)u[q];
 }
+// theta: columns pz floats apart (pz >= nz); dst: nz levels per column
 __global__ void k_snapshot_theta(float *__restrict__ dst, const float *__restrict__ th,
-                                 const double *__restrict__ Tref, size_t n, int nz) {
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
-        dst[q] = (float)((double)th[q] + Tref[q % nz]);
+                                 const double *__restrict__ Tref, size_t n, int nz, int pz) {
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const size_t col = q / nz, k = q - col * nz;
+        dst[q] = (float)((double)th[col * pz + k] + Tref[k]);
+    }
 }
 
 int gw_launch_snapshot(gw_ctx *c, float *dst) {
     const size_t N = (size_t)c->nx * c->ny * c->nz;
     if (c->precision == GW_PREC_MIXED)
-        k_snapshot_theta<<<152 * 8, 256, 0, c->stream>>>(dst, c->f_u, c->d_Tref, N, c->nz);
+        k_snapshot_theta<<<152 * 8, 256, 0, c->stream>>>(dst, c->f_u, c->d_Tref, N, c->nz, c->pz);
     else
         k_snapshot_f64<<<152 * 8, 256, 0, c->stream>>>(dst, c->d_u, N);
     GW_CUDA(cudaGetLastError());

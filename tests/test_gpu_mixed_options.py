@@ -99,3 +99,38 @@ def test_adjoint_refuses_options(gwlib):
         A.adjoint(c, w["T0"], w["dt"], 2)
     assert e.value.code == _lib.GW_ERR_UNSUPPORTED
     c.close()
+
+
+def fp64_run(w, nsteps):
+    cache = create_cache(backend=GB300(precision="fp64"), gridx=w["gridx"], gridy=w["gridy"],
+                         gridz=w["gridz"], materials=w["materials"], boreholes=w["boreholes"],
+                         inlet_model=w["inlet_model"])
+    sol = solve(ODEProblem(rhs_diffusion_z, w["T0"], (0.0, nsteps * w["dt"]), cache),
+                ROCK2(max_stages=100, eigen_est=eigen_estimator), dt=w["dt"], adaptive=False)
+    cache.close()
+    return sol
+
+
+@pytest.mark.parametrize("name", list(CASES) + ["2mm"])
+def test_refine_double_float_matches_double(name, gwlib, monkeypatch):
+    """GW_MIXED_REFINE forms its residual in double-float on the FP32 pipe
+    (k_half_refine_df, the default) or in double (k_half_refine,
+    GW_REFINE_F64=1).  Both residuals are exact far below the float rounding
+    of the corrected field, so the two refined fields differ only where x + d
+    rounds to neighbouring floats (carried on by the later steps), and the
+    double-float one is as close to the FP64 solution as the double one."""
+    w = W.single_well_2mm() if name == "2mm" else W.small_case(**CASES[name])
+    n = 4
+    ref = fp64_run(w, n)
+    monkeypatch.setenv("GW_REFINE_F64", "1")
+    c0, d64 = mixed_run(w, n, _lib.GW_MIXED_REFINE)
+    monkeypatch.delenv("GW_REFINE_F64")
+    c1, dff = mixed_run(w, n, _lib.GW_MIXED_REFINE)
+    e64 = np.max(np.abs(d64.u[-1] - ref.u[-1]))
+    eff = np.max(np.abs(dff.u[-1] - ref.u[-1]))
+    o64 = np.max(np.abs(d64.T_outlet - ref.T_outlet))
+    off = np.max(np.abs(dff.T_outlet - ref.T_outlet))
+    assert eff <= 1.25 * e64 + 2e-5, (eff, e64)
+    assert off <= 1.25 * o64 + 2e-6, (off, o64)
+    assert np.max(np.abs(dff.u[-1] - d64.u[-1])) < 2e-4
+    c0.close(); c1.close()
