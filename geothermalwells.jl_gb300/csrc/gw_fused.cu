@@ -870,7 +870,8 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                                                         const T *__restrict__ fib,
                                                         const T *__restrict__ fcu, int nx, int ny,
                                                         int nz, int pz, int countz, int m_begin, int m_end,
-                                                        const __grid_constant__ CUtensorMap tmap, int *err) {
+                                                        const __grid_constant__ CUtensorMap tmap,
+                                                        const __grid_constant__ CUtensorMap qmap, int *err) {
     static_assert(!TMA || sizeof(T) == 4, "tensor-map tiles: float fields only");
     static_assert(TMA || NB == 2, "the cp.async path double-buffers");
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -879,7 +880,12 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     constexpr int kTile = HR * kRow;
     constexpr int kRowS = (TMA && !XL) ? 32 : kRow;        // rows apart in a tile
     constexpr int kSlotS = (TMA && !XL) ? HR * 32 : 32;    // line slots apart in a tile
-    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(smem_raw + (size_t)NB * kTile * sizeof(T));
+    // TMA: the chunk's row coefficients of the block's lines for the block's
+    // z-class ([line][row] quads) arrive with the tile, on its mbarrier
+    constexpr int kQ = HW * HR;
+    Quad<T> *qtile = reinterpret_cast<Quad<T> *>(smem_raw + (size_t)NB * kTile * sizeof(T));
+    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(
+        smem_raw + (size_t)NB * kTile * sizeof(T) + (TMA ? (size_t)NB * kQ * sizeof(Quad<T>) : 0));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nl = XL ? ny : nx;   // lines per level
     const int N = XL ? nx : ny;    // line length
@@ -891,7 +897,13 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     // element (k, line m, row l): x-lines (k, j=m, i=l), y-lines (k, i=m, j=l)
     const long long mst = XL ? (long long)pz : (long long)pz * ny;
     const long long rst = XL ? (long long)pz * ny : (long long)pz;
-    const size_t fb = ((size_t)(GW_OK_G(zclass + kc, 112) ? zclass[kc] : 0) * nl + mc) * N;
+    const int zcl = GW_OK_G(zclass + kc, 112) ? zclass[kc] : 0;
+    const size_t fb = ((size_t)zcl * nl + mc) * N;
+    // the block's z-class (its first level's): lanes of another class, at a
+    // class boundary, read their coefficients from global memory
+    const int kb0 = k0 < nz ? k0 : nz - 1;
+    const int zcb = GW_OK_G(zclass + kb0, 112) ? zclass[kb0] : 0;
+    const bool qs_ok = TMA && zcl == zcb;
     const int *pline = pipe_line + (size_t)mc * N;
     // lines through no pipe column skip the per-row pipe lookup (most lines)
     const bool pipe_levels = k < countz && GW_OK_G(pipe_line + (size_t)nl * N + mc, 113) &&
@@ -925,11 +937,12 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
             if (threadIdx.x == 0) {
                 // the buffer's previous chunk was read through the generic proxy
                 asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                mbar_expect_tx(mbar + buf, (unsigned)(kTile * sizeof(T)));
+                mbar_expect_tx(mbar + buf, (unsigned)(kTile * sizeof(T) + kQ * sizeof(Quad<T>)));
                 if (XL)
                     tma_tile3(t, &tmap, k0, m0 - 1, l0, mbar + buf);
                 else
                     tma_tile3(t, &tmap, k0, l0, m0 - 1, mbar + buf);
+                tma_tile3(qtile + buf * kQ, &qmap, 4 * l0, m0, zcb, mbar + buf);
             }
             return;
         }
@@ -981,6 +994,11 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
         const T *row = tile + buf * kTile + warp * kSlotS + lane;
         const int l0 = ch * HR;
         const Quad<T> *qc = hql + l0;
+        const Quad<T> *qsm = qtile + buf * kQ + warp * HR;   // this line's staged quads (TMA)
+        auto quad = [&](int r) -> Quad<T> {
+            if (qs_ok) return GW_OK_D(qsm + r, smem_raw, 114) ? qsm[r] : Quad<T>{};
+            return GW_OK_G(qc + r, 104) ? qc[r] : Quad<T>{};
+        };
         if (l0 + HR <= N && !line_pipe) {
             // full chunk, no pipe column on the line: straight-line rows
 #pragma unroll
@@ -989,7 +1007,7 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                 T xm[kHG], xc[kHG], xp[kHG];
 #pragma unroll
                 for (int g = 0; g < kHG; ++g) {
-                    q[g] = GW_OK_G(qc + r0 + g, 104) ? qc[r0 + g] : Quad<T>{};
+                    q[g] = quad(r0 + g);
                     const T *rw = row + (r0 + g) * kRowS;
                     xm[g] = rd(rw); xc[g] = rd(rw + kSlotS); xp[g] = rd(rw + 2 * kSlotS);
                 }
@@ -1011,7 +1029,7 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                 int pq[kHG];
 #pragma unroll
                 for (int g = 0; g < kHG; ++g) {
-                    q[g] = GW_OK_G(qc + r0 + g, 104) ? qc[r0 + g] : Quad<T>{};
+                    q[g] = quad(r0 + g);
                     const T *rw = row + (r0 + g) * kRowS;
                     xm[g] = rd(rw); xc[g] = rd(rw + kSlotS); xp[g] = rd(rw + 2 * kSlotS);
                     pq[g] = pipe_levels && GW_OK_G(pline + l0 + r0 + g, 105) ? __ldg(pline + l0 + r0 + g) : -1;
@@ -1033,7 +1051,7 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
             const int rmax = min(HR, N - l0);
             for (int r = 0; r < rmax; ++r) {
                 const int l = l0 + r;
-                const Quad<T> q = GW_OK_G(qc + r, 104) ? qc[r] : Quad<T>{};
+                const Quad<T> q = quad(r);
                 const T *rw = row + r * kRowS;
                 const T ay = q.w * y;
                 T yn = fma(q.x, rd(rw + kSlotS), fma(q.y, rd(rw + 2 * kSlotS), fma(q.z, rd(rw), -ay)));
@@ -1712,7 +1730,9 @@ size_t half_smem(int cfg) { return 2 * (size_t)kTileHR[cfg] * (kTileHW[cfg] + 2)
 // shared memory with the ring's mbarriers
 constexpr int kTileNB[6] = {3, 3, 3, 2, 3, 2};
 template <int HW, int HR, int NB>
-constexpr size_t tma_smem() { return (size_t)NB * HR * (HW + 2) * 32 * sizeof(float) + 8 * NB; }
+constexpr size_t tma_smem() {
+    return (size_t)NB * HR * (HW + 2) * 32 * sizeof(float) + (size_t)NB * HW * HR * 4 * sizeof(float) + 8 * NB;
+}
 
 // the tensor map of src's tiles, or null (another buffer, or no maps)
 inline const CUtensorMap *tile_map(const gw_ctx *c, const void *src, int xlines, int cfg) {
@@ -1723,30 +1743,32 @@ inline const CUtensorMap *tile_map(const gw_ctx *c, const void *src, int xlines,
 
 template <typename T, int HW, int HR, int NB>
 void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, const Quad<T> *hq,
-                 const GwFactors<T> &f, const T *pp, size_t smem, int mb, int me, const CUtensorMap *map) {
+                 const GwFactors<T> &f, const T *pp, size_t smem, int mb, int me, const CUtensorMap *map,
+                 const CUtensorMap *qmap) {
     static const CUtensorMap kNoMap = {};
     dim3 grid((c->nz + 31) / 32, (me - mb + HW - 1) / HW);
     if constexpr (sizeof(T) == 4) {
-        if (map) {
+        if (map && qmap) {
+            const CUtensorMap &qm = *qmap;
             if (xlines)
                 k_half_tile<T, true, HW, HR, NB, true><<<grid, 32 * HW, tma_smem<HW, HR, NB>(), st>>>(
                     dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
-                    mb, me, *map, c->d_err);
+                    mb, me, *map, qm, c->d_err);
             else
                 k_half_tile<T, false, HW, HR, NB, true><<<grid, 32 * HW, tma_smem<HW, HR, NB>(), st>>>(
                     dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
-                    mb, me, *map, c->d_err);
+                    mb, me, *map, qm, c->d_err);
             return;
         }
     }
     if (xlines)
         k_half_tile<T, true, HW, HR><<<grid, 32 * HW, smem, st>>>(
             dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz, mb, me,
-            kNoMap, c->d_err);
+            kNoMap, kNoMap, c->d_err);
     else
         k_half_tile<T, false, HW, HR><<<grid, 32 * HW, smem, st>>>(
             dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz, mb, me,
-            kNoMap, c->d_err);
+            kNoMap, kNoMap, c->d_err);
 }
 
 template <typename T>
@@ -1780,13 +1802,14 @@ int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h, int mb = 
     }
     const size_t sm = half_smem<T>(cfg);
     const CUtensorMap *map = sizeof(T) == 4 ? tile_map(c, src, xlines, cfg) : nullptr;
+    const CUtensorMap *qmap = map ? &c->qmaps[xlines ? 0 : 1][cfg] : nullptr;
     switch (cfg) {
-        case 1: half_launch<T, 8, 16, kTileNB[1]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
-        case 2: half_launch<T, 8, 8, kTileNB[2]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
-        case 3: half_launch<T, 4, 32, kTileNB[3]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
-        case 4: half_launch<T, 2, 16, kTileNB[4]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
-        case 5: half_launch<T, 8, 32, kTileNB[5]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
-        default: half_launch<T, 4, 16, kTileNB[0]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map); break;
+        case 1: half_launch<T, 8, 16, kTileNB[1]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
+        case 2: half_launch<T, 8, 8, kTileNB[2]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
+        case 3: half_launch<T, 4, 32, kTileNB[3]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
+        case 4: half_launch<T, 2, 16, kTileNB[4]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
+        case 5: half_launch<T, 8, 32, kTileNB[5]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
+        default: half_launch<T, 4, 16, kTileNB[0]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
     }
     GW_CUDA(cudaGetLastError());
     return GW_OK;
@@ -1897,6 +1920,21 @@ void encode_tile_maps(gw_ctx *c) {
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
                     return;
             }
+    // the half-step coefficient quads, [z-class][line][row] float4: a tensor of
+    // (4 floats x rows, lines, z-classes); box: a chunk's rows x the block's lines
+    for (int d = 0; d < 2; ++d) {
+        const int nl = d == 0 ? c->ny : c->nx, N = d == 0 ? c->nx : c->ny;
+        const cuuint64_t qd[3] = {(cuuint64_t)4 * N, (cuuint64_t)nl, (cuuint64_t)c->n_zclass};
+        const cuuint64_t qs[2] = {(cuuint64_t)N * 4 * sizeof(float), (cuuint64_t)nl * N * 4 * sizeof(float)};
+        float *tab = d == 0 ? c->c32.hx : c->c32.hy;
+        for (int cfg = 0; cfg < 6; ++cfg) {
+            const cuuint32_t box[3] = {(cuuint32_t)(4 * kTileHR[cfg]), (cuuint32_t)kTileHW[cfg], 1};
+            if (enc(&c->qmaps[d][cfg], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, tab, qd, qs, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return;
+        }
+    }
     c->tma_ok = true;
 }
 

@@ -137,6 +137,7 @@ struct gw_ctx {
     int pz = 0;                       // level pitch of the fused fields: nz (FP64), nz rounded up to 4 (mixed)
     // mixed path: 3-D tensor maps of the half-step tiles, [source: f_u, f_temp][x-, y-lines][tiling]
     CUtensorMap tmaps[2][2][6];
+    CUtensorMap qmaps[2][6];          // their row-coefficient quads, [x-, y-lines][tiling]
     bool tma_ok = false;              // maps encoded (else the half step copies with cp.async)
     int *d_err = nullptr;             // set by a kernel whose bounded wait ran out
     int rock2w_per_sm[9] = {};        // resident blocks per SM of the window ROCK2 kernel, by LPT
