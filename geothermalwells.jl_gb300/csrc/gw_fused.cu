@@ -639,10 +639,22 @@ __global__ void __launch_bounds__(32 * kReduceWarps) k_pipe_reduce(double *__res
     const int i0 = bchunk[4 * b], i1 = bchunk[4 * b + 1], o0 = bchunk[4 * b + 2], o1 = bchunk[4 * b + 3];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int k = blockIdx.x * 32 + lane;
+    // four running sums (chunks w, w + 8, w + 16, w + 24 of each round of 32),
+    // so four loads are in flight; they are added in a fixed order
     double sacc = 0.0;
-    if (k < nz)
-        for (int ch = o0 + w; ch < o1; ch += kReduceWarps)
-            sacc += GW_OK_G(part + (size_t)ch * nz + k, 313) ? part[(size_t)ch * nz + k] : 0.0;
+    if (k < nz) {
+        auto ld = [&](int ch) { return GW_OK_G(part + (size_t)ch * nz + k, 313) ? part[(size_t)ch * nz + k] : 0.0; };
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        int ch = o0 + w;
+        for (; ch + 3 * kReduceWarps < o1; ch += 4 * kReduceWarps) {
+            a0 += ld(ch);
+            a1 += ld(ch + kReduceWarps);
+            a2 += ld(ch + 2 * kReduceWarps);
+            a3 += ld(ch + 3 * kReduceWarps);
+        }
+        for (; ch < o1; ch += kReduceWarps) a0 += ld(ch);
+        sacc = (a0 + a1) + (a2 + a3);
+    }
     s_red[threadIdx.x] = sacc;
     __syncthreads();
     if (w == 0 && k < nz) {
@@ -654,10 +666,25 @@ __global__ void __launch_bounds__(32 * kReduceWarps) k_pipe_reduce(double *__res
     if (blockIdx.x != 0) return;   // the whole block: the outlet is block 0's
     __syncthreads();   // every read of s_red above is done
     const int nlev = GW_OK_G(nlev_b + b, 315) ? nlev_b[b] : 0;
+    // (chunk, level) elements, level fastest (coalesced), spread over the
+    // block; each thread keeps four running sums (four loads in flight),
+    // added in a fixed order
     const int total = nlev * (i1 - i0);
-    double acc = 0.0;
-    for (int e = threadIdx.x; e < total; e += blockDim.x)   // level fastest: coalesced
-        acc += GW_OK_G(part + (size_t)(i0 + e / nlev) * nz + e % nlev, 313) ? part[(size_t)(i0 + e / nlev) * nz + e % nlev] : 0.0;
+    auto ld = [&](int e) {
+        const size_t q = (size_t)(i0 + e / nlev) * nz + e % nlev;
+        return GW_OK_G(part + q, 313) ? part[q] : 0.0;
+    };
+    const int bd = blockDim.x;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int e = threadIdx.x;
+    for (; e + 3 * bd < total; e += 4 * bd) {
+        a0 += ld(e);
+        a1 += ld(e + bd);
+        a2 += ld(e + 2 * bd);
+        a3 += ld(e + 3 * bd);
+    }
+    for (; e < total; e += bd) a0 += ld(e);
+    const double acc = (a0 + a1) + (a2 + a3);
     s_red[threadIdx.x] = acc;
     __syncthreads();
     for (int r = blockDim.x / 2; r > 0; r >>= 1) {
