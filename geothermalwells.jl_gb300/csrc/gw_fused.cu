@@ -84,6 +84,57 @@ __device__ __forceinline__ void tma_tile3(void *dst, const CUtensorMap *map, int
         : "memory");
 }
 
+// Tensor memory (TMEM, 128 lanes x 512 32-bit columns per SM) as a scratch
+// store of the half step's forward-elimination values.  Allocation by one
+// warp (the address lands in shared memory), freed by the same warp before
+// the block exits; a warp reaches only its lane quarter (lanes
+// 32 (warp % 4) ..), one lane per thread with the 32x32b shapes.
+__device__ __forceinline__ void tm_alloc(unsigned *slot, unsigned ncols) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(slot);
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(a), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void tm_dealloc(unsigned taddr, unsigned ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tm_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tm_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tm_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory"); }
+// 8 / 16 consecutive columns of this thread's lane
+__device__ __forceinline__ void tm_st8(unsigned ta, const float *v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};\n" ::"r"(ta),
+                 "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+                 : "memory");
+}
+__device__ __forceinline__ void tm_st16(unsigned ta, const float *v) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16};\n" ::"r"(ta),
+        "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
+        "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
+        : "memory");
+}
+__device__ __forceinline__ void tm_ld16(unsigned ta, float *v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]),
+          "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15])
+        : "r"(ta)
+        : "memory");
+}
+// the registers of the loads before it hold their values only after this
+// wait: they pass through it, so no use of them moves above it
+__device__ __forceinline__ void tm_wait_ld(float *v) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n"
+                 : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7]),
+                   "+f"(v[8]), "+f"(v[9]), "+f"(v[10]), "+f"(v[11]), "+f"(v[12]), "+f"(v[13]), "+f"(v[14]),
+                   "+f"(v[15])
+                 :
+                 : "memory");
+}
+
 // ---------------------------------------------------------------------------
 // 1. ROCK2 on whole columns
 // sc: per recurrence stage j = 1..s-2: (h mu_j, kappa_j); then (h sigma,
@@ -888,7 +939,20 @@ struct alignas(4 * sizeof(T)) Quad {
 // and awaited on the buffer's mbarrier.  Tile layout: [row][line][32] for the
 // x-lines and the cp.async path, [line][row][32] for TMA y-lines (the tensor's
 // dimensions are levels, j, i).
-template <typename T, bool XL, int HW, int HR, int NB = 2, bool TMA = false>
+//
+// TM (with TMA; blocks of 4 or 8 lines): the forward values stay on chip, in
+// tensor memory.  The block allocates tm_cw columns (a power of two >= N) per
+// line slot -- a warp uses its TMEM lane quarter (warp % 4), warps w and w + 4
+// the column blocks 0 and tm_cw -- after its first tiles are in flight (the
+// allocation waits while other blocks of the SM hold the 512 columns; those
+// blocks, resident with their first tiles loaded, start at once when it is
+// freed).  Each chunk's y_l of a lane go to its TMEM lane as HR consecutive
+// columns; the backward sweep reads them 16 at a time, the next batch and
+// its coefficients in flight, and writes x_l.  The field then crosses HBM
+// once per direction plus the halo lines, with no y_l round trip through L2,
+// and the values and their order of operations are those of the global-memory
+// form: bitwise the same field.
+template <typename T, bool XL, int HW, int HR, int NB = 2, bool TMA = false, bool TM = false>
 __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, const T *__restrict__ src,
                                                         const T *__restrict__ pp,
                                                         const int *__restrict__ pipe_line,
@@ -898,9 +962,11 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                                                         const T *__restrict__ fcu, int nx, int ny,
                                                         int nz, int pz, int countz, int m_begin, int m_end,
                                                         const __grid_constant__ CUtensorMap tmap,
-                                                        const __grid_constant__ CUtensorMap qmap, int *err) {
+                                                        const __grid_constant__ CUtensorMap qmap, int *err,
+                                                        int tm_cw = 0) {
     static_assert(!TMA || sizeof(T) == 4, "tensor-map tiles: float fields only");
     static_assert(TMA || NB == 2, "the cp.async path double-buffers");
+    static_assert(!TM || (TMA && (HR == 8 || HR == 16 || HR == 32)), "TMEM forward values: TMA tiles of 8-32 rows");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T *tile = reinterpret_cast<T *>(smem_raw);   // [NB][tile]
     constexpr int kRow = (HW + 2) * 32;
@@ -913,6 +979,7 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     Quad<T> *qtile = reinterpret_cast<Quad<T> *>(smem_raw + (size_t)NB * kTile * sizeof(T));
     unsigned long long *mbar = reinterpret_cast<unsigned long long *>(
         smem_raw + (size_t)NB * kTile * sizeof(T) + (TMA ? (size_t)NB * kQ * sizeof(Quad<T>) : 0));
+    unsigned *tslot = reinterpret_cast<unsigned *>(mbar + NB);   // TM: the TMEM allocation's address
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nl = XL ? ny : nx;   // lines per level
     const int N = XL ? nx : ny;    // line length
@@ -996,14 +1063,37 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
 
     T y = T(0);
     T *dr = dl;
+    const unsigned tm_cols = TM ? (unsigned)tm_cw * ((HW + 3) / 4) : 0u;
+    unsigned tbase = 0, taddr = 0;
+    T yb[TM ? HR : 1];   // TM: the chunk's forward values of this lane
     if constexpr (TMA) {
         if (threadIdx.x < NB) mbar_init(mbar + threadIdx.x, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         __syncthreads();
         for (int b = 0; b < NB - 1 && b < nchunk; ++b) load_chunk(b, b);
+        if constexpr (TM) {
+            if (warp == 0) {
+                __syncwarp();
+                tm_alloc(tslot, tm_cols);
+            }
+            tm_fence_before();
+            __syncthreads();
+            tm_fence_after();
+            tbase = *tslot;
+            taddr = tbase + ((unsigned)(32 * (warp & 3)) << 16) + (unsigned)((warp >> 2) * tm_cw);
+        }
     } else {
         load_chunk(0, 0);
     }
+    auto put = [&](int r, T v) {
+        if constexpr (TM) {
+            yb[r] = v;
+        } else {
+            (void)r;
+            if (active && GW_OK_G(dr, 108)) *dr = v;
+            dr += rst;
+        }
+    };
     for (int ch = 0; ch < nchunk; ++ch) {
         const int buf = TMA ? ch % NB : ch & 1;
         if constexpr (TMA) {
@@ -1041,8 +1131,7 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
 #pragma unroll
                 for (int g = 0; g < kHG; ++g) {
                     y = fma(q[g].x, xc[g], fma(q[g].y, xp[g], fma(q[g].z, xm[g], -q[g].w * y)));
-                    if (active && GW_OK_G(dr, 108)) *dr = y;
-                    dr += rst;
+                    put(r0 + g, y);
                 }
             }
         } else if (l0 + HR <= N) {
@@ -1070,13 +1159,12 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                 for (int g = 0; g < kHG; ++g) {
                     const T ay = q[g].w * y;
                     y = pq[g] >= 0 ? fma(pv[g], iv[g], -ay) : fma(q[g].x, xc[g], fma(q[g].y, xp[g], fma(q[g].z, xm[g], -ay)));
-                    if (active && GW_OK_G(dr, 108)) *dr = y;
-                    dr += rst;
+                    put(r0 + g, y);
                 }
             }
         } else {
             const int rmax = min(HR, N - l0);
-            for (int r = 0; r < rmax; ++r) {
+            auto row_step = [&](int r) {
                 const int l = l0 + r;
                 const Quad<T> q = quad(r);
                 const T *rw = row + r * kRowS;
@@ -1087,11 +1175,90 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                     yn = fma(GW_OK_G(pp + (size_t)pq * countz + k, 106) ? pp[(size_t)pq * countz + k] : T(0),
                              GW_OK_G(fib + fb + l, 107) ? __ldg(fib + fb + l) : T(0), -ay);
                 y = yn;
-                if (active && GW_OK_G(dr, 108)) *dr = y;
-                dr += rst;
+            };
+            if constexpr (TM) {
+#pragma unroll
+                for (int r = 0; r < HR; ++r) {
+                    if (r < rmax) row_step(r);
+                    yb[r] = y;
+                }
+            } else {
+                for (int r = 0; r < rmax; ++r) {
+                    row_step(r);
+                    put(r, y);
+                }
+            }
+        }
+        if constexpr (TM) {
+            __syncwarp();
+            if (GW_OK_I(l0 + HR - 1, tm_cw, 115)) {
+                if constexpr (HR == 8) {
+                    tm_st8(taddr + l0, yb);
+                } else {
+                    tm_st16(taddr + l0, yb);
+                    if constexpr (HR == 32) tm_st16(taddr + l0 + 16, yb + 16);
+                }
             }
         }
         __syncthreads();   // the buffer is refilled NB - 1 chunks later
+    }
+    if constexpr (TM) {
+        tm_wait_st();
+        if (m < m_end) {
+            const T *cuf = fcu + fb;
+            if (kok && GW_OK_G(dl + (long long)(N - 1) * rst, 111)) __stcs(dl + (long long)(N - 1) * rst, y);
+            T x = y;
+            if (N >= 2) {
+                int cb = (N - 2) >> 4;
+                float cur[16], nxt[16];
+                T cuc[16], cun[16];
+                const bool cok = GW_OK_I(16 * cb + 15, tm_cw, 116);
+                if (cok) tm_ld16(taddr + 16 * cb, cur);
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    cuc[j] = 16 * cb + j < N && GW_OK_G(cuf + 16 * cb + j, 110) ? __ldg(cuf + 16 * cb + j) : T(0);
+                if (cok) tm_wait_ld(cur);
+                for (;;) {
+                    const int r0 = 16 * cb;
+                    if (cb > 0) {
+                        tm_ld16(taddr + r0 - 16, nxt);
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            cun[j] = GW_OK_G(cuf + r0 - 16 + j, 110) ? __ldg(cuf + r0 - 16 + j) : T(0);
+                    }
+                    T *pc = dl + (long long)r0 * rst;
+                    if (r0 + 15 <= N - 2) {
+#pragma unroll
+                        for (int j = 15; j >= 0; --j) {
+                            x = cur[j] - cuc[j] * x;
+                            if (kok && GW_OK_G(pc + (long long)j * rst, 111)) __stcs(pc + (long long)j * rst, x);
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 15; j >= 0; --j) {
+                            if (r0 + j <= N - 2) {
+                                x = cur[j] - cuc[j] * x;
+                                if (kok && GW_OK_G(pc + (long long)j * rst, 111))
+                                    __stcs(pc + (long long)j * rst, x);
+                            }
+                        }
+                    }
+                    if (cb == 0) break;
+                    tm_wait_ld(nxt);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) { cur[j] = nxt[j]; cuc[j] = cun[j]; }
+                    --cb;
+                }
+            }
+        }
+        tm_fence_before();
+        __syncthreads();
+        tm_fence_after();
+        if (warp == 0) {
+            __syncwarp();
+            tm_dealloc(tbase, tm_cols);
+        }
+        return;
     }
     if (!active) return;
     // backward sweep: batches of kHB rows are loaded before the previous
@@ -1758,7 +1925,18 @@ size_t half_smem(int cfg) { return 2 * (size_t)kTileHR[cfg] * (kTileHW[cfg] + 2)
 constexpr int kTileNB[6] = {3, 3, 3, 2, 3, 2};
 template <int HW, int HR, int NB>
 constexpr size_t tma_smem() {
-    return (size_t)NB * HR * (HW + 2) * 32 * sizeof(float) + (size_t)NB * HW * HR * 4 * sizeof(float) + 8 * NB;
+    return (size_t)NB * HR * (HW + 2) * 32 * sizeof(float) + (size_t)NB * HW * HR * 4 * sizeof(float) + 8 * NB + 16;
+}
+
+// TMEM columns per line slot of the TM half step: a power of two >= N (and
+// >= 32, the smallest allocation); 0 for blocks of fewer than four lines
+// (half of the TMEM lanes would stay unused) or whose slots would not fit the
+// SM's 512 columns: the forward values then go through global memory
+inline int tm_columns(int N, int HW) {
+    if (HW < 4) return 0;
+    int cw = 32;
+    while (cw < N) cw *= 2;
+    return cw * ((HW + 3) / 4) <= 512 ? cw : 0;
 }
 
 // the tensor map of src's tiles, or null (another buffer, or no maps)
@@ -1775,6 +1953,20 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
     static const CUtensorMap kNoMap = {};
     dim3 grid((c->nz + 31) / 32, (me - mb + HW - 1) / HW);
     if constexpr (sizeof(T) == 4) {
+        // forward values in TMEM where the block's lines fit the SM's columns
+        const int cw = c->half_tmem && map && qmap ? tm_columns(xlines ? c->nx : c->ny, HW) : 0;
+        if (cw > 0) {
+            const CUtensorMap &qm = *qmap;
+            if (xlines)
+                k_half_tile<T, true, HW, HR, NB, true, true><<<grid, 32 * HW, tma_smem<HW, HR, NB>(), st>>>(
+                    dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
+                    mb, me, *map, qm, c->d_err, cw);
+            else
+                k_half_tile<T, false, HW, HR, NB, true, true><<<grid, 32 * HW, tma_smem<HW, HR, NB>(), st>>>(
+                    dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
+                    mb, me, *map, qm, c->d_err, cw);
+            return;
+        }
         if (map && qmap) {
             const CUtensorMap &qm = *qmap;
             if (xlines)
@@ -1888,6 +2080,12 @@ cudaError_t half_attr() {
         if ((e = cudaFuncSetAttribute(k_half_tile<T, true, HW, HR, NB, true>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, st)))
             return e;
+        if ((e = cudaFuncSetAttribute(k_half_tile<T, true, HW, HR, NB, true, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, st)))
+            return e;
+        if ((e = cudaFuncSetAttribute(k_half_tile<T, false, HW, HR, NB, true, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, st)))
+            return e;
         return cudaFuncSetAttribute(k_half_tile<T, false, HW, HR, NB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     st);
     }
@@ -1897,9 +2095,12 @@ cudaError_t half_attr() {
 template <typename T>
 cudaError_t half_attrs() {
     cudaError_t e;
-    if ((e = half_attr<T, 8, 16, kTileNB[1]>()) != cudaSuccess || (e = half_attr<T, 4, 16, kTileNB[0]>()) != cudaSuccess ||
-        (e = half_attr<T, 8, 8, kTileNB[2]>()) != cudaSuccess || (e = half_attr<T, 4, 32, kTileNB[3]>()) != cudaSuccess ||
-        (e = half_attr<T, 2, 16, kTileNB[4]>()) != cudaSuccess || (e = half_attr<T, 8, 32, kTileNB[5]>()) != cudaSuccess)
+    if ((e = half_attr<T, 8, 16, kTileNB[1]>()) != cudaSuccess ||
+        (e = half_attr<T, 4, 16, kTileNB[0]>()) != cudaSuccess ||
+        (e = half_attr<T, 8, 8, kTileNB[2]>()) != cudaSuccess ||
+        (e = half_attr<T, 4, 32, kTileNB[3]>()) != cudaSuccess ||
+        (e = half_attr<T, 2, 16, kTileNB[4]>()) != cudaSuccess ||
+        (e = half_attr<T, 8, 32, kTileNB[5]>()) != cudaSuccess)
         return e;
     return cudaSuccess;
 }
@@ -2094,6 +2295,11 @@ int gw_fused_prepare(gw_ctx *c) {
     // tensor-map tiles for the mixed half steps (GW_HALF_CPASYNC=1 keeps cp.async)
     const char *hc = std::getenv("GW_HALF_CPASYNC");
     if (!(hc && *hc && *hc != '0')) encode_tile_maps(c);
+    // forward values of the tensor-map half steps in TMEM (GW_HALF_GLOBAL=1
+    // keeps them in global memory)
+    const char *hg = std::getenv("GW_HALF_GLOBAL");
+    c->half_tmem = !(hg && *hg && *hg != '0');
+
     return GW_OK;
 }
 

@@ -1,0 +1,99 @@
+"""The mixed half step with its forward-elimination values in tensor memory
+(TMEM; the default of the tensor-map half step) against the same kernel with
+the values stored to and reloaded from global memory (GW_HALF_GLOBAL=1).
+Both evaluate the same recurrences in the same order, so the fields and
+outlet series must agree bitwise: every tiling, in-line and overlapped steps,
+lines of 36..88 rows (partial chunks and partial backward batches), lines
+longer than 256 rows (the 8-line tilings then keep their values in global
+memory, the others take 512 TMEM columns), and the two benchmark wells."""
+import numpy as np
+import pytest
+
+from geothermalwells_gb300 import (GB300, ODEProblem, ROCK2, create_cache, eigen_estimator,
+                                   rhs_diffusion_z, solve)
+from geothermalwells_gb300 import _lib
+from geothermalwells_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def refined(w, times):
+    """The case with every x interval split in two, `times` times (more rows
+    per x-line; the pipes keep their grid columns)."""
+    gx = np.asarray(w["gridx"], dtype=np.float64)
+    for _ in range(times):
+        mid = 0.5 * (gx[1:] + gx[:-1])
+        gx = np.sort(np.concatenate([gx, mid]))
+    w = dict(w)
+    w["gridx"] = gx
+    w["T0"] = W.initial_condition_thermal_gradient(None, np.float64, gx, w["gridy"], w["gridz"],
+                                                   T_surface=5.0, gradient=0.5)
+    return w
+
+
+CASES = {
+    "single": lambda: W.small_case(),                                                   # 36 x 36 x 14
+    "three_wells_layers_hx": lambda: W.small_case(n_layers=3, inlet="hx", nbh=3, nz_cells=40),   # 88 x 40
+    "deep": lambda: W.small_case(nz_cells=300, n_layers=2),                             # nz = 301
+    "2mm": W.single_well_2mm,
+    "large": W.single_well_large,
+}
+
+
+def run(w, monkeypatch, global_y, tiling=None, overlap=None, nsteps=3):
+    monkeypatch.delenv("GW_HALF_CPASYNC", raising=False)
+    if global_y:
+        monkeypatch.setenv("GW_HALF_GLOBAL", "1")
+    else:
+        monkeypatch.delenv("GW_HALF_GLOBAL", raising=False)
+    c = create_cache(backend=GB300(precision="mixed"), gridx=w["gridx"], gridy=w["gridy"],
+                     gridz=w["gridz"], materials=w["materials"], boreholes=w["boreholes"],
+                     inlet_model=w["inlet_model"])
+    L = _lib.load()
+    if tiling is not None:
+        _lib.check(L.gw_set_tiling(c.ctx, tiling))
+    if overlap is not None:
+        _lib.check(L.gw_set_overlap(c.ctx, overlap))
+    sol = solve(ODEProblem(rhs_diffusion_z, w["T0"], (0.0, nsteps * w["dt"]), c),
+                ROCK2(max_stages=100, eigen_est=eigen_estimator), dt=w["dt"])
+    c.close()
+    return sol
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_tmem_equals_global(name, gwlib, monkeypatch):
+    w = CASES[name]()
+    n = 2 if name in ("2mm", "large") else 3
+    a = run(w, monkeypatch, global_y=True, nsteps=n)
+    b = run(w, monkeypatch, global_y=False, nsteps=n)
+    assert np.all(np.isfinite(b.u[-1]))
+    assert np.array_equal(a.u[-1], b.u[-1])
+    assert np.array_equal(a.T_outlet, b.T_outlet)
+
+
+@pytest.mark.parametrize("tiling", range(6))
+def test_every_tiling(tiling, gwlib, monkeypatch):
+    w = W.small_case(n_layers=2, nbh=2, nz_cells=30)
+    a = run(w, monkeypatch, global_y=True, tiling=tiling)
+    b = run(w, monkeypatch, global_y=False, tiling=tiling)
+    assert np.array_equal(a.u[-1], b.u[-1])
+    assert np.array_equal(a.T_outlet, b.T_outlet)
+
+
+@pytest.mark.parametrize("overlap", [0, 1])
+def test_overlapped_step(overlap, gwlib, monkeypatch):
+    w = W.small_case(n_layers=2, nbh=3, nz_cells=45)
+    a = run(w, monkeypatch, global_y=True, overlap=overlap)
+    b = run(w, monkeypatch, global_y=False, overlap=overlap)
+    assert np.array_equal(a.u[-1], b.u[-1])
+    assert np.array_equal(a.T_outlet, b.T_outlet)
+
+
+@pytest.mark.parametrize("tiling", [0, 1, 3, 4])
+def test_long_lines(tiling, gwlib, monkeypatch):
+    w = refined(W.small_case(nz_cells=20), 3)
+    assert len(w["gridx"]) > 256
+    a = run(w, monkeypatch, global_y=True, tiling=tiling)
+    b = run(w, monkeypatch, global_y=False, tiling=tiling)
+    assert np.array_equal(a.u[-1], b.u[-1])
+    assert np.array_equal(a.T_outlet, b.T_outlet)
