@@ -917,10 +917,12 @@ __global__ void __launch_bounds__(128) k_advect_c(T *__restrict__ pp, const T *_
 // for their backward sweep (large well: half steps 1-2 % faster).
 // Tilings (lines per block HW, rows per chunk HR); the autotuner picks one
 // per context, the default is the first.
-constexpr int kTilings = 7;   // the last one is the segmented kernel (k_half_seg)
-constexpr int kTileHW[kTilings] = {4, 8, 8, 4, 2, 8, 2};
-constexpr int kTileHR[kTilings] = {16, 16, 8, 32, 16, 32, 16};
+// 7 .. 12 are the row tiles of 0 .. 5 with the forward values in global memory.
+constexpr int kTilings = 13;   // 6 is the segmented kernel (k_half_seg)
+constexpr int kTileHW[kTilings] = {4, 8, 8, 4, 2, 8, 2, 4, 8, 8, 4, 2, 8};
+constexpr int kTileHR[kTilings] = {16, 16, 8, 32, 16, 32, 16, 16, 16, 8, 32, 16, 32};
 constexpr int kSegCfg = 6;
+constexpr int kGlobalCfg = 7;   // first tiling with the forward values in global memory
 static_assert(kTilings == GW_TILINGS, "tiling count of the C ABI");
 constexpr int kSegS = 8, kSegR = 32;   // segments per line, rows per segment (lines up to 256)
 constexpr int kHG = 4;    // rows whose coefficients are loaded together
@@ -1949,12 +1951,12 @@ inline const CUtensorMap *tile_map(const gw_ctx *c, const void *src, int xlines,
 template <typename T, int HW, int HR, int NB>
 void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, const Quad<T> *hq,
                  const GwFactors<T> &f, const T *pp, size_t smem, int mb, int me, const CUtensorMap *map,
-                 const CUtensorMap *qmap) {
+                 const CUtensorMap *qmap, bool tm) {
     static const CUtensorMap kNoMap = {};
     dim3 grid((c->nz + 31) / 32, (me - mb + HW - 1) / HW);
     if constexpr (sizeof(T) == 4) {
         // forward values in TMEM where the block's lines fit the SM's columns
-        const int cw = c->half_tmem && map && qmap ? tm_columns(xlines ? c->nx : c->ny, HW) : 0;
+        const int cw = tm && map && qmap ? tm_columns(xlines ? c->nx : c->ny, HW) : 0;
         if (cw > 0) {
             const CUtensorMap &qm = *qmap;
             if (xlines)
@@ -2003,6 +2005,9 @@ int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h, int mb = 
     if (me <= mb) return GW_OK;
     int cfg = c->half_cfg;
     const int N = xlines ? c->nx : c->ny;
+    // tilings 7..12: the row tiles 0..5 with the forward values in global memory
+    const bool tm = c->half_tmem && cfg < kSegCfg;
+    if (cfg >= kGlobalCfg) cfg -= kGlobalCfg;
     if (cfg == kSegCfg) {
         if (N <= kSegS * kSegR) {
             dim3 grid((c->nz + 31) / 32, (me - mb + 1) / 2);
@@ -2022,13 +2027,14 @@ int launch_half(gw_ctx *c, T *dst, const T *src, int xlines, double h, int mb = 
     const size_t sm = half_smem<T>(cfg);
     const CUtensorMap *map = sizeof(T) == 4 ? tile_map(c, src, xlines, cfg) : nullptr;
     const CUtensorMap *qmap = map ? &c->qmaps[xlines ? 0 : 1][cfg] : nullptr;
+
     switch (cfg) {
-        case 1: half_launch<T, 8, 16, kTileNB[1]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
-        case 2: half_launch<T, 8, 8, kTileNB[2]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
-        case 3: half_launch<T, 4, 32, kTileNB[3]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
-        case 4: half_launch<T, 2, 16, kTileNB[4]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
-        case 5: half_launch<T, 8, 32, kTileNB[5]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
-        default: half_launch<T, 4, 16, kTileNB[0]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap); break;
+        case 1: half_launch<T, 8, 16, kTileNB[1]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap, tm); break;
+        case 2: half_launch<T, 8, 8, kTileNB[2]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap, tm); break;
+        case 3: half_launch<T, 4, 32, kTileNB[3]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap, tm); break;
+        case 4: half_launch<T, 2, 16, kTileNB[4]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap, tm); break;
+        case 5: half_launch<T, 8, 32, kTileNB[5]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap, tm); break;
+        default: half_launch<T, 4, 16, kTileNB[0]>(c, st, dst, src, xlines, hq, f, B.pp, sm, mb, me, map, qmap, tm); break;
     }
     GW_CUDA(cudaGetLastError());
     return GW_OK;

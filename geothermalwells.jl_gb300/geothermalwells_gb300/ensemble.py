@@ -12,9 +12,12 @@ import numpy as np
 from . import _lib
 from .cache import GB300, create_cache
 
-# (lines per block, rows per chunk) of the tiled half step; the last entry is
-# the segmented half step (2 lines per block, 8 segments of up to 32 rows)
-TILINGS = ((4, 16), (8, 16), (8, 8), (4, 32), (2, 16), (8, 32), (2, "seg8x32"))
+# (lines per block, rows per chunk) of the tiled half step (mixed path: the
+# forward-elimination values in tensor memory where they fit); entry 6 is the
+# segmented half step (2 lines per block, 8 segments of up to 32 rows); 7-12
+# are the row tiles of 0-5 with the forward values in global memory
+_ROWS = ((4, 16), (8, 16), (8, 8), (4, 32), (2, 16), (8, 32))
+TILINGS = _ROWS + ((2, "seg8x32"),) + tuple((hw, hr, "global") for hw, hr in _ROWS)
 
 
 class Ensemble:

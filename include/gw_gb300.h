@@ -219,7 +219,7 @@ int gw_set_mixed_options(gw_ctx *ctx, int flags);
 
 /* Half-step kernel of this context (0 .. GW_TILINGS-1, see GW_TILINGS); all
  * give the same field bitwise except the segmented tiling 6.  gw_create picks
- * the default; gw_get_info reports the setting (tiling). */
+ * the default (0); gw_get_info reports the setting (tiling). */
 int gw_set_tiling(gw_ctx *ctx, int tiling);
 /* Stage count gw_step uses for dt (and whether its interval covers dt*lambda). */
 int gw_rock2_stages(gw_ctx *ctx, double dt, int max_stages, int *stages, int *covered);
@@ -277,8 +277,13 @@ int gw_profile_kernels(gw_ctx *ctx, double dt, int reps, double *ms_out);
  * by the caller and must outlive the batch; per-design state, outlet series
  * and energies are read with the single-context getters. */
 typedef struct gw_batch gw_batch;
-#define GW_TILINGS 7   /* half-step kernels: 0-5 row tiles (lines per block, rows per chunk),
-                          6 lines split into register-resident segments */
+#define GW_TILINGS 13  /* half-step kernels: 0-5 row tiles (lines per block, rows per chunk)
+                          of the mixed path keeping the forward-elimination values in tensor
+                          memory where the block's lines fit (blocks of 4 or 8 lines, lines
+                          of up to 512 / 256 rows); 6 lines split into register-resident
+                          segments; 7-12 the row tiles of 0-5 with the forward values in
+                          global memory (more resident blocks per SM, which pays when many
+                          designs run at once).  FP64 contexts: 7-12 are 0-5. */
 int gw_batch_create(gw_ctx *const *ctxs, int n, gw_batch **out);
 int gw_batch_destroy(gw_batch *batch);
 /* Use one tiling (0 .. GW_TILINGS-1) for every design (0 is the default). */
