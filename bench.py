@@ -58,6 +58,10 @@ def parse():
     p.add_argument("--accuracy-suite", action="store_true",
                    help="errors of every GPU path on every configuration (oracle / FP64 reference)")
     p.add_argument("--suite", default="", help="with --accuracy-suite: subset, e.g. cfg1,cfg2")
+    p.add_argument("--kernels", action="store_true",
+                   help="single-well workloads: only the per-kernel timing (each fused kernel "
+                        "launched --steps times on the full grid, outside the step graph)")
+    p.add_argument("--tiling", type=int, default=-1, help="half-step tiling of the context (default: its own)")
     return p.parse_args()
 
 
@@ -185,6 +189,28 @@ def run_reference(args):
             "e2e": {"value": cb["value"], "unit": METRIC, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def run_kernels(args):
+    """Per-kernel device times (CUDA events) of the fused step's kernels on
+    the full grid, each launched --steps times on its own: the launches a
+    single-kernel profiler capture selects."""
+    import ctypes
+    from geothermalwells_gb300 import _lib, create_cache, GB300
+    L = _lib.load()
+    w = workload(args.workload, args.dt)
+    cache = create_cache(backend=GB300(precision=args.precision), gridx=w["gridx"], gridy=w["gridy"],
+                         gridz=w["gridz"], materials=w["materials"], boreholes=w["boreholes"],
+                         inlet_model=w["inlet_model"])
+    cache.set_field(w["T0"])
+    if args.tiling >= 0:
+        _lib.check(L.gw_set_tiling(cache.ctx, args.tiling))
+    prof = (ctypes.c_double * len(_lib.KERNELS))()
+    _lib.check(L.gw_profile_kernels(cache.ctx, w["dt"], max(1, args.steps), prof))
+    print(json.dumps({"workload": w.get("name", args.workload), "precision": args.precision,
+                      "launches_per_kernel": max(1, args.steps),
+                      "kernel_ms": dict(zip(_lib.KERNELS, list(prof)))}), flush=True)
+    cache.close()
 
 
 def run_ours(args):
@@ -723,6 +749,9 @@ def main():
         return
     if args.accuracy:
         run_accuracy(args)
+        return
+    if args.kernels:
+        run_kernels(args)
         return
     if args.impl == "reference":
         run_reference(args)
