@@ -950,7 +950,10 @@ struct alignas(4 * sizeof(T)) Quad {
 // blocks, resident with their first tiles loaded, start at once when it is
 // freed).  Each chunk's y_l of a lane go to its TMEM lane as HR consecutive
 // columns; the backward sweep reads them 16 at a time, the next batch and
-// its coefficients in flight, and writes x_l.  The field then crosses HBM
+// its coefficients in flight, and writes x_l.  With tm_cw < N (the split
+// form: 128 columns, a ring of two) rows tm_cw .. N - 1 go to the block's
+// shared memory instead, which lets three blocks of 205-row lines work per
+// SM where whole lines in TMEM let two.  The field then crosses HBM
 // once per direction plus the halo lines, with no y_l round trip through L2,
 // and the values and their order of operations are those of the global-memory
 // form: bitwise the same field.
@@ -1068,6 +1071,12 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
     const unsigned tm_cols = TM ? (unsigned)tm_cw * ((HW + 3) / 4) : 0u;
     unsigned tbase = 0, taddr = 0;
     T yb[TM ? HR : 1];   // TM: the chunk's forward values of this lane
+    // TM with tm_cw < N: rows tm_cw .. of each line in shared memory after the
+    // ring, [warp][row - tm_cw][32]
+    constexpr size_t kYsOff = ((size_t)NB * kTile * sizeof(T) + (TMA ? (size_t)NB * kQ * sizeof(Quad<T>) : 0) +
+                               8 * NB + 16 + 15) / 16 * 16;
+    const int ys_rows = TM ? max(0, nchunk * HR - tm_cw) : 0;
+    float *ysw = reinterpret_cast<float *>(smem_raw + kYsOff) + (size_t)warp * ys_rows * 32 + lane;
     if constexpr (TMA) {
         if (threadIdx.x < NB) mbar_init(mbar + threadIdx.x, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -1193,12 +1202,21 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
         }
         if constexpr (TM) {
             __syncwarp();
-            if (GW_OK_I(l0 + HR - 1, tm_cw, 115)) {
-                if constexpr (HR == 8) {
-                    tm_st8(taddr + l0, yb);
-                } else {
-                    tm_st16(taddr + l0, yb);
-                    if constexpr (HR == 32) tm_st16(taddr + l0 + 16, yb + 16);
+            if (l0 < tm_cw) {
+                // columns l0 .. l0 + HR - 1 of this lane (tm_cw is a multiple of HR)
+                if (GW_OK_I(l0 + HR - 1, tm_cw, 115)) {
+                    if constexpr (HR == 8) {
+                        tm_st8(taddr + l0, yb);
+                    } else {
+                        tm_st16(taddr + l0, yb);
+                        if constexpr (HR == 32) tm_st16(taddr + l0 + 16, yb + 16);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < HR; ++r) {
+                    float *p = ysw + (size_t)(l0 - tm_cw + r) * 32;
+                    if (GW_OK_D(p, smem_raw, 117)) *p = yb[r];
                 }
             }
         }
@@ -1214,16 +1232,28 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                 int cb = (N - 2) >> 4;
                 float cur[16], nxt[16];
                 T cuc[16], cun[16];
-                const bool cok = GW_OK_I(16 * cb + 15, tm_cw, 116);
-                if (cok) tm_ld16(taddr + 16 * cb, cur);
+                // rows rb .. rb + 15 from TMEM or, at and beyond tm_cw, from
+                // shared memory (tm_cw is a multiple of 16)
+                auto load_batch = [&](int rb, float *v) {
+                    if (rb < tm_cw) {
+                        if (GW_OK_I(rb + 15, tm_cw, 116)) tm_ld16(taddr + rb, v);
+                        return;
+                    }
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const float *p = ysw + (size_t)(rb - tm_cw + j) * 32;
+                        v[j] = GW_OK_D(p, smem_raw, 118) ? *p : 0.f;
+                    }
+                };
+                load_batch(16 * cb, cur);
 #pragma unroll
                 for (int j = 0; j < 16; ++j)
                     cuc[j] = 16 * cb + j < N && GW_OK_G(cuf + 16 * cb + j, 110) ? __ldg(cuf + 16 * cb + j) : T(0);
-                if (cok) tm_wait_ld(cur);
+                tm_wait_ld(cur);   // (no TMEM load pending: returns at once)
                 for (;;) {
                     const int r0 = 16 * cb;
                     if (cb > 0) {
-                        tm_ld16(taddr + r0 - 16, nxt);
+                        load_batch(r0 - 16, nxt);
 #pragma unroll
                         for (int j = 0; j < 16; ++j)
                             cun[j] = GW_OK_G(cuf + r0 - 16 + j, 110) ? __ldg(cuf + r0 - 16 + j) : T(0);
@@ -1957,6 +1987,29 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
     if constexpr (sizeof(T) == 4) {
         // forward values in TMEM where the block's lines fit the SM's columns
         const int cw = tm && map && qmap ? tm_columns(xlines ? c->nx : c->ny, HW) : 0;
+        if constexpr (HW == 4 && HR == 16) {
+            // rows 0..127 in TMEM, the rest in the block's shared memory (ring
+            // of two), where that keeps more blocks per SM at work than whole
+            // lines in TMEM (512 / cw blocks): e.g. 205-row lines, 3 against 2
+            const int N = xlines ? c->nx : c->ny;
+            if (cw > 128 && c->half_split && c->smem_per_sm > 0) {
+                const size_t ys = (size_t)HW * (((N + HR - 1) / HR) * HR - 128) * 32 * sizeof(float);
+                const size_t sm2 = (tma_smem<HW, HR, 2>() + 15) / 16 * 16 + ys;
+                const int fit = c->smem_per_sm / (int)(sm2 + 1024);
+                if (std::min(4, fit) > 512 / cw) {
+                    const CUtensorMap &qm = *qmap;
+                    if (xlines)
+                        k_half_tile<T, true, HW, HR, 2, true, true><<<grid, 32 * HW, sm2, st>>>(
+                            dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz,
+                            c->countz, mb, me, *map, qm, c->d_err, 128);
+                    else
+                        k_half_tile<T, false, HW, HR, 2, true, true><<<grid, 32 * HW, sm2, st>>>(
+                            dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz,
+                            c->countz, mb, me, *map, qm, c->d_err, 128);
+                    return;
+                }
+            }
+        }
         if (cw > 0) {
             const CUtensorMap &qm = *qmap;
             if (xlines)
@@ -2101,6 +2154,17 @@ cudaError_t half_attr() {
 template <typename T>
 cudaError_t half_attrs() {
     cudaError_t e;
+    if constexpr (sizeof(T) == 4) {
+        // the split TMEM / shared-memory form takes up to the per-block maximum
+        int dev = 0, mx = 0;
+        if ((e = cudaGetDevice(&dev)) ||
+            (e = cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) ||
+            (e = cudaFuncSetAttribute(k_half_tile<float, true, 4, 16, 2, true, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) ||
+            (e = cudaFuncSetAttribute(k_half_tile<float, false, 4, 16, 2, true, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mx)))
+            return e;
+    }
     if ((e = half_attr<T, 8, 16, kTileNB[1]>()) != cudaSuccess ||
         (e = half_attr<T, 4, 16, kTileNB[0]>()) != cudaSuccess ||
         (e = half_attr<T, 8, 8, kTileNB[2]>()) != cudaSuccess ||
@@ -2305,6 +2369,12 @@ int gw_fused_prepare(gw_ctx *c) {
     // keeps them in global memory)
     const char *hg = std::getenv("GW_HALF_GLOBAL");
     c->half_tmem = !(hg && *hg && *hg != '0');
+    // rows beyond 128 in shared memory where that runs more blocks per SM
+    // (GW_HALF_TMEM_SPLIT=0 keeps whole lines in TMEM)
+    const char *hs = std::getenv("GW_HALF_TMEM_SPLIT");
+    c->half_split = !(hs && *hs == '0');
+    if ((e = cudaDeviceGetAttribute(&c->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device)))
+        return gw_cuda_fail(e, "cudaDeviceGetAttribute(shared memory per SM)");
 
     return GW_OK;
 }

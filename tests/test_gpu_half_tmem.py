@@ -5,7 +5,9 @@ Both evaluate the same recurrences in the same order, so the fields and
 outlet series must agree bitwise: every tiling, in-line and overlapped steps,
 lines of 36..88 rows (partial chunks and partial backward batches), lines
 longer than 256 rows (the 8-line tilings then keep their values in global
-memory, the others take 512 TMEM columns), and the two benchmark wells."""
+memory, the others split them between 128 TMEM columns and shared memory),
+and the two benchmark wells (the large well's 205-row lines take the split
+form in tiling 0, the 2 mm well's 225-row lines whole-line TMEM)."""
 import numpy as np
 import pytest
 
