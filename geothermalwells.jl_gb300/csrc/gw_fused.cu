@@ -1077,12 +1077,21 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                                8 * NB + 16 + 15) / 16 * 16;
     const int ys_rows = TM ? max(0, nchunk * HR - tm_cw) : 0;
     float *ysw = reinterpret_cast<float *>(smem_raw + kYsOff) + (size_t)warp * ys_rows * 32 + lane;
+    // TM: the line's backward-sweep coefficients cu_l of the block's z-class,
+    // copied to shared memory while the forward sweep runs ([warp][row])
+    const int cu_rows = TM ? (N + 31) / 32 * 32 : 0;
+    T *cus = reinterpret_cast<T *>(smem_raw + kYsOff + (size_t)HW * ys_rows * 32 * sizeof(float)) +
+             (size_t)warp * cu_rows;
     if constexpr (TMA) {
         if (threadIdx.x < NB) mbar_init(mbar + threadIdx.x, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         __syncthreads();
         for (int b = 0; b < NB - 1 && b < nchunk; ++b) load_chunk(b, b);
         if constexpr (TM) {
+            const T *cub = fcu + ((size_t)zcb * nl + mc) * N;   // the block class's row of this line
+            for (int r = lane; r < cu_rows; r += 32)
+                tile_copy(cus + r, cub + r, r < N);
+            cp_async_commit();
             if (warp == 0) {
                 __syncwarp();
                 tm_alloc(tslot, tm_cols);
@@ -1226,6 +1235,14 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
         tm_wait_st();
         if (m < m_end) {
             const T *cuf = fcu + fb;
+            // cu_l from shared memory where every lane is of the block's class
+            cp_async_wait<0>();
+            __syncwarp();
+            const bool wq = __all_sync(0xffffffffu, qs_ok);
+            auto cu_at = [&](int l) -> T {
+                if (wq) return GW_OK_D(cus + l, smem_raw, 119) ? cus[l] : T(0);
+                return GW_OK_G(cuf + l, 110) ? __ldg(cuf + l) : T(0);
+            };
             if (kok && GW_OK_G(dl + (long long)(N - 1) * rst, 111)) __stcs(dl + (long long)(N - 1) * rst, y);
             T x = y;
             if (N >= 2) {
@@ -1248,7 +1265,7 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                 load_batch(16 * cb, cur);
 #pragma unroll
                 for (int j = 0; j < 16; ++j)
-                    cuc[j] = 16 * cb + j < N && GW_OK_G(cuf + 16 * cb + j, 110) ? __ldg(cuf + 16 * cb + j) : T(0);
+                    cuc[j] = 16 * cb + j < N ? cu_at(16 * cb + j) : T(0);
                 tm_wait_ld(cur);   // (no TMEM load pending: returns at once)
                 for (;;) {
                     const int r0 = 16 * cb;
@@ -1256,7 +1273,7 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                         load_batch(r0 - 16, nxt);
 #pragma unroll
                         for (int j = 0; j < 16; ++j)
-                            cun[j] = GW_OK_G(cuf + r0 - 16 + j, 110) ? __ldg(cuf + r0 - 16 + j) : T(0);
+                            cun[j] = cu_at(r0 - 16 + j);
                     }
                     T *pc = dl + (long long)r0 * rst;
                     if (r0 + 15 <= N - 2) {
@@ -1964,6 +1981,9 @@ constexpr size_t tma_smem() {
 // >= 32, the smallest allocation); 0 for blocks of fewer than four lines
 // (half of the TMEM lanes would stay unused) or whose slots would not fit the
 // SM's 512 columns: the forward values then go through global memory
+// shared memory of the TM half step's staged backward-sweep coefficients
+inline size_t tm_cu_smem(int N, int HW) { return (size_t)HW * ((N + 31) / 32 * 32) * sizeof(float); }
+
 inline int tm_columns(int N, int HW) {
     if (HW < 4) return 0;
     int cw = 32;
@@ -1994,7 +2014,7 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
             const int N = xlines ? c->nx : c->ny;
             if (cw > 128 && c->half_split && c->smem_per_sm > 0) {
                 const size_t ys = (size_t)HW * (((N + HR - 1) / HR) * HR - 128) * 32 * sizeof(float);
-                const size_t sm2 = (tma_smem<HW, HR, 2>() + 15) / 16 * 16 + ys;
+                const size_t sm2 = (tma_smem<HW, HR, 2>() + 15) / 16 * 16 + ys + tm_cu_smem(N, HW);
                 const int fit = c->smem_per_sm / (int)(sm2 + 1024);
                 if (std::min(4, fit) > 512 / cw) {
                     const CUtensorMap &qm = *qmap;
@@ -2012,12 +2032,13 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
         }
         if (cw > 0) {
             const CUtensorMap &qm = *qmap;
+            const size_t smt = (tma_smem<HW, HR, NB>() + 15) / 16 * 16 + tm_cu_smem(xlines ? c->nx : c->ny, HW);
             if (xlines)
-                k_half_tile<T, true, HW, HR, NB, true, true><<<grid, 32 * HW, tma_smem<HW, HR, NB>(), st>>>(
+                k_half_tile<T, true, HW, HR, NB, true, true><<<grid, 32 * HW, smt, st>>>(
                     dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
                     mb, me, *map, qm, c->d_err, cw);
             else
-                k_half_tile<T, false, HW, HR, NB, true, true><<<grid, 32 * HW, tma_smem<HW, HR, NB>(), st>>>(
+                k_half_tile<T, false, HW, HR, NB, true, true><<<grid, 32 * HW, smt, st>>>(
                     dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
                     mb, me, *map, qm, c->d_err, cw);
             return;
@@ -2139,11 +2160,13 @@ cudaError_t half_attr() {
         if ((e = cudaFuncSetAttribute(k_half_tile<T, true, HW, HR, NB, true>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, st)))
             return e;
+        // with the staged coefficients of lines up to 512 (4 lines) or 256 rows (8)
+        const int stm = (st + 15) / 16 * 16 + (int)tm_cu_smem(HW <= 4 ? 512 : 256, HW);
         if ((e = cudaFuncSetAttribute(k_half_tile<T, true, HW, HR, NB, true, true>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, st)))
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, stm)))
             return e;
         if ((e = cudaFuncSetAttribute(k_half_tile<T, false, HW, HR, NB, true, true>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, st)))
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, stm)))
             return e;
         return cudaFuncSetAttribute(k_half_tile<T, false, HW, HR, NB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     st);
