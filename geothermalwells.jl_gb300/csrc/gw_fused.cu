@@ -2007,6 +2007,13 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
     if constexpr (sizeof(T) == 4) {
         // forward values in TMEM where the block's lines fit the SM's columns
         const int cw = tm && map && qmap ? tm_columns(xlines ? c->nx : c->ny, HW) : 0;
+        // ... and where the whole half step (every line of the direction, over
+        // however many launches the step splits it into) has at least four
+        // rounds of the blocks an SM runs with them: with fewer, the last round
+        // leaves SMs idle for a block's whole line, and the global-memory form,
+        // five or more resident blocks per SM, does the step in fewer rounds
+        const long long full_blocks = (long long)grid.x * (((xlines ? c->ny : c->nx) + HW - 1) / HW);
+        auto enough = [&](int active) { return c->half_tm_force || full_blocks >= 4LL * active * c->sms; };
         if constexpr (HW == 4 && HR == 16) {
             // rows 0..127 in TMEM, the rest in the block's shared memory (ring
             // of two), where that keeps more blocks per SM at work than whole
@@ -2016,7 +2023,7 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
                 const size_t ys = (size_t)HW * (((N + HR - 1) / HR) * HR - 128) * 32 * sizeof(float);
                 const size_t sm2 = (tma_smem<HW, HR, 2>() + 15) / 16 * 16 + ys + tm_cu_smem(N, HW);
                 const int fit = c->smem_per_sm / (int)(sm2 + 1024);
-                if (std::min(4, fit) > 512 / cw) {
+                if (std::min(4, fit) > 512 / cw && enough(std::min(4, fit))) {
                     const CUtensorMap &qm = *qmap;
                     if (xlines)
                         k_half_tile<T, true, HW, HR, 2, true, true><<<grid, 32 * HW, sm2, st>>>(
@@ -2030,7 +2037,7 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
                 }
             }
         }
-        if (cw > 0) {
+        if (cw > 0 && enough(512 / (cw * ((HW + 3) / 4)))) {
             const CUtensorMap &qm = *qmap;
             const size_t smt = (tma_smem<HW, HR, NB>() + 15) / 16 * 16 + tm_cu_smem(xlines ? c->nx : c->ny, HW);
             if (xlines)
@@ -2396,6 +2403,10 @@ int gw_fused_prepare(gw_ctx *c) {
     // (GW_HALF_TMEM_SPLIT=0 keeps whole lines in TMEM)
     const char *hs = std::getenv("GW_HALF_TMEM_SPLIT");
     c->half_split = !(hs && *hs == '0');
+    // on-chip forward values also for half steps of fewer than four rounds of
+    // blocks (GW_HALF_TMEM_FORCE=1: the tests' small grids)
+    const char *hf = std::getenv("GW_HALF_TMEM_FORCE");
+    c->half_tm_force = hf && *hf && *hf != '0';
     if ((e = cudaDeviceGetAttribute(&c->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device)))
         return gw_cuda_fail(e, "cudaDeviceGetAttribute(shared memory per SM)");
 

@@ -141,6 +141,7 @@ struct gw_ctx {
     bool tma_ok = false;              // maps encoded (else the half step copies with cp.async)
     bool half_tmem = false;           // tensor-map half steps keep their forward values in TMEM
     bool half_split = false;          // ... rows beyond 128 in shared memory where that runs more blocks
+    bool half_tm_force = false;       // ... also for half steps of fewer than four rounds of blocks
     int smem_per_sm = 0;              // shared memory per SM (bytes)
     int *d_err = nullptr;             // set by a kernel whose bounded wait ran out
     int rock2w_per_sm[9] = {};        // resident blocks per SM of the window ROCK2 kernel, by LPT

@@ -2,7 +2,9 @@
 (TMEM; the default of the tensor-map half step) against the same kernel with
 the values stored to and reloaded from global memory (GW_HALF_GLOBAL=1).
 Both evaluate the same recurrences in the same order, so the fields and
-outlet series must agree bitwise: every tiling, in-line and overlapped steps,
+outlet series must agree bitwise (the on-chip runs set GW_HALF_TMEM_FORCE=1:
+without it a half step of fewer than four rounds of blocks keeps its values
+in global memory): every tiling, in-line and overlapped steps,
 lines of 36..88 rows (partial chunks and partial backward batches), lines
 longer than 256 rows (the 8-line tilings then keep their values in global
 memory, the others split them between 128 TMEM columns and shared memory),
@@ -46,8 +48,12 @@ def run(w, monkeypatch, global_y, tiling=None, overlap=None, nsteps=3):
     monkeypatch.delenv("GW_HALF_CPASYNC", raising=False)
     if global_y:
         monkeypatch.setenv("GW_HALF_GLOBAL", "1")
+        monkeypatch.delenv("GW_HALF_TMEM_FORCE", raising=False)
     else:
         monkeypatch.delenv("GW_HALF_GLOBAL", raising=False)
+        # on chip even where a half step has fewer than four rounds of blocks
+        # (every grid here but the large well's)
+        monkeypatch.setenv("GW_HALF_TMEM_FORCE", "1")
     c = create_cache(backend=GB300(precision="mixed"), gridx=w["gridx"], gridy=w["gridy"],
                      gridz=w["gridz"], materials=w["materials"], boreholes=w["boreholes"],
                      inlet_model=w["inlet_model"])
@@ -60,6 +66,22 @@ def run(w, monkeypatch, global_y, tiling=None, overlap=None, nsteps=3):
                 ROCK2(max_stages=100, eigen_est=eigen_estimator), dt=w["dt"])
     c.close()
     return sol
+
+
+def test_default_small_grid_equals_global(gwlib, monkeypatch):
+    """Without the override (the library's own choice of form for a grid of a
+    few thousand cells) the field is the global form's, bitwise."""
+    w = CASES["single"]()
+    monkeypatch.delenv("GW_HALF_CPASYNC", raising=False)
+    monkeypatch.delenv("GW_HALF_GLOBAL", raising=False)
+    monkeypatch.delenv("GW_HALF_TMEM_FORCE", raising=False)
+    c = create_cache(backend=GB300(precision="mixed"), gridx=w["gridx"], gridy=w["gridy"],
+                     gridz=w["gridz"], materials=w["materials"], boreholes=w["boreholes"],
+                     inlet_model=w["inlet_model"])
+    sol = solve(ODEProblem(rhs_diffusion_z, w["T0"], (0.0, 3 * w["dt"]), c),
+                ROCK2(max_stages=100, eigen_est=eigen_estimator), dt=w["dt"])
+    c.close()
+    assert np.array_equal(sol.u[-1], run(w, monkeypatch, global_y=True).u[-1])
 
 
 @pytest.mark.parametrize("name", list(CASES))
