@@ -61,7 +61,9 @@ def parse():
     p.add_argument("--kernels", action="store_true",
                    help="single-well workloads: only the per-kernel timing (each fused kernel "
                         "launched --steps times on the full grid, outside the step graph)")
-    p.add_argument("--tiling", type=int, default=-1, help="half-step tiling of the context (default: its own)")
+    p.add_argument("--tiling", type=int, default=-1,
+                   help="half-step tiling of the context, or of every ensemble design without autotuning "
+                        "(default: the context's own; the ensemble autotunes)")
     return p.parse_args()
 
 
@@ -556,7 +558,11 @@ def run_ensemble(args):
     # down for part of the designs (departure points above the surface at
     # high flow, divergence on fine z grids); the work per step is the same
     dt = args.dt if args.dt > 0 else 600.0
-    choice = ens.autotune(dt, reps=2)
+    if args.tiling >= 0:   # one tiling for every design, no autotuning
+        ens.set_tiling(args.tiling)
+        choice = [args.tiling] * len(designs)
+    else:
+        choice = ens.autotune(dt, reps=2)
     ens.step(dt, args.warmup)
     clocks = Clocks(0)
     ms_tuned = ens.step(dt, args.steps)
