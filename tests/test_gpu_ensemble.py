@@ -84,3 +84,42 @@ def test_device_initial_field_equals_host_field(precision, gwlib):
         assert np.array_equal(ca.get_field(), cb.get_field())
         assert np.array_equal(a.outlet_series(d, 3), b.outlet_series(d, 3))
     a.close(); b.close()
+
+
+def _refined_x(w, times):
+    """The design with every x interval split in two, `times` times."""
+    from geothermalwells_gb300.physics import initial_condition_thermal_gradient
+    gx = np.asarray(w["gridx"], dtype=np.float64)
+    for _ in range(times):
+        gx = np.sort(np.concatenate([gx, 0.5 * (gx[1:] + gx[:-1])]))
+    return dict(w, gridx=gx, T0=initial_condition_thermal_gradient(None, np.float64, gx, w["gridy"], w["gridz"],
+                                                                   T_surface=5.0, gradient=0.5))
+
+
+@pytest.mark.parametrize("tiling", [0, 1])
+def test_on_chip_half_steps_of_designs_running_at_once(tiling, gwlib, monkeypatch):
+    """Eight designs whose half steps keep their forward values in tensor
+    memory run at once on their own streams: their blocks share every SM's
+    512 TMEM columns (x-lines of 141 rows take the split form's 128 columns
+    per block, x-lines of 481 rows all 512 with the 4-line tiling, so blocks
+    of different designs wait for each other's columns).  The
+    fields and outlet series equal those of the same ensemble with the
+    forward values in global memory, bitwise."""
+    ds = [_refined_x(W.small_case(n_layers=1 + q % 3, nbh=1 + q % 2, nz_cells=12 + 4 * q), 3 if q % 2 else 2)
+          for q in range(8)]
+    monkeypatch.delenv("GW_HALF_CPASYNC", raising=False)
+    monkeypatch.delenv("GW_HALF_TMEM_FORCE", raising=False)
+    monkeypatch.setenv("GW_HALF_GLOBAL", "1")
+    a = Ensemble(ds, precision="mixed")
+    monkeypatch.delenv("GW_HALF_GLOBAL")
+    monkeypatch.setenv("GW_HALF_TMEM_FORCE", "1")
+    b = Ensemble(ds, precision="mixed")
+    a.set_tiling(tiling)
+    b.set_tiling(tiling)
+    a.step(40.0, 3)
+    b.step(40.0, 3)
+    for d, (ca, cb) in enumerate(zip(a.caches, b.caches)):
+        assert np.all(np.isfinite(cb.get_field()))
+        assert np.array_equal(ca.get_field(), cb.get_field())
+        assert np.array_equal(a.outlet_series(d, 3), b.outlet_series(d, 3))
+    a.close(); b.close()
