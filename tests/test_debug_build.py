@@ -3,8 +3,10 @@ fused step's kernels check every global address against the registry of the
 contexts' allocations and every dynamic shared-memory access against the
 block's size, and a failed check comes back as GW_ERR_ARG (no trap).  This
 target runs the small-case parity cases (both precisions, in-line and
-overlapped steps), the reference's example and the 2 mm well, and every
-half-step tiling of the ensemble through that build in a child process.
+overlapped steps), the reference's example and the 2 mm well, every
+half-step tiling of the ensemble, and the mixed half steps with their forward
+values in tensor memory and shared memory through that build in a child
+process.
 
 Opt-in (it compiles a second library, about 2.5 minutes):
     GW_DEBUG_BUILD_TESTS=1 python -m pytest tests/test_debug_build.py -m gpu"""
@@ -66,6 +68,28 @@ for prec in ("fp64", "mixed"):
         e.set_tiling(t)
         e.step(40.0, 3)
         e.close()
+# the mixed half steps with their forward values on chip (forced on these
+# small grids): whole lines in TMEM, the split form (141-row lines), 512-column
+# blocks (281-row lines), and the 2 mm well
+import os
+os.environ["GW_HALF_TMEM_FORCE"] = "1"
+def refined(w, times):
+    from geothermalwells_gb300.physics import initial_condition_thermal_gradient
+    gx = np.asarray(w["gridx"], dtype=np.float64)
+    for _ in range(times):
+        gx = np.sort(np.concatenate([gx, 0.5 * (gx[1:] + gx[:-1])]))
+    return dict(w, gridx=gx, T0=initial_condition_thermal_gradient(None, np.float64, gx, w["gridy"], w["gridz"],
+                                                                   T_surface=5.0, gradient=0.5))
+for w in (W.small_case(n_layers=2, nbh=2), refined(W.small_case(nz_cells=20), 2),
+          refined(W.small_case(nz_cells=20), 3), W.single_well_2mm()):
+    for t in (0, 1, 3):
+        c = create_cache(backend=GB300(precision="mixed"), gridx=w["gridx"], gridy=w["gridy"],
+                         gridz=w["gridz"], materials=w["materials"], boreholes=w["boreholes"],
+                         inlet_model=w["inlet_model"])
+        _lib.check(L.gw_set_tiling(c.ctx, t))
+        solve(ODEProblem(rhs_diffusion_z, w["T0"], (0.0, 2 * w["dt"]), c),
+              ROCK2(max_stages=100, eigen_est=eigen_estimator), dt=w["dt"])
+        c.close()
 print("debug build: no bounds check failed")
 '''
 
