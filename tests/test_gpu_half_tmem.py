@@ -121,3 +121,45 @@ def test_long_lines(tiling, gwlib, monkeypatch):
     b = run(w, monkeypatch, global_y=False, tiling=tiling)
     assert np.array_equal(a.u[-1], b.u[-1])
     assert np.array_equal(a.T_outlet, b.T_outlet)
+
+
+def with_nx(w, n):
+    """The case with exactly n x-points: outer points dropped (alternating
+    ends; the pipes sit in the refined middle) or added beyond the ends at
+    0.2 m spacing."""
+    gx = list(np.asarray(w["gridx"], dtype=np.float64))
+    left = True
+    while len(gx) > n:
+        gx.pop(0 if left else -1)
+        left = not left
+    while len(gx) < n:
+        if left:
+            gx.insert(0, gx[0] - 0.2)
+        else:
+            gx.append(gx[-1] + 0.2)
+        left = not left
+    gx = np.asarray(gx)
+    w = dict(w)
+    w["gridx"] = gx
+    w["T0"] = W.initial_condition_thermal_gradient(None, np.float64, gx, w["gridy"], w["gridz"],
+                                                   T_surface=5.0, gradient=0.5)
+    return w
+
+
+@pytest.mark.parametrize("nz_cells", [12, 45])
+@pytest.mark.parametrize("nx", [20, 31, 33, 128, 129, 144, 208, 209, 256, 257])
+def test_line_lengths_at_the_edges(nx, nz_cells, gwlib, monkeypatch):
+    """x-lines whose length sits at the kernel's edges: one or two chunks,
+    partial backward batches, the split form's 128-row boundary (129: one row
+    in shared memory), its largest shared-memory share (208 / 209 rows) and
+    the step to 512 columns per block (256 / 257); nz = 13 and 46 levels
+    (one partial level block, two level blocks).  Tilings 0 (16-row chunks)
+    and 3 (32-row chunks); bitwise the global-memory form."""
+    w = with_nx(W.small_case(nz_cells=nz_cells), nx)
+    assert len(w["gridx"]) == nx
+    for tiling in (0, 3):
+        a = run(w, monkeypatch, global_y=True, tiling=tiling, nsteps=2)
+        b = run(w, monkeypatch, global_y=False, tiling=tiling, nsteps=2)
+        assert np.all(np.isfinite(b.u[-1]))
+        assert np.array_equal(a.u[-1], b.u[-1]), tiling
+        assert np.array_equal(a.T_outlet, b.T_outlet), tiling
