@@ -225,16 +225,18 @@ int gw_batch_step(gw_batch *b, double dt, int nsteps, int max_stages) {
     if (nsteps == 0) return GW_OK;
     std::vector<int> gen(n);
     for (int d = 0; d < n; ++d) gen[d] = b->ctx[d]->series_gen;
-    if (!b->graph || b->graph_dt != dt || b->graph_s != s || b->graph_gen != gen ||
+    if (!b->graph1 || b->graph_dt != dt || b->graph_s != s || b->graph_gen != gen ||
         b->graph_steps_cap < nsteps) {
         if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
         if (b->graph1) { cudaGraphExecDestroy(b->graph1); b->graph1 = nullptr; }
-        if ((rc = capture(b, dt, s, kSteps, &b->graph)) || (rc = capture(b, dt, s, 1, &b->graph1))) return rc;
+        if ((rc = capture(b, dt, s, 1, &b->graph1))) return rc;
         b->graph_dt = dt;
         b->graph_s = s;
         b->graph_gen = gen;
         b->graph_steps_cap = nsteps;
     }
+    // the kSteps-step graph only for calls that use it
+    if (nsteps >= kSteps && !b->graph && (rc = capture(b, dt, s, kSteps, &b->graph))) return rc;
     for (gw_ctx *c : b->ctx) GW_CUDA(cudaStreamSynchronize(c->stream));
     GW_CUDA(cudaEventRecord(b->ev0, b->stream));
     for (int k = 0; k + kSteps <= nsteps; k += kSteps) GW_CUDA(cudaGraphLaunch(b->graph, b->stream));
