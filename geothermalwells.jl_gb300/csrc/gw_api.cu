@@ -554,6 +554,7 @@ int gw_destroy(gw_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->graph_k) cudaGraphExecDestroy(c->graph_k);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->ev_a) cudaEventDestroy(c->ev_a);
@@ -842,6 +843,11 @@ int gw_rock2_stages(gw_ctx *c, double dt, int max_stages, int *stages, int *cove
     return gw_rock2_choose(dt, c->eigen_estimate, max_stages, stages, covered);
 }
 
+// steps per graph launch of gw_step for calls of at least that many (the
+// rest one step per launch): 8 steps trim the gaps between launches (large
+// well 0.5985 -> 0.5962 ms per step, 2 mm well 0.2456 -> 0.2425; 32: the same)
+constexpr int kGraphSteps = 8;
+
 int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
     if (!c) return gw_fail(GW_ERR_ARG, "NULL context");
     if (nsteps < 0) return gw_fail(GW_ERR_ARG, "nsteps must be >= 0");
@@ -864,30 +870,42 @@ int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
     if ((rc = gw_set_step_time(c, t0, dt))) return rc;
     c->t_now = t0 + nsteps * dt;
     if (nsteps == 0) return sync(c);
-    if (!c->graph || c->graph_dt != dt || c->graph_s != s || c->graph_gen != c->series_gen) {
-        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+    // one step, or kGraphSteps steps, per graph launch
+    auto capture = [&](int steps, cudaGraphExec_t *out) -> int {
         cudaGraph_t g;
         GW_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        int r3;
-        if (c->fused) {
-            r3 = gw_fused_step(c, dt, s);
-        } else {
-            int r1 = rock2_step(c, c->d_u, c->d_g1, c->d_temp, dt, s);
-            int r2 = r1 ? r1 : adi_adv(c, c->d_u, c->d_temp, dt);
-            r3 = r2 ? r2 : gw_launch_record(c, dt);
+        int r3 = GW_OK;
+        for (int k = 0; k < steps && r3 == GW_OK; ++k) {
+            if (c->fused) {
+                r3 = gw_fused_step(c, dt, s);
+            } else {
+                int r1 = rock2_step(c, c->d_u, c->d_g1, c->d_temp, dt, s);
+                int r2 = r1 ? r1 : adi_adv(c, c->d_u, c->d_temp, dt);
+                r3 = r2 ? r2 : gw_launch_record(c, dt);
+            }
         }
         cudaError_t e = cudaStreamEndCapture(c->stream, &g);
         if (r3) { if (e == cudaSuccess) cudaGraphDestroy(g); return r3; }
         if (e != cudaSuccess) return gw_cuda_fail(e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&c->graph, g, 0);
+        e = cudaGraphInstantiate(out, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return gw_cuda_fail(e, "cudaGraphInstantiate");
+        return GW_OK;
+    };
+    if (!c->graph || c->graph_dt != dt || c->graph_s != s || c->graph_gen != c->series_gen) {
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+        if (c->graph_k) { cudaGraphExecDestroy(c->graph_k); c->graph_k = nullptr; }
+        if ((rc = capture(1, &c->graph))) return rc;
         c->graph_dt = dt;
         c->graph_s = s;
         c->graph_gen = c->series_gen;
     }
+    if (nsteps >= kGraphSteps && !c->graph_k && (rc = capture(kGraphSteps, &c->graph_k))) return rc;
     GW_CUDA(cudaEventRecord(c->ev0, c->stream));
-    for (int n = 0; n < nsteps; ++n) GW_CUDA(cudaGraphLaunch(c->graph, c->stream));
+    int n = 0;
+    if (c->graph_k)
+        for (; n + kGraphSteps <= nsteps; n += kGraphSteps) GW_CUDA(cudaGraphLaunch(c->graph_k, c->stream));
+    for (; n < nsteps; ++n) GW_CUDA(cudaGraphLaunch(c->graph, c->stream));
     GW_CUDA(cudaEventRecord(c->ev1, c->stream));
     if ((rc = sync(c)) || (rc = gw_debug_status(c->device)) || (rc = gw_fused_status(c))) return rc;
     float ms = 0.f;

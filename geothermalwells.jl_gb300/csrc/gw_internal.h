@@ -175,6 +175,7 @@ struct gw_ctx {
     int snap_next = 0;
     // graph cache for gw_step
     cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph_k = nullptr;   // several steps per launch (calls of at least that many)
     double graph_dt = -1.0;
     int graph_s = -1;
     int graph_gen = -1;               // series_gen the graph was captured with

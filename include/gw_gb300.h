@@ -196,7 +196,8 @@ int gw_lincomb(gw_ctx *ctx, double *dst_dev, int n, const double *coeffs,
 /* Advance u by nsteps fixed steps of size dt from time t0: per step one
  * ROCK2 step of rhs_diffusion_z! (stage count from the eigenvalue estimate,
  * src/solver.jl:495, capped at max_stages) then ADI_and_ADV_callback!.  The
- * step is captured once in a CUDA graph and replayed.  Records the outlet
+ * step is captured once in CUDA graphs (of one step, and of eight for calls
+ * of at least eight steps) and replayed.  Records the outlet
  * temperature and extracted heat after every step. */
 int gw_step(gw_ctx *ctx, double t0, double dt, int nsteps, int max_stages);
 /* Run the step's two pipe passes (and the x-lines through the pipes) on a
@@ -272,8 +273,9 @@ int gw_profile_kernels(gw_ctx *ctx, double dt, int reps, double *ms_out);
 /* Configuration 4 of the benchmark set (no single counterpart in the
  * reference, which runs one cache per solve): a batch advances the contexts
  * of many designs -- each created by gw_create with GW_PREC_MIXED or
- * GW_PREC_FP64 on one device -- with one CUDA-graph launch per step in
- * which the designs' fused steps run concurrently.  The contexts stay owned
+ * GW_PREC_FP64 on one device -- with CUDA-graph launches of 32 steps (one
+ * step for the remainder) in which the designs' fused steps run
+ * concurrently.  The contexts stay owned
  * by the caller and must outlive the batch; per-design state, outlet series
  * and energies are read with the single-context getters. */
 typedef struct gw_batch gw_batch;
