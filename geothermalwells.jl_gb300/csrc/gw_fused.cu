@@ -2284,9 +2284,11 @@ int fused_step(gw_ctx *c, double dt, int s) {
         if ((rc = launch_rock2<T>(c, s, ab, c->ncol_a))) return rc;
         GW_CUDA(cudaEventRecord(c->ev_a, s1));
         GW_CUDA(cudaStreamWaitEvent(s2, c->ev_a, 0));
+        // the step's record needs only the second pipe pass's outlet (and
+        // inlet) values, so it runs here, beside the other x-lines and ROCK2
         if ((rc = launch_pipe<T>(c, B.u, GW_DIR_Y, dt / 2, s2)) ||
             (rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2, c->jlo, c->jhi + 1, s2)) ||
-            (rc = launch_pipe<T>(c, B.temp, GW_DIR_X, dt / 2, s2)))
+            (rc = launch_pipe<T>(c, B.temp, GW_DIR_X, dt / 2, s2)) || (rc = gw_launch_record(c, dt, s2)))
             return rc;
         GW_CUDA(cudaEventRecord(c->ev_px, s2));
         if ((rc = launch_rock2<T>(c, s, ab + c->ncol_a, c->ncol_b)) ||
@@ -2294,8 +2296,7 @@ int fused_step(gw_ctx *c, double dt, int s) {
             (rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2, c->jhi + 1, c->ny, s1)))
             return rc;
         GW_CUDA(cudaStreamWaitEvent(s1, c->ev_px, 0));
-        if ((rc = launch_half<T>(c, B.u, B.temp, 0, dt / 2))) return rc;
-        return gw_launch_record(c, dt);
+        return launch_half<T>(c, B.u, B.temp, 0, dt / 2);
     }
     if ((rc = launch_rock2<T>(c, s))) return rc;
     if ((rc = launch_pipe<T>(c, B.u, GW_DIR_Y, dt / 2))) return rc;

@@ -242,7 +242,8 @@ int gw_launch_thomas(gw_ctx *c, double *U, const double *RHS, int dir);
 int gw_launch_advection(gw_ctx *c, double *phi, double dt, double t = 0.0);
 // T_in(t) of the context's schedule (host); the same formula as the device.
 double gw_schedule_at(const gw_ctx *c, double t);
-int gw_launch_record(gw_ctx *c, double dt);
+// on stream st (NULL: the context's stream)
+int gw_launch_record(gw_ctx *c, double dt, cudaStream_t st = nullptr);
 int gw_launch_check_finite(gw_ctx *c, const double *u, size_t n);
 int gw_launch_lincomb(gw_ctx *c, double *dst, int n, const double *w, const double *const *src);
 // u = col[k] in every column (col: nz device doubles)

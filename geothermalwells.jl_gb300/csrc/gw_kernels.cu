@@ -401,9 +401,9 @@ int gw_launch_advection(gw_ctx *c, double *phi, double dt, double t) {
     return GW_OK;
 }
 
-int gw_launch_record(gw_ctx *c, double dt) {
+int gw_launch_record(gw_ctx *c, double dt, cudaStream_t st) {
     int threads = ((c->nbh + 31) / 32) * 32;
-    k_record<<<1, threads, 0, c->stream>>>(c->d_series, c->d_energy, c->d_step_counter, c->d_outlet,
+    k_record<<<1, threads, 0, st ? st : c->stream>>>(c->d_series, c->d_energy, c->d_step_counter, c->d_outlet,
                                            c->d_bh, c->nbh, c->series_cap, dt,
                                            c->rho_c_water / 998.2, c->inlet_kind, c->inlet_param, c->d_inlet);
     GW_CUDA(cudaGetLastError());
