@@ -403,6 +403,8 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         if (ncol > 0) {
             c->jlo = *std::min_element(c->pipe_j.begin(), c->pipe_j.end());
             c->jhi = *std::max_element(c->pipe_j.begin(), c->pipe_j.end());
+            c->ilo = *std::min_element(c->pipe_i.begin(), c->pipe_i.end());
+            c->ihi = *std::max_element(c->pipe_i.begin(), c->pipe_i.end());
         }
         std::vector<int> ab;
         ab.reserve(order.size());

@@ -968,7 +968,7 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
                                                         int nz, int pz, int countz, int m_begin, int m_end,
                                                         const __grid_constant__ CUtensorMap tmap,
                                                         const __grid_constant__ CUtensorMap qmap, int *err,
-                                                        int tm_cw = 0) {
+                                                        int tm_cw = 0, int prow_lo = 0, int prow_hi = 0x7fffffff) {
     static_assert(!TMA || sizeof(T) == 4, "tensor-map tiles: float fields only");
     static_assert(TMA || NB == 2, "the cp.async path double-buffers");
     static_assert(!TM || (TMA && (HR == 8 || HR == 16 || HR == 32)), "TMEM forward values: TMA tiles of 8-32 rows");
@@ -1136,8 +1136,10 @@ __global__ void __launch_bounds__(32 * HW) k_half_tile(T *__restrict__ dst, cons
             if (qs_ok) return GW_OK_D(qsm + r, smem_raw, 114) ? qsm[r] : Quad<T>{};
             return GW_OK_G(qc + r, 104) ? qc[r] : Quad<T>{};
         };
-        if (l0 + HR <= N && !line_pipe) {
-            // full chunk, no pipe column on the line: straight-line rows
+        // pipe columns lie in rows prow_lo .. prow_hi of every line
+        const bool chunk_pipe = line_pipe && l0 + HR > prow_lo && l0 <= prow_hi;
+        if (l0 + HR <= N && !chunk_pipe) {
+            // full chunk, no pipe column in it: straight-line rows
 #pragma unroll
             for (int r0 = 0; r0 < HR; r0 += kHG) {
                 Quad<T> q[kHG];
@@ -2004,6 +2006,8 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
                  const CUtensorMap *qmap, bool tm) {
     static const CUtensorMap kNoMap = {};
     dim3 grid((c->nz + 31) / 32, (me - mb + HW - 1) / HW);
+    // rows along the lines that hold pipe columns (chunks outside take the fast path)
+    const int plo = xlines ? c->ilo : c->jlo, phi = xlines ? c->ihi : c->jhi;
     if constexpr (sizeof(T) == 4) {
         // forward values in TMEM where the block's lines fit the SM's columns
         const int cw = tm && map && qmap ? tm_columns(xlines ? c->nx : c->ny, HW) : 0;
@@ -2028,11 +2032,11 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
                     if (xlines)
                         k_half_tile<T, true, HW, HR, 2, true, true><<<grid, 32 * HW, sm2, st>>>(
                             dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz,
-                            c->countz, mb, me, *map, qm, c->d_err, 128);
+                            c->countz, mb, me, *map, qm, c->d_err, 128, plo, phi);
                     else
                         k_half_tile<T, false, HW, HR, 2, true, true><<<grid, 32 * HW, sm2, st>>>(
                             dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz,
-                            c->countz, mb, me, *map, qm, c->d_err, 128);
+                            c->countz, mb, me, *map, qm, c->d_err, 128, plo, phi);
                     return;
                 }
             }
@@ -2043,11 +2047,11 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
             if (xlines)
                 k_half_tile<T, true, HW, HR, NB, true, true><<<grid, 32 * HW, smt, st>>>(
                     dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
-                    mb, me, *map, qm, c->d_err, cw);
+                    mb, me, *map, qm, c->d_err, cw, plo, phi);
             else
                 k_half_tile<T, false, HW, HR, NB, true, true><<<grid, 32 * HW, smt, st>>>(
                     dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
-                    mb, me, *map, qm, c->d_err, cw);
+                    mb, me, *map, qm, c->d_err, cw, plo, phi);
             return;
         }
         if (map && qmap) {
@@ -2055,22 +2059,22 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
             if (xlines)
                 k_half_tile<T, true, HW, HR, NB, true><<<grid, 32 * HW, tma_smem<HW, HR, NB>(), st>>>(
                     dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
-                    mb, me, *map, qm, c->d_err);
+                    mb, me, *map, qm, c->d_err, 0, plo, phi);
             else
                 k_half_tile<T, false, HW, HR, NB, true><<<grid, 32 * HW, tma_smem<HW, HR, NB>(), st>>>(
                     dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz,
-                    mb, me, *map, qm, c->d_err);
+                    mb, me, *map, qm, c->d_err, 0, plo, phi);
             return;
         }
     }
     if (xlines)
         k_half_tile<T, true, HW, HR><<<grid, 32 * HW, smem, st>>>(
             dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz, mb, me,
-            kNoMap, kNoMap, c->d_err);
+            kNoMap, kNoMap, c->d_err, 0, plo, phi);
     else
         k_half_tile<T, false, HW, HR><<<grid, 32 * HW, smem, st>>>(
             dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz, c->countz, mb, me,
-            kNoMap, kNoMap, c->d_err);
+            kNoMap, kNoMap, c->d_err, 0, plo, phi);
 }
 
 template <typename T>

@@ -97,6 +97,7 @@ struct gw_ctx {
     // the pipes read) and then the rest (ncol_b), each sorted by profile.
     int *d_colorder_ab = nullptr;
     int ncol_a = 0, ncol_b = 0, jlo = -1, jhi = -1;
+    int ilo = -1, ihi = -1;           // columns (i) holding pipe columns
     bool overlap = false;
     cudaStream_t stream2 = nullptr;   // the pipe passes' stream inside the step graph
     cudaEvent_t ev_a = nullptr, ev_px = nullptr;
