@@ -607,7 +607,9 @@ inline dim3 chunk_grid(int kblocks, int nchunks) {
     return dim3(kblocks, std::min(nchunks, kChunkRows), (nchunks + kChunkRows - 1) / kChunkRows);
 }
 
-template <typename T>
+// PR columns per round (8: large well pipe pass 0.0596 -> 0.0544 ms, 2 mm
+// well 0.0437 -> 0.0402 ms against 4; 16: 0.0571 / 0.0415)
+template <typename T, int PR = 8>
 __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *__restrict__ part,
                                                     const T *__restrict__ src,
                                                     const int4 *__restrict__ chunks,
@@ -647,16 +649,17 @@ __global__ void __launch_bounds__(128) k_pipe_sweep(T *__restrict__ tp, double *
                     (GW_OK_G(cmt + t, 305) ? __ldg(cmt + t) : T(0)) * (xc - xm);
         return fma(hh, a, xc);
     };
-    // four columns per round: their loads are independent and overlap; the
+    // kPR columns per round: their loads are independent and overlap; the
     // sum still runs over the columns in order
+    constexpr int kPR = PR;
     double acc = 0.0;
     int q = C.y;
-    for (; q + 4 <= C.z; q += 4) {
-        T v[4];
+    for (; q + kPR <= C.z; q += kPR) {
+        T v[kPR];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = sweep(q + u);
+        for (int u = 0; u < kPR; ++u) v[u] = sweep(q + u);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kPR; ++u) {
             if (GW_OK_G(tp + (size_t)(q + u) * nz + k, 306)) tp[(size_t)(q + u) * nz + k] = v[u];
             acc += (double)v[u];
         }
