@@ -229,6 +229,8 @@ def run_ours(args):
     s, cov = ctypes.c_int(), ctypes.c_int()
     _lib.check(L.gw_rock2_stages(cache.ctx, dt, 100, ctypes.byref(s), ctypes.byref(cov)))
     cache.set_field(w["T0"])
+    if args.tiling >= 0:
+        _lib.check(L.gw_set_tiling(cache.ctx, args.tiling))
     # rock2 columns, 2 half steps, 2 x 3 pipe kernels, record; the overlapped
     # step splits ROCK2 in two launches and the x-lines in three
     info = _lib.Info()
@@ -320,7 +322,8 @@ def run_ours(args):
         "dtype": "f64" if args.precision == "fp64" else "f32 (f64 outlet and energy balance)", "data": "synthetic",
         "config": {"workload": w["name"], "cells": ncell, "dt_s": dt, "rock2_stages": s.value,
                    "precision": args.precision, "l2": "inputs larger than L2 (field %.0f MB)"
-                   % (ncell * 8 / 1e6), "parallelism": "replicas" if world > 1 else "single"},
+                   % (ncell * 8 / 1e6), "parallelism": "replicas" if world > 1 else "single",
+                   "half_step_tiling": int(info.tiling)},
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel_ms": kms,

@@ -2003,6 +2003,36 @@ inline const CUtensorMap *tile_map(const gw_ctx *c, const void *src, int xlines,
     return b < 0 ? nullptr : &c->tmaps[b][xlines ? 0 : 1][cfg];
 }
 
+// Where the mixed half step of HW-line x HR-row tensor-map tiles keeps its
+// forward values: 0 global memory, 1 whole lines in TMEM (*cw columns per
+// block), 2 the split form (rows 0..127 in TMEM, the rest in shared memory;
+// *sm2 bytes of shared memory per block).
+template <int HW, int HR>
+int half_tm_mode(const gw_ctx *c, int xlines, int *cw, size_t *sm2) {
+    const int N = xlines ? c->nx : c->ny;
+    // forward values in TMEM where the block's lines fit the SM's columns
+    *cw = tm_columns(N, HW);
+    // ... and where the whole half step (every line of the direction, over
+    // however many launches the step splits it into) has at least four
+    // rounds of the blocks an SM runs with them: with fewer, the last round
+    // leaves SMs idle for a block's whole line, and the global-memory form,
+    // five or more resident blocks per SM, does the step in fewer rounds
+    const long long full_blocks = (long long)((c->nz + 31) / 32) * (((xlines ? c->ny : c->nx) + HW - 1) / HW);
+    auto enough = [&](int active) { return c->half_tm_force || full_blocks >= 4LL * active * c->sms; };
+    if constexpr (HW == 4 && HR == 16) {
+        // rows 0..127 in TMEM, the rest in the block's shared memory (ring
+        // of two), where that keeps more blocks per SM at work than whole
+        // lines in TMEM (512 / cw blocks): e.g. 205-row lines, 3 against 2
+        if (*cw > 128 && c->half_split && c->smem_per_sm > 0) {
+            const size_t ys = (size_t)HW * (((N + HR - 1) / HR) * HR - 128) * 32 * sizeof(float);
+            *sm2 = (tma_smem<HW, HR, 2>() + 15) / 16 * 16 + ys + tm_cu_smem(N, HW);
+            const int fit = c->smem_per_sm / (int)(*sm2 + 1024);
+            if (std::min(4, fit) > 512 / *cw && enough(std::min(4, fit))) return 2;
+        }
+    }
+    return *cw > 0 && enough(512 / (*cw * ((HW + 3) / 4))) ? 1 : 0;
+}
+
 template <typename T, int HW, int HR, int NB>
 void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, const Quad<T> *hq,
                  const GwFactors<T> &f, const T *pp, size_t smem, int mb, int me, const CUtensorMap *map,
@@ -2012,39 +2042,24 @@ void half_launch(gw_ctx *c, cudaStream_t st, T *dst, const T *src, int xlines, c
     // rows along the lines that hold pipe columns (chunks outside take the fast path)
     const int plo = xlines ? c->ilo : c->jlo, phi = xlines ? c->ihi : c->jhi;
     if constexpr (sizeof(T) == 4) {
-        // forward values in TMEM where the block's lines fit the SM's columns
-        const int cw = tm && map && qmap ? tm_columns(xlines ? c->nx : c->ny, HW) : 0;
-        // ... and where the whole half step (every line of the direction, over
-        // however many launches the step splits it into) has at least four
-        // rounds of the blocks an SM runs with them: with fewer, the last round
-        // leaves SMs idle for a block's whole line, and the global-memory form,
-        // five or more resident blocks per SM, does the step in fewer rounds
-        const long long full_blocks = (long long)grid.x * (((xlines ? c->ny : c->nx) + HW - 1) / HW);
-        auto enough = [&](int active) { return c->half_tm_force || full_blocks >= 4LL * active * c->sms; };
+        int cw = 0;
+        size_t sm2 = 0;
+        const int mode = tm && map && qmap ? half_tm_mode<HW, HR>(c, xlines, &cw, &sm2) : 0;
         if constexpr (HW == 4 && HR == 16) {
-            // rows 0..127 in TMEM, the rest in the block's shared memory (ring
-            // of two), where that keeps more blocks per SM at work than whole
-            // lines in TMEM (512 / cw blocks): e.g. 205-row lines, 3 against 2
-            const int N = xlines ? c->nx : c->ny;
-            if (cw > 128 && c->half_split && c->smem_per_sm > 0) {
-                const size_t ys = (size_t)HW * (((N + HR - 1) / HR) * HR - 128) * 32 * sizeof(float);
-                const size_t sm2 = (tma_smem<HW, HR, 2>() + 15) / 16 * 16 + ys + tm_cu_smem(N, HW);
-                const int fit = c->smem_per_sm / (int)(sm2 + 1024);
-                if (std::min(4, fit) > 512 / cw && enough(std::min(4, fit))) {
-                    const CUtensorMap &qm = *qmap;
-                    if (xlines)
-                        k_half_tile<T, true, HW, HR, 2, true, true><<<grid, 32 * HW, sm2, st>>>(
-                            dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz,
-                            c->countz, mb, me, *map, qm, c->d_err, 128, plo, phi);
-                    else
-                        k_half_tile<T, false, HW, HR, 2, true, true><<<grid, 32 * HW, sm2, st>>>(
-                            dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz,
-                            c->countz, mb, me, *map, qm, c->d_err, 128, plo, phi);
-                    return;
-                }
+            if (mode == 2) {
+                const CUtensorMap &qm = *qmap;
+                if (xlines)
+                    k_half_tile<T, true, HW, HR, 2, true, true><<<grid, 32 * HW, sm2, st>>>(
+                        dst, src, pp, c->d_pipe_lx, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz,
+                        c->countz, mb, me, *map, qm, c->d_err, 128, plo, phi);
+                else
+                    k_half_tile<T, false, HW, HR, 2, true, true><<<grid, 32 * HW, sm2, st>>>(
+                        dst, src, pp, c->d_pipe_ly, c->d_zclass, hq, f.ib, f.cu, c->nx, c->ny, c->nz, c->pz,
+                        c->countz, mb, me, *map, qm, c->d_err, 128, plo, phi);
+                return;
             }
         }
-        if (cw > 0 && enough(512 / (cw * ((HW + 3) / 4)))) {
+        if (mode == 1) {
             const CUtensorMap &qm = *qmap;
             const size_t smt = (tma_smem<HW, HR, NB>() + 15) / 16 * 16 + tm_cu_smem(xlines ? c->nx : c->ny, HW);
             if (xlines)
@@ -2417,6 +2432,17 @@ int gw_fused_prepare(gw_ctx *c) {
     c->half_tm_force = hf && *hf && *hf != '0';
     if ((e = cudaDeviceGetAttribute(&c->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device)))
         return gw_cuda_fail(e, "cudaDeviceGetAttribute(shared memory per SM)");
+    // default tiling: 4 lines x 16 rows (0); where neither direction's half
+    // step of that tiling keeps its forward values on chip (fewer than four
+    // rounds of blocks), 8 lines x 8 rows with the values in global memory
+    // (9), whose blocks carry 8 lines beside 2 halo lines instead of 4
+    // (225 x 225 x 402: 0.227 against 0.237 ms per step)
+    if (c->tma_ok && c->half_tmem) {
+        int cw;
+        size_t sm2;
+        if (!half_tm_mode<4, 16>(c, 1, &cw, &sm2) && !half_tm_mode<4, 16>(c, 0, &cw, &sm2))
+            c->half_cfg = kGlobalCfg + 2;
+    }
 
     return GW_OK;
 }

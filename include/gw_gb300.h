@@ -220,7 +220,10 @@ int gw_set_mixed_options(gw_ctx *ctx, int flags);
 
 /* Half-step kernel of this context (0 .. GW_TILINGS-1, see GW_TILINGS); all
  * give the same field bitwise except the segmented tiling 6.  gw_create picks
- * the default (0); gw_get_info reports the setting (tiling). */
+ * 0, except for mixed contexts whose half steps of tiling 0 would keep their
+ * forward values in global memory (fewer than four rounds of blocks per
+ * half step): those start with 9 (8 lines x 8 rows, global memory).
+ * gw_get_info reports the setting (tiling). */
 int gw_set_tiling(gw_ctx *ctx, int tiling);
 /* Stage count gw_step uses for dt (and whether its interval covers dt*lambda). */
 int gw_rock2_stages(gw_ctx *ctx, double dt, int max_stages, int *stages, int *covered);

@@ -49,9 +49,34 @@ def test_column_kernel_limit_survives_a_smaller_context(gwlib):
 
 
 def test_fused_context_reports_fused(gwlib):
-    c = make(W.small_case(), "mixed")
+    c = make(W.small_case(), "fp64")
     i = info(c)
     assert i.fused == 1 and i.modular_reason == 0 and i.tiling == 0 and i.mixed_options == 0
+    c.close()
+
+
+def test_default_tiling(gwlib, monkeypatch):
+    """Mixed contexts start with tiling 0 (4 lines x 16 rows, forward values
+    on chip) where its half steps have at least four rounds of blocks, else
+    with tiling 9 (8 x 8, forward values in global memory); FP64 contexts
+    always with 0."""
+    monkeypatch.delenv("GW_HALF_TMEM_FORCE", raising=False)
+    monkeypatch.delenv("GW_HALF_GLOBAL", raising=False)
+    monkeypatch.delenv("GW_HALF_CPASYNC", raising=False)
+    c = make(W.small_case(), "mixed")          # 36 x 36 x 14: nine blocks per half step
+    assert info(c).fused == 1 and info(c).tiling == 9
+    c.close()
+    c = make(W.single_well_large(), "mixed")   # 63 level blocks x 52 line groups
+    assert info(c).tiling == 0
+    c.close()
+    monkeypatch.setenv("GW_HALF_TMEM_FORCE", "1")
+    c = make(W.small_case(), "mixed")
+    assert info(c).tiling == 0
+    c.close()
+    monkeypatch.delenv("GW_HALF_TMEM_FORCE")
+    monkeypatch.setenv("GW_HALF_GLOBAL", "1")  # the same tiling with its values in global memory
+    c = make(W.small_case(), "mixed")
+    assert info(c).tiling == 0
     c.close()
 
 
