@@ -412,7 +412,18 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
             const int j = q % c->ny;
             return ncol > 0 && j >= c->jlo - 1 && j <= c->jhi + 1;
         };
-        for (int q : order) if (in_a(q)) ab.push_back(q);
+        // within rows jlo-1..jhi+1: the pipe columns and their y-neighbours
+        // (what the y pipe pass reads) first, ncol_p of them
+        std::vector<char> in_p((size_t)c->nx * c->ny, 0);
+        for (int q = 0; q < ncol; ++q) {
+            const size_t col = (size_t)c->pipe_i[q] * c->ny + c->pipe_j[q];
+            in_p[col] = 1;
+            if (c->pipe_j[q] > 0) in_p[col - 1] = 1;
+            if (c->pipe_j[q] < c->ny - 1) in_p[col + 1] = 1;
+        }
+        for (int q : order) if (in_p[q]) ab.push_back(q);
+        c->ncol_p = (int)ab.size();
+        for (int q : order) if (in_a(q) && !in_p[q]) ab.push_back(q);
         c->ncol_a = (int)ab.size();
         for (int q : order) if (!in_a(q)) ab.push_back(q);
         c->ncol_b = (int)ab.size() - c->ncol_a;
@@ -421,7 +432,9 @@ int gw_create(const gw_desc *desc, gw_ctx **out) {
         c->overlap = ncol > 0 && 2 * (long long)c->ncol_a <= (long long)order.size();
         if ((e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking)) != cudaSuccess ||
             (e = cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming)) != cudaSuccess ||
-            (e = cudaEventCreateWithFlags(&c->ev_px, cudaEventDisableTiming)) != cudaSuccess)
+            (e = cudaEventCreateWithFlags(&c->ev_px, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&c->ev_p, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&c->ev_q, cudaEventDisableTiming)) != cudaSuccess)
             return fail(gw_cuda_fail(e, "stream / event"));
     }
     if ((rc = upload(c, &c->d_gz, c->gz)) || (rc = upload(c, &c->d_zclass, c->zclass)) ||
@@ -561,6 +574,8 @@ int gw_destroy(gw_ctx *c) {
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->ev_a) cudaEventDestroy(c->ev_a);
     if (c->ev_px) cudaEventDestroy(c->ev_px);
+    if (c->ev_p) cudaEventDestroy(c->ev_p);
+    if (c->ev_q) cudaEventDestroy(c->ev_q);
     if (c->stream2) { cudaStreamSynchronize(c->stream2); cudaStreamDestroy(c->stream2); }
     if (c->snap_stream) { cudaStreamSynchronize(c->snap_stream); cudaStreamDestroy(c->snap_stream); }
     for (int b = 0; b < 2; ++b) {
@@ -894,10 +909,73 @@ int gw_step(gw_ctx *c, double t0, double dt, int nsteps, int max_stages) {
         if (e != cudaSuccess) return gw_cuda_fail(e, "cudaGraphInstantiate");
         return GW_OK;
     };
+    // The overlapped step's two launch orders give the same state bitwise;
+    // which is faster depends on which stream's chain is the longer
+    // (205 x 205 x 2002: order 1 by 4%, 225 x 225 x 402: order 0 by 5%).  A
+    // new step size, stage count or setting times both as the graphs gw_step
+    // launches (kGraphSteps steps each; one-step graphs hide part of the
+    // difference): one warm-up launch of each, then three rounds with the
+    // order inside a round alternating, the best round counting (64 trial
+    // steps: 15 ms on 225 x 225 x 402, 37 ms on 205 x 205 x 2002).  The state
+    // is restored (field, outlet and energy values; the step counter
+    // restarts) and the faster graph kept.
+    auto tune_order = [&]() -> int {
+        const bool mix = mixed(c);
+        const size_t bytes = gw_field_slots(c) * (mix ? sizeof(float) : sizeof(double));
+        void *u = mix ? (void *)c->f_u : (void *)c->d_u, *save = mix ? (void *)c->f_g1 : (void *)c->d_g1;
+        std::vector<double> outl(c->nbh), energy(c->nbh);
+        GW_CUDA(cudaMemcpyAsync(save, u, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        GW_CUDA(cudaMemcpyAsync(outl.data(), c->d_outlet, c->nbh * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        GW_CUDA(cudaMemcpyAsync(energy.data(), c->d_energy, c->nbh * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+        cudaGraphExec_t g[2] = {nullptr, nullptr};
+        float best_ms[2] = {1e30f, 1e30f};
+        int r = GW_OK;
+        for (int o = 0; o < 2 && r == GW_OK; ++o) {
+            c->step_order = o;
+            r = capture(kGraphSteps, &g[o]);
+        }
+        cudaError_t e = cudaSuccess;
+        for (int o = 0; o < 2 && r == GW_OK && e == cudaSuccess; ++o) e = cudaGraphLaunch(g[o], c->stream);
+        for (int round = 0; round < 3 && r == GW_OK && e == cudaSuccess; ++round)
+            for (int q = 0; q < 2 && e == cudaSuccess; ++q) {
+                const int o = q ^ (round & 1);
+                float ms = 0.f;
+                if ((e = cudaEventRecord(c->ev0, c->stream)) != cudaSuccess) break;
+                e = cudaGraphLaunch(g[o], c->stream);
+                if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->stream);
+                if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+                best_ms[o] = std::min(best_ms[o], ms);
+            }
+        if (r == GW_OK && e != cudaSuccess) r = gw_cuda_fail(e, "timing the step orders");
+        const int best = best_ms[1] < best_ms[0] ? 1 : 0;
+        if (g[1 - best]) cudaGraphExecDestroy(g[1 - best]);
+        if (r != GW_OK) {
+            if (g[best]) cudaGraphExecDestroy(g[best]);
+            return r;
+        }
+        c->step_order = best;
+        c->graph_k = g[best];
+        GW_CUDA(cudaMemcpyAsync(u, save, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        GW_CUDA(cudaMemcpyAsync(c->d_outlet, outl.data(), c->nbh * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        GW_CUDA(cudaMemcpyAsync(c->d_energy, energy.data(), c->nbh * sizeof(double), cudaMemcpyHostToDevice,
+                                c->stream));
+        GW_CUDA(cudaMemsetAsync(c->d_step_counter, 0, sizeof(int), c->stream));
+        GW_CUDA(cudaStreamSynchronize(c->stream));
+        return capture(1, &c->graph);
+    };
     if (!c->graph || c->graph_dt != dt || c->graph_s != s || c->graph_gen != c->series_gen) {
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
         if (c->graph_k) { cudaGraphExecDestroy(c->graph_k); c->graph_k = nullptr; }
-        if ((rc = capture(1, &c->graph))) return rc;
+        // timed again for a new step size, stage count or setting (each
+        // setter resets graph_dt), not for a longer outlet series alone
+        const bool retime = c->graph_dt != dt || c->graph_s != s;
+        if (c->fused && c->overlap && c->step_order_fixed < 0 && retime) {
+            if ((rc = tune_order())) return rc;
+        } else if ((rc = capture(1, &c->graph))) {
+            return rc;
+        }
         c->graph_dt = dt;
         c->graph_s = s;
         c->graph_gen = c->series_gen;

@@ -1856,13 +1856,13 @@ inline int rock2_win_lpt(int nz, int s, int *nwin) {
 
 template <int LPT>
 int launch_rock2_win(gw_ctx *c, int s, int nwin, float *u, const float *czm, const float *czp,
-                     const float *fref, const int *order, long long ncols) {
+                     const float *fref, const int *order, long long ncols, cudaStream_t st) {
     auto kern = s == 3 ? k_rock2_win<LPT, kWinNB, true> : k_rock2_win<LPT, kWinNB, false>;
     const long long per_sm = c->rock2w_per_sm[LPT] > 0 ? c->rock2w_per_sm[LPT] : 1;
     const long long need = (ncols * nwin + kWinWarps - 1) / kWinWarps;   // one warp per window
     long long grid = std::min(per_sm * c->sms, need);
     grid = std::max(grid, (long long)(nwin + kWinWarps - 1) / kWinWarps);   // one whole set of windows
-    kern<<<(unsigned)grid, 32 * kWinWarps, win_smem(LPT), c->stream>>>(
+    kern<<<(unsigned)grid, 32 * kWinWarps, win_smem(LPT), st>>>(
         u, order, c->d_colprof, czm, czp, fref, c->f_stage, s, c->nz, c->pz, (int)ncols, nwin);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
@@ -1870,7 +1870,8 @@ int launch_rock2_win(gw_ctx *c, int s, int nwin, float *u, const float *czm, con
 
 template <typename T, bool INC>
 int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *fref,
-                   const int *order = nullptr, long long ncols = -1) {
+                   const int *order = nullptr, long long ncols = -1, cudaStream_t st = nullptr) {
+    if (!st) st = c->stream;
     if (!order) order = c->d_colorder;
     if (ncols < 0) ncols = (long long)c->nx * c->ny;
     if (ncols == 0) return GW_OK;
@@ -1878,26 +1879,26 @@ int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *
         int nwin = 0;
         const int wl = c->rock2_block ? 0 : rock2_win_lpt(c->nz, s, &nwin);
         switch (wl) {
-            case 4: return launch_rock2_win<4>(c, s, nwin, u, czm, czp, fref, order, ncols);
-            case 5: return launch_rock2_win<5>(c, s, nwin, u, czm, czp, fref, order, ncols);
-            case 6: return launch_rock2_win<6>(c, s, nwin, u, czm, czp, fref, order, ncols);
-            case 7: return launch_rock2_win<7>(c, s, nwin, u, czm, czp, fref, order, ncols);
-            case 8: return launch_rock2_win<8>(c, s, nwin, u, czm, czp, fref, order, ncols);
+            case 4: return launch_rock2_win<4>(c, s, nwin, u, czm, czp, fref, order, ncols, st);
+            case 5: return launch_rock2_win<5>(c, s, nwin, u, czm, czp, fref, order, ncols, st);
+            case 6: return launch_rock2_win<6>(c, s, nwin, u, czm, czp, fref, order, ncols, st);
+            case 7: return launch_rock2_win<7>(c, s, nwin, u, czm, czp, fref, order, ncols, st);
+            case 8: return launch_rock2_win<8>(c, s, nwin, u, czm, czp, fref, order, ncols, st);
             default: break;
         }
     }
     const int lpt = rock2_lpt(c->nz, sizeof(T) == 4);
     unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid ? ncols : c->rock2_grid);
     switch (lpt) {
-        case 2: k_rock2_reg<T, INC, 2><<<grid, c->rock2_nt, reg_smem<T>(2, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
-        case 4: k_rock2_reg<T, INC, 4><<<grid, c->rock2_nt, reg_smem<T>(4, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
-        case 5: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 5><<<grid, c->rock2_nt, reg_smem<T>(5, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
-        case 6: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 6><<<grid, c->rock2_nt, reg_smem<T>(6, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
-        case 7: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 7><<<grid, c->rock2_nt, reg_smem<T>(7, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
-        case 8: k_rock2_reg<T, INC, 8><<<grid, c->rock2_nt, reg_smem<T>(8, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
-        case 16: k_rock2_reg<T, INC, 16><<<grid, c->rock2_nt, reg_smem<T>(16, c->rock2_nt), c->stream>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 2: k_rock2_reg<T, INC, 2><<<grid, c->rock2_nt, reg_smem<T>(2, c->rock2_nt), st>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 4: k_rock2_reg<T, INC, 4><<<grid, c->rock2_nt, reg_smem<T>(4, c->rock2_nt), st>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 5: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 5><<<grid, c->rock2_nt, reg_smem<T>(5, c->rock2_nt), st>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 6: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 6><<<grid, c->rock2_nt, reg_smem<T>(6, c->rock2_nt), st>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 7: if constexpr (sizeof(T) == 4) k_rock2_reg<T, INC, 7><<<grid, c->rock2_nt, reg_smem<T>(7, c->rock2_nt), st>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 8: k_rock2_reg<T, INC, 8><<<grid, c->rock2_nt, reg_smem<T>(8, c->rock2_nt), st>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
+        case 16: k_rock2_reg<T, INC, 16><<<grid, c->rock2_nt, reg_smem<T>(16, c->rock2_nt), st>>>(u, order, c->d_colprof, czm, czp, fref, stage_table<T>(c), s, c->nz, c->pz, ncols); break;
         default:
-            k_rock2_col<T, INC><<<grid, 256, rock2_smem<T>(c->nz), c->stream>>>(u, c->d_colprof, czm, czp, fref,
+            k_rock2_col<T, INC><<<grid, 256, rock2_smem<T>(c->nz), st>>>(u, c->d_colprof, czm, czp, fref,
                                                                             c->d_stage, s, c->nz, c->pz, ncols);
     }
     GW_CUDA(cudaGetLastError());
@@ -1906,7 +1907,8 @@ int launch_rock2_t(gw_ctx *c, int s, T *u, const T *czm, const T *czp, const T *
 
 // GW_MIXED_ROCK2_F64: the column kernel with double stages over the float
 // field (double tables, the double A_z T_ref source), LPT by the double rule.
-int launch_rock2_f64(gw_ctx *c, int s, const int *order, long long ncols) {
+int launch_rock2_f64(gw_ctx *c, int s, const int *order, long long ncols, cudaStream_t st = nullptr) {
+    if (!st) st = c->stream;
     if (!order) order = c->d_colorder;
     if (ncols < 0) ncols = (long long)c->nx * c->ny;
     if (ncols == 0) return GW_OK;
@@ -1914,10 +1916,10 @@ int launch_rock2_f64(gw_ctx *c, int s, const int *order, long long ncols) {
     const unsigned grid = (unsigned)(ncols < (long long)c->rock2_grid64 ? ncols : c->rock2_grid64);
     const double *czm = c->c64.czm, *czp = c->c64.czp, *fr = c->d_fref64, *sc = c->d_stage;
     switch (lpt) {
-        case 2: k_rock2_reg<float, true, 2, double><<<grid, nt, reg_smem<float>(2, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
-        case 4: k_rock2_reg<float, true, 4, double><<<grid, nt, reg_smem<float>(4, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
-        case 8: k_rock2_reg<float, true, 8, double><<<grid, nt, reg_smem<float>(8, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
-        case 16: k_rock2_reg<float, true, 16, double><<<grid, nt, reg_smem<float>(16, nt), c->stream>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
+        case 2: k_rock2_reg<float, true, 2, double><<<grid, nt, reg_smem<float>(2, nt), st>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
+        case 4: k_rock2_reg<float, true, 4, double><<<grid, nt, reg_smem<float>(4, nt), st>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
+        case 8: k_rock2_reg<float, true, 8, double><<<grid, nt, reg_smem<float>(8, nt), st>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
+        case 16: k_rock2_reg<float, true, 16, double><<<grid, nt, reg_smem<float>(16, nt), st>>>(c->f_u, order, c->d_colprof, czm, czp, fr, sc, s, c->nz, c->pz, ncols); break;
         default: return gw_fail(GW_ERR_UNSUPPORTED, "GW_MIXED_ROCK2_F64 supports nz <= 4096");
     }
     GW_CUDA(cudaGetLastError());
@@ -1925,14 +1927,14 @@ int launch_rock2_f64(gw_ctx *c, int s, const int *order, long long ncols) {
 }
 
 template <typename T>
-int launch_rock2(gw_ctx *c, int s, const int *order = nullptr, long long ncols = -1) {
-    if (sizeof(T) == 4 && (c->mixed_flags & GW_MIXED_ROCK2_F64)) return launch_rock2_f64(c, s, order, ncols);
+int launch_rock2(gw_ctx *c, int s, const int *order = nullptr, long long ncols = -1, cudaStream_t st = nullptr) {
+    if (sizeof(T) == 4 && (c->mixed_flags & GW_MIXED_ROCK2_F64)) return launch_rock2_f64(c, s, order, ncols, st);
     Bufs<T> B = bufs<T>(c);
     if (sizeof(T) == 4)
         return launch_rock2_t<float, true>(c, s, (float *)B.u, (const float *)B.ct->czm,
-                                           (const float *)B.ct->czp, (const float *)B.fref, order, ncols);
+                                           (const float *)B.ct->czp, (const float *)B.fref, order, ncols, st);
     return launch_rock2_t<double, false>(c, s, (double *)B.u, (const double *)B.ct->czm,
-                                         (const double *)B.ct->czp, nullptr, order, ncols);
+                                         (const double *)B.ct->czp, nullptr, order, ncols, st);
 }
 
 // explicit sweep along edir at the pipe columns, outlet/annulus means, advection
@@ -2296,13 +2298,40 @@ int fused_step(gw_ctx *c, double dt, int s) {
     // the pipe values it used are still in pp: the in-line order
     const bool refine = sizeof(T) == 4 && (c->mixed_flags & GW_MIXED_REFINE);
     if (c->overlap && rock2_lpt(c->nz, sizeof(T) == 4) > 0 && !refine) {
-        // The pipe passes need only the rows around the pipes: ROCK2 first
-        // does the columns of rows jlo-1..jhi+1; then a second stream runs
-        // the y pipe pass, the x-lines through the pipes (rows jlo..jhi) and
-        // the x pipe pass while the first finishes ROCK2 and the other
-        // x-lines; the y-lines wait for both.
+        // The pipe passes need only the rows around the pipes.  Order 0:
+        // ROCK2 first does the columns of rows jlo-1..jhi+1; then a second
+        // stream runs the y pipe pass, the x-lines through the pipes (rows
+        // jlo..jhi) and the x pipe pass while the first finishes ROCK2 and
+        // the other x-lines; the y-lines wait for both.  Order 1: the second
+        // stream starts at once with ROCK2 of the pipe columns and their
+        // y-neighbours (all the y pipe pass reads) and the y pipe pass, while
+        // the first does ROCK2 of the rest of rows jlo-1..jhi+1 (which the
+        // x-lines through the pipes wait for), then of the other rows, then
+        // the other x-lines (which wait for the pipe columns' ROCK2).  Both
+        // give the same field bitwise; gw_step times them.
         const int *ab = c->d_colorder_ab;
         cudaStream_t s1 = c->stream, s2 = c->stream2;
+        if (c->step_order == 1) {
+            GW_CUDA(cudaEventRecord(c->ev_a, s1));
+            GW_CUDA(cudaStreamWaitEvent(s2, c->ev_a, 0));
+            if ((rc = launch_rock2<T>(c, s, ab, c->ncol_p, s2))) return rc;
+            GW_CUDA(cudaEventRecord(c->ev_p, s2));
+            if ((rc = launch_pipe<T>(c, B.u, GW_DIR_Y, dt / 2, s2))) return rc;
+            if ((rc = launch_rock2<T>(c, s, ab + c->ncol_p, c->ncol_a - c->ncol_p, s1))) return rc;
+            GW_CUDA(cudaEventRecord(c->ev_q, s1));
+            GW_CUDA(cudaStreamWaitEvent(s2, c->ev_q, 0));
+            if ((rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2, c->jlo, c->jhi + 1, s2)) ||
+                (rc = launch_pipe<T>(c, B.temp, GW_DIR_X, dt / 2, s2)) || (rc = gw_launch_record(c, dt, s2)))
+                return rc;
+            GW_CUDA(cudaEventRecord(c->ev_px, s2));
+            if ((rc = launch_rock2<T>(c, s, ab + c->ncol_a, c->ncol_b, s1))) return rc;
+            GW_CUDA(cudaStreamWaitEvent(s1, c->ev_p, 0));
+            if ((rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2, 0, c->jlo, s1)) ||
+                (rc = launch_half<T>(c, B.temp, B.u, 1, dt / 2, c->jhi + 1, c->ny, s1)))
+                return rc;
+            GW_CUDA(cudaStreamWaitEvent(s1, c->ev_px, 0));
+            return launch_half<T>(c, B.u, B.temp, 0, dt / 2);
+        }
         if ((rc = launch_rock2<T>(c, s, ab, c->ncol_a))) return rc;
         GW_CUDA(cudaEventRecord(c->ev_a, s1));
         GW_CUDA(cudaStreamWaitEvent(s2, c->ev_a, 0));
@@ -2430,6 +2459,12 @@ int gw_fused_prepare(gw_ctx *c) {
     // blocks (GW_HALF_TMEM_FORCE=1: the tests' small grids)
     const char *hf = std::getenv("GW_HALF_TMEM_FORCE");
     c->half_tm_force = hf && *hf && *hf != '0';
+    // launch order of the overlapped step: chosen by timing (unset), or fixed
+    // (GW_STEP_ORDER=0: the pipe rows' ROCK2 columns first; 1: the pipe
+    // columns and their y-neighbours first on the second stream)
+    const char *so = std::getenv("GW_STEP_ORDER");
+    c->step_order_fixed = so && (*so == '0' || *so == '1') ? *so - '0' : -1;
+    if (c->step_order_fixed >= 0) c->step_order = c->step_order_fixed;
     if ((e = cudaDeviceGetAttribute(&c->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device)))
         return gw_cuda_fail(e, "cudaDeviceGetAttribute(shared memory per SM)");
     // default tiling: 4 lines x 16 rows (0); where neither direction's half

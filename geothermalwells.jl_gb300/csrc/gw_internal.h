@@ -97,10 +97,13 @@ struct gw_ctx {
     // the pipes read) and then the rest (ncol_b), each sorted by profile.
     int *d_colorder_ab = nullptr;
     int ncol_a = 0, ncol_b = 0, jlo = -1, jhi = -1;
+    int ncol_p = 0;   // of the ncol_a: the pipe columns and their y-neighbours, first
+    int step_order = 0;           // launch order of the overlapped step (0 / 1, gw_fused.cu fused_step)
+    int step_order_fixed = -1;    // -1: chosen by timing when gw_step captures a new graph
     int ilo = -1, ihi = -1;           // columns (i) holding pipe columns
     bool overlap = false;
     cudaStream_t stream2 = nullptr;   // the pipe passes' stream inside the step graph
-    cudaEvent_t ev_a = nullptr, ev_px = nullptr;
+    cudaEvent_t ev_a = nullptr, ev_px = nullptr, ev_p = nullptr, ev_q = nullptr;
     int *d_pipe_i = nullptr, *d_pipe_j = nullptr, *d_pipe_b = nullptr;
     GwBhDev *d_bh = nullptr;
     GwCoefTables<double> c64;
