@@ -601,6 +601,7 @@ int gw_get_info(gw_ctx *c, gw_info_t *o) {
     o->modular_reason = c->modular_reason;
     o->tiling = c->half_cfg;
     o->mixed_options = c->mixed_flags;
+    o->step_order = c->step_order;
     return GW_OK;
 }
 

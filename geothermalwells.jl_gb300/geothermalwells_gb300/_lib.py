@@ -62,7 +62,7 @@ class Info(ctypes.Structure):
                  "n_zclass", "n_profiles")] + \
                [("eigen_estimate", ctypes.c_double), ("device_bytes", ctypes.c_longlong),
                 ("overlap", ctypes.c_int), ("fused", ctypes.c_int), ("modular_reason", ctypes.c_int),
-                ("tiling", ctypes.c_int), ("mixed_options", ctypes.c_int)]
+                ("tiling", ctypes.c_int), ("mixed_options", ctypes.c_int), ("step_order", ctypes.c_int)]
 
 
 SIGNATURES = {

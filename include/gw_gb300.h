@@ -99,6 +99,10 @@ typedef struct gw_info_t {
     int modular_reason;              /* why fused == 0: GW_MODULAR_* bits, 0 when fused */
     int tiling;                      /* half-step kernel (gw_set_tiling) */
     int mixed_options;               /* GW_MIXED_* flags (gw_set_mixed_options) */
+    int step_order;                  /* launch order of the overlapped step that gw_step
+                                        chose by timing for the last step size: 0 ROCK2
+                                        of the pipe rows first, 1 of the pipe columns
+                                        first on the second stream (same state bitwise) */
 } gw_info_t;
 
 /* gw_info_t.modular_reason bits */
@@ -198,7 +202,11 @@ int gw_lincomb(gw_ctx *ctx, double *dst_dev, int n, const double *coeffs,
  * src/solver.jl:495, capped at max_stages) then ADI_and_ADV_callback!.  The
  * step is captured once in CUDA graphs (of one step, and of eight for calls
  * of at least eight steps) and replayed.  Records the outlet
- * temperature and extracted heat after every step. */
+ * temperature and extracted heat after every step.  When the step runs its
+ * pipe passes on a second stream (gw_info_t.overlap), the first call for a
+ * new step size (or after a setter) times the step's two launch orders on 64
+ * trial steps, restores the field, outlet and energy values, and keeps the
+ * faster order (gw_info_t.step_order); both give the same state bitwise. */
 int gw_step(gw_ctx *ctx, double t0, double dt, int nsteps, int max_stages);
 /* Run the step's two pipe passes (and the x-lines through the pipes) on a
  * second stream, overlapping the rest of the step (on = 1; the default where

@@ -138,6 +138,7 @@ struct GwInfo
     eigen_estimate::Cdouble
     device_bytes::Clonglong
     overlap::Cint; fused::Cint; modular_reason::Cint; tiling::Cint; mixed_options::Cint
+    step_order::Cint
 end
 
 struct AdjointInfo
