@@ -410,10 +410,18 @@ __global__ void __launch_bounds__(256, LPT <= 8 ? (sizeof(C) == 4 ? 3 : 2) : 1) 
 // their levels at least s from an interior edge.  Window w starts at level
 // w (W - 2 s); the last window reaches the column's end (padding levels are
 // zero-filled with zero coefficients, as in k_rock2_reg).
-// Warps are independent: warp g of the grid owns window g % nwin of its
-// columns (every (g / nwin)-th of the profile-sorted order, so the window's
-// coefficient rows stay in registers), and streams them through a private
-// ring of NB staging buffers (NB - 1 windows in flight) with cp.async.
+// A block holds whole column slots: blockDim / (32 nwin) slots of nwin
+// warps (nwin <= 8), warp wib owning window wib % nwin of its slot's
+// columns (every slots-th of the profile-sorted order, so the window's
+// coefficient rows stay in registers), streamed through a private ring of NB
+// staging buffers (NB - 1 windows in flight) with cp.async.  The halo levels
+// a window reads are levels its neighbour windows store, in place, so a
+// slot's warps meet at a named barrier once per column, after every
+// window's copy of that column has landed and before any window stores it.
+// (Without it a window fetching late, e.g. in a block started after its
+// neighbour's when another stream's kernels held the SMs, read stored values
+// as halo.  An mbarrier per ring buffer, arrived on when a copy lands and
+// waited on just before the store, measured no faster.)
 // S3: the instance for s = 3 (one recurrence stage, no g_{j-2} to keep).
 template <int LPT, int NB, bool S3>
 __global__ void __launch_bounds__(256, 3) k_rock2_win(float *__restrict__ u, const int *__restrict__ order,
@@ -427,11 +435,11 @@ __global__ void __launch_bounds__(256, 3) k_rock2_win(float *__restrict__ u, con
     constexpr int WS = W + W / 32;   // padded slots of one staging buffer
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int g = blockIdx.x * (blockDim.x >> 5) + wib;
-    const int slots = gridDim.x * (blockDim.x >> 5) / nwin;   // column slots
-    if (g >= slots * nwin) return;   // warps beyond the last whole set of windows
-    const int w = g % nwin;
-    const int slot = g / nwin;
+    const int spb = (blockDim.x >> 5) / nwin;               // column slots per block (blockDim: whole slots)
+    const int slots = gridDim.x * spb;
+    const int w = wib % nwin;
+    const int slot = blockIdx.x * spb + wib / nwin;
+    const unsigned bar_id = 1 + wib / nwin, bar_n = 32 * nwin;   // the slot's named barrier
     float *ring = reinterpret_cast<float *>(smem_raw) + (size_t)wib * NB * WS;
     const int ws = w * (W - 2 * s);                      // first level of the window
     const int lo = w == 0 ? 0 : ws + s;                  // stored levels [lo, hi)
@@ -506,6 +514,8 @@ __global__ void __launch_bounds__(256, 3) k_rock2_win(float *__restrict__ u, con
         }
         cp_async_wait<NB - 1>();
         __syncwarp();
+        // every window of the slot holds this column before any stores it
+        if (nwin > 1) asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(bar_n) : "memory");
         float *st = ring + (size_t)buf * WS;
         float F0[LPT], prev[LPT], cur[LPT];
         float left, right;
@@ -1839,7 +1849,9 @@ inline size_t win_smem(int lpt) { return (size_t)kWinWarps * kWinNB * (32 * lpt 
 
 // Levels per lane and window count of k_rock2_win for nz levels and s stages:
 // among 4..8 levels per lane, the fewest padded levels (windows x W); 0 when
-// the halo (s levels per interior edge) would exceed a quarter of the window.
+// the halo (s levels per interior edge) would exceed a quarter of the window
+// or a column would need more windows than a block has warps (its windows
+// share a block; deeper columns take the block kernel).
 inline int rock2_win_lpt(int nz, int s, int *nwin) {
     int best = 0, bn = 0;
     long long bw = 0;
@@ -1847,7 +1859,7 @@ inline int rock2_win_lpt(int nz, int s, int *nwin) {
         const int W = 32 * L;
         if (8 * s > W) continue;
         const int n = nz <= W ? 1 : 1 + (nz - W + (W - 2 * s) - 1) / (W - 2 * s);
-        if (n > 64) continue;
+        if (n > kWinWarps) continue;
         if (!best || (long long)n * W < bw) { best = L; bn = n; bw = (long long)n * W; }
     }
     *nwin = bn;
@@ -1858,11 +1870,15 @@ template <int LPT>
 int launch_rock2_win(gw_ctx *c, int s, int nwin, float *u, const float *czm, const float *czp,
                      const float *fref, const int *order, long long ncols, cudaStream_t st) {
     auto kern = s == 3 ? k_rock2_win<LPT, kWinNB, true> : k_rock2_win<LPT, kWinNB, false>;
-    const long long per_sm = c->rock2w_per_sm[LPT] > 0 ? c->rock2w_per_sm[LPT] : 1;
-    const long long need = (ncols * nwin + kWinWarps - 1) / kWinWarps;   // one warp per window
-    long long grid = std::min(per_sm * c->sms, need);
-    grid = std::max(grid, (long long)(nwin + kWinWarps - 1) / kWinWarps);   // one whole set of windows
-    kern<<<(unsigned)grid, 32 * kWinWarps, win_smem(LPT), st>>>(
+    // blocks of whole column slots: spb slots of nwin warps (nwin <= kWinWarps)
+    const int spb = kWinWarps / nwin, warps = spb * nwin;
+    // resident blocks per SM: those of kWinWarps warps, scaled to this size
+    const long long per_sm =
+        std::max(1LL, (long long)(c->rock2w_per_sm[LPT] > 0 ? c->rock2w_per_sm[LPT] : 1) * kWinWarps / warps);
+    const long long need = (ncols + spb - 1) / spb;
+    const long long grid = std::max(1LL, std::min(per_sm * c->sms, need));
+    const size_t smem = (size_t)warps * kWinNB * (32 * LPT + LPT) * sizeof(float);
+    kern<<<(unsigned)grid, 32 * warps, smem, st>>>(
         u, order, c->d_colprof, czm, czp, fref, c->f_stage, s, c->nz, c->pz, (int)ncols, nwin);
     GW_CUDA(cudaGetLastError());
     return GW_OK;
